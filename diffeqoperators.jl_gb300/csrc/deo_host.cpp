@@ -1,0 +1,1154 @@
+// deo_host.cpp -- host side of libdeo: operator and boundary-condition
+// constructors, the row-table compiler, plans and the C ABI (include/deo.h).
+//
+// The constructors restate DiffEqOperators.jl's (cited per function) so a
+// caller without Julia gets the same tables; a Julia caller passes its own
+// DerivativeOperator tables through deo_operator_from_tables instead.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/deo.h"
+#include "deo_internal.h"
+
+using deo::PlanDev;
+using deo::RowTabDev;
+using deo::TermDev;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static deo_status fail(deo_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+static deo_status fail(deo_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return s;
+}
+
+static deo_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? DEO_ERR_OOM : DEO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr, what)                         \
+    do {                                             \
+        cudaError_t e_ = (expr);                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+extern "C" const char* deo_last_error(void) { return g_err.c_str(); }
+extern "C" int deo_abi_version(void) { return DEO_ABI_VERSION; }
+
+// ---------------------------------------------------------------------------
+// Float64 ^ Int as Julia computes it (Base.pow_body, compensated squaring):
+// the operators scale their weights by 1/dx^d with this.
+// ---------------------------------------------------------------------------
+static double pow_int(double x, long n) {
+    if (n == 0) return 1.0;
+    if (n == 3) return x * x * x;
+    double y = 1.0, xnlo = 0.0, ynlo = 0.0;
+    if (n < 0) {
+        const double rx = 1.0 / x;
+        if (n == -2) return rx * rx;
+        if (std::isfinite(x)) xnlo = -std::fma(x, rx, -1.0) * rx;
+        x = rx;
+        n = -n;
+    }
+    while (n > 1) {
+        if (n & 1) {
+            const double err = std::fma(y, xnlo, x * ynlo);
+            const double hi = x * y;
+            ynlo = std::fma(x, y, -hi) + err;
+            y = hi;
+        }
+        const double err = x * 2 * xnlo;
+        const double hi = x * x;
+        xnlo = std::fma(x, x, -hi) + err;
+        x = hi;
+        n >>= 1;
+    }
+    const double err = std::fma(y, xnlo, x * ynlo);
+    return (std::isfinite(x) && std::isfinite(err)) ? std::fma(x, y, err) : x * y;
+}
+
+// ---------------------------------------------------------------------------
+// Fornberg weights (fornberg.jl:7-62): recurrence over the points, then the
+// centre entry absorbs the rounding residue of the weight sum.
+// ---------------------------------------------------------------------------
+static std::vector<double> fd_weights(int m, double x0, const std::vector<double>& x) {
+    const int n = (int)x.size();
+    const int w = m + 1;
+    std::vector<double> C((size_t)n * w, 0.0);  // C[row*w + order]
+    C[0] = 1.0;
+    double c1 = 1.0, c4 = x[0] - x0;
+    for (int i = 1; i < n; ++i) {
+        const int mn = std::min(i, m);
+        double c2 = 1.0;
+        const double c5 = c4;
+        c4 = x[i] - x0;
+        for (int j = 0; j < i; ++j) {
+            const double c3 = x[i] - x[j];
+            c2 *= c3;
+            if (j == i - 1) {
+                for (int s = mn; s >= 1; --s)
+                    C[(size_t)i * w + s] = c1 * ((double)s * C[(size_t)(i - 1) * w + s - 1] - c5 * C[(size_t)(i - 1) * w + s]) / c2;
+                C[(size_t)i * w] = -c1 * c5 * C[(size_t)(i - 1) * w] / c2;
+            }
+            for (int s = mn; s >= 1; --s)
+                C[(size_t)j * w + s] = (c4 * C[(size_t)j * w + s] - (double)s * C[(size_t)j * w + s - 1]) / c3;
+            C[(size_t)j * w] = c4 * C[(size_t)j * w] / c3;
+        }
+        c1 = c2;
+    }
+    std::vector<double> out(n);
+    for (int i = 0; i < n; ++i) out[i] = C[(size_t)i * w + m];
+    if (m != 0) {
+        double s = out[0];
+        for (int i = 1; i < n; ++i) s = s + out[i];
+        out[n / 2] -= s;
+    }
+    return out;
+}
+
+// ---------------------------------------------------------------------------
+// operators
+// ---------------------------------------------------------------------------
+struct deo_operator {
+    int d = 0, a = 0, len = 0, stl = 0, bstl = 0, bpc = 0, off = 0;
+    int wind = 0, uniform = 1, cfs = 1;
+    int n_st = 0, n_low = 0, n_high = 0;
+    std::vector<double> st, lo, hi, coeff;
+    int halves() const { return (wind && !uniform) ? 2 : 1; }
+    const double* S(int row, int h = 0) const { return &st[((size_t)h * n_st + row) * stl]; }
+    const double* Lo(int row, int h = 0) const { return &lo[((size_t)h * n_low + row) * bstl]; }
+    const double* Hi(int row, int h = 0) const { return &hi[((size_t)h * n_high + row) * bstl]; }
+};
+
+static void append(std::vector<double>& dst, const std::vector<double>& r) { dst.insert(dst.end(), r.begin(), r.end()); }
+static std::vector<double> iota_d(int lo, int hi, int step = 1) {
+    std::vector<double> v;
+    for (int k = lo; step > 0 ? k <= hi : k >= hi; k += step) v.push_back((double)k);
+    return v;
+}
+static std::vector<double> times(double s, std::vector<double> v) {
+    for (auto& e : v) e = s * e;
+    return v;
+}
+
+extern "C" deo_status deo_calculate_weights(int order, double x0, const double* x, int n, double* out) {
+    if (!x || !out || n <= 0) return fail(DEO_ERR_BAD_ARG, "null or empty point set");
+    if (order < 0 || order >= n) return fail(DEO_ERR_BAD_ARG, "Not enough points for the requested order.");
+    std::vector<double> w = fd_weights(order, x0, std::vector<double>(x, x + n));
+    std::copy(w.begin(), w.end(), out);
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_centered_difference(int d, int a, const double* dx, int ndx, int len, deo_operator** out) {
+    if (!out || !dx) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (a <= 1) return fail(DEO_ERR_BAD_ARG, "approximation_order must be greater than 1.");
+    if (d < 0 || len < 1) return fail(DEO_ERR_BAD_ARG, "invalid derivative order or length");
+    if (ndx != 1 && ndx != len + 1) return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 or len+1 entries");
+    auto op = std::make_unique<deo_operator>();
+    op->d = d; op->a = a; op->len = len;
+    op->stl = d + a - 1 + (d + a) % 2;
+    op->bstl = d + a;
+    op->bpc = op->stl / 2 - 1;
+    if (std::max(op->stl, op->bstl) > DEO_MAX_NW) return fail(DEO_ERR_UNSUPPORTED, "stencil wider than %d", DEO_MAX_NW);
+    const int stl = op->stl, bstl = op->bstl, bpc = op->bpc;
+    if (ndx == 1) {
+        op->uniform = 1;
+        const double s = 1.0 / pow_int(dx[0], d);
+        append(op->st, times(s, fd_weights(d, 0.0, iota_d(-(stl / 2), stl / 2))));
+        op->n_st = 1;
+        std::vector<std::vector<double>> low;
+        const std::vector<double> lx = iota_d(0, bstl - 1);
+        for (int x0 = 1; x0 <= stl / 2 - 1; ++x0) low.push_back(times(s, fd_weights(d, (double)x0, lx)));
+        for (auto& r : low) append(op->lo, r);
+        // high = reverse(map(reverse, low * (-1)^d))  (derivative_operator.jl:114-116)
+        const double sg = (d % 2 == 0) ? 1.0 : -1.0;
+        for (int i = bpc - 1; i >= 0; --i)
+            for (int k = 0; k < bstl; ++k) op->hi.push_back(low[i][bstl - 1 - k] * sg);
+    } else {
+        op->uniform = 0;
+        if (len + 1 - bpc < bpc + 2 && len - 2 * bpc < 0) return fail(DEO_ERR_BAD_SHAPE, "grid too short for stencil");
+        std::vector<double> sx(stl, 0.0);
+        const int c = stl / 2;
+        for (int i = bpc + 2; i <= len + 1 - bpc; ++i) {  // generate_coordinates, :137-148
+            for (auto& e : sx) e = e * 0.0;
+            for (int k = 1; k <= stl / 2; ++k) {
+                sx[c + k] = sx[c + k - 1] + dx[i + k - 2];
+                sx[c - k] = sx[c - k + 1] - dx[i - k - 1];
+            }
+            append(op->st, fd_weights(d, 0.0, sx));
+        }
+        op->n_st = std::max(0, len - 2 * bpc);
+        std::vector<double> lx(bstl), hx(bstl);
+        lx[0] = 0.0;
+        for (int k = 1; k < bstl; ++k) lx[k] = lx[k - 1] + dx[k - 1];
+        for (int k = 0; k < bstl; ++k) hx[k] = (k == 0) ? dx[ndx - bstl] : hx[k - 1] + dx[ndx - bstl + k];
+        for (int i = 1; i <= bpc; ++i) append(op->lo, fd_weights(d, lx[i], lx));
+        for (int i = bpc; i >= 1; --i) append(op->hi, fd_weights(d, hx[bstl - 1 - i], hx));
+    }
+    op->n_low = op->n_high = bpc;
+    op->coeff.assign(len, 0.0 + 1.0);
+    op->cfs = 1;
+    *out = op.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_upwind_difference(int d, int a, const double* dx, int ndx, int len, int off,
+                                            deo_operator** out) {
+    if (!out || !dx) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (off < 0) return fail(DEO_ERR_BAD_ARG, "Number of offside points should be non-negative");
+    if (off > (d + a - 1) / 2) return fail(DEO_ERR_BAD_ARG, "Number of offside points should not exceed the primary wind points");
+    if (d < 0 || a < 1 || len < 1) return fail(DEO_ERR_BAD_ARG, "invalid derivative order or length");
+    if (ndx != 1 && ndx != len + 1) return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 or len+1 entries");
+    auto op = std::make_unique<deo_operator>();
+    op->d = d; op->a = a; op->len = len; op->wind = 1; op->off = off;
+    op->stl = op->bstl = d + a;
+    op->bpc = op->bstl - 2 - off;
+    if (op->stl > DEO_MAX_NW) return fail(DEO_ERR_UNSUPPORTED, "stencil wider than %d", DEO_MAX_NW);
+    const int stl = op->stl, bstl = op->bstl, bpc = op->bpc;
+    if (ndx == 1) {
+        op->uniform = 1;
+        const double h = dx[0];
+        const double s = 1.0 / pow_int(h, d);
+        append(op->st, times(s, fd_weights(d, 0.0, iota_d(-off, stl - 1 - off))));
+        op->n_st = 1;
+        const std::vector<double> lx = iota_d(0, bstl - 1);
+        for (int x0 = 1; x0 <= bstl - 2 - off; ++x0) append(op->lo, times(s, fd_weights(d, (double)x0, lx)));
+        op->n_low = bpc;
+        const std::vector<double> hx = iota_d(0, -(bstl - 1), -1);
+        const double sh = pow_int(-1.0 / h, d);
+        int nh = 0;
+        for (int x0 = -1; x0 >= -(bstl - 2); --x0, ++nh) append(op->hi, times(sh, fd_weights(d, (double)x0, hx)));
+        op->n_high = nh;
+    } else {
+        op->uniform = 0;
+        if (len - 2 * bpc < 0) return fail(DEO_ERR_BAD_SHAPE, "grid too short for stencil");
+        std::vector<double> x(len + 2);
+        x[0] = 0.0;
+        for (int k = 1; k <= len + 1; ++k) x[k] = x[k - 1] + dx[k - 1];
+        auto X = [&](int j) { return x[j - 1]; };
+        auto sub = [&](int lo, int hi) { return std::vector<double>(x.begin() + (lo - 1), x.begin() + hi); };
+        std::vector<double> up, dn;
+        if (off == 0) {
+            for (int i = 1; i <= bpc; ++i) append(up, fd_weights(d, X(i + 1), sub(i + 1, i + bstl)));
+        } else {
+            for (int i = 1; i <= off - 1; ++i) append(up, fd_weights(d, X(i + 1), sub(1, bstl)));
+            for (int i = off; i <= bpc; ++i) append(up, fd_weights(d, X(i + 1), sub(i + 1 - off, i + bstl - off)));
+        }
+        for (int i = 1; i <= bpc; ++i) append(dn, fd_weights(d, X(i + 1), sub(1, bstl)));
+        op->lo = up;
+        append(op->lo, dn);
+        op->n_low = bpc;
+        up.clear(); dn.clear();
+        for (int i = bpc + 1; i <= len - bpc; ++i) append(up, fd_weights(d, X(i + 1), sub(i + 1 - off, i + stl - off)));
+        for (int i = bpc + 1; i <= len - bpc; ++i)
+            append(dn, fd_weights(d, X(i + 1), sub(i - stl + 2 + off, i + 1 + off)));
+        op->st = up;
+        append(op->st, dn);
+        op->n_st = std::max(0, len - 2 * bpc);
+        up.clear(); dn.clear();
+        for (int i = len - bpc + 1 - off; i <= len; ++i) append(up, fd_weights(d, X(i + 1), sub(len - bstl + 3, len + 2)));
+        if (off == 0) {
+            for (int i = len - bpc + 1; i <= len; ++i) append(dn, fd_weights(d, X(i + 1), sub(i - stl + 2, i + 1)));
+        } else {
+            for (int i = len - bpc + 1 - off; i <= len - off + 1; ++i)
+                append(dn, fd_weights(d, X(i + 1), sub(i - stl + 2 + off, i + 1 + off)));
+            for (int i = len - off + 2; i <= len; ++i) append(dn, fd_weights(d, X(i + 1), sub(len - stl + 3, len + 2)));
+        }
+        op->hi = up;
+        append(op->hi, dn);
+        op->n_high = bpc + off;
+    }
+    op->coeff.assign(len, 0.0 + 1.0);
+    op->cfs = 1;
+    *out = op.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_operator_from_tables(const deo_operator_desc* ds, deo_operator** out) {
+    if (!ds || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
+    auto op = std::make_unique<deo_operator>();
+    op->d = ds->derivative_order; op->a = ds->approximation_order; op->len = ds->len;
+    op->stl = ds->stencil_length; op->bstl = ds->boundary_stencil_length; op->bpc = ds->boundary_point_count;
+    op->off = ds->offside; op->wind = ds->winding != 0; op->uniform = ds->uniform != 0; op->cfs = ds->coeff_func_sign;
+    op->n_st = ds->n_stencil_rows; op->n_low = ds->n_low_rows; op->n_high = ds->n_high_rows;
+    if (op->len < 1 || op->stl < 1 || op->bstl < 1 || op->bpc < 0 || op->off < 0)
+        return fail(DEO_ERR_BAD_ARG, "invalid operator sizes");
+    if (std::max(op->stl, op->bstl) > DEO_MAX_NW) return fail(DEO_ERR_UNSUPPORTED, "stencil wider than %d", DEO_MAX_NW);
+    const int h = op->halves();
+    if (op->uniform ? op->n_st != 1 : op->n_st != std::max(0, op->len - 2 * op->bpc))
+        return fail(DEO_ERR_BAD_SHAPE, "stencil row count does not match len and boundary_point_count");
+    if (!ds->stencil_coefs || !ds->coefficients) return fail(DEO_ERR_BAD_ARG, "null table");
+    op->st.assign(ds->stencil_coefs, ds->stencil_coefs + (size_t)h * op->n_st * op->stl);
+    if (op->n_low) {
+        if (!ds->low_boundary_coefs) return fail(DEO_ERR_BAD_ARG, "null low boundary table");
+        op->lo.assign(ds->low_boundary_coefs, ds->low_boundary_coefs + (size_t)h * op->n_low * op->bstl);
+    }
+    if (op->n_high) {
+        if (!ds->high_boundary_coefs) return fail(DEO_ERR_BAD_ARG, "null high boundary table");
+        op->hi.assign(ds->high_boundary_coefs, ds->high_boundary_coefs + (size_t)h * op->n_high * op->bstl);
+    }
+    op->coeff.assign(ds->coefficients, ds->coefficients + op->len);
+    *out = op.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_operator_describe(const deo_operator* op, deo_operator_desc* ds) {
+    if (!op || !ds) return fail(DEO_ERR_BAD_ARG, "null argument");
+    ds->derivative_order = op->d; ds->approximation_order = op->a; ds->len = op->len;
+    ds->stencil_length = op->stl; ds->boundary_stencil_length = op->bstl; ds->boundary_point_count = op->bpc;
+    ds->offside = op->off; ds->winding = op->wind; ds->uniform = op->uniform; ds->coeff_func_sign = op->cfs;
+    ds->n_stencil_rows = op->n_st; ds->n_low_rows = op->n_low; ds->n_high_rows = op->n_high;
+    ds->stencil_coefs = op->st.data(); ds->low_boundary_coefs = op->lo.data();
+    ds->high_boundary_coefs = op->hi.data(); ds->coefficients = op->coeff.data();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_operator_set_coefficients(deo_operator* op, const double* c, int n, int cfs) {
+    if (!op || !c) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (n != 1 && n != op->len)
+        return fail(DEO_ERR_BAD_SHAPE, "length of c (%d) must match length of A (%d)", n, op->len);
+    for (int i = 0; i < op->len; ++i) op->coeff[i] = 0.0 + (n == 1 ? c[0] : c[i]);
+    op->cfs = cfs;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_operator_scale_coefficients(deo_operator* op, const double* c, int n) {
+    if (!op || !c) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (n != 1 && n != op->len)
+        return fail(DEO_ERR_BAD_SHAPE, "length of c (%d) must match length of A (%d)", n, op->len);
+    for (int i = 0; i < op->len; ++i) op->coeff[i] = (n == 1 ? c[0] : c[i]) * op->coeff[i];
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_operator_clone(const deo_operator* op, deo_operator** out) {
+    if (!op || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = new deo_operator(*op);
+    return DEO_OK;
+}
+
+extern "C" void deo_operator_destroy(deo_operator* op) { delete op; }
+
+// ---------------------------------------------------------------------------
+// boundary conditions
+// ---------------------------------------------------------------------------
+static std::vector<double> one_to(int n) { return iota_d(1, n); }
+
+extern "C" deo_status deo_robin_bc(const double* l, const double* r, const double* dx, int ndx, int order, deo_bc* q) {
+    if (!l || !r || !dx || !q) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (order < 1 || order > DEO_MAX_BC) return fail(DEO_ERR_UNSUPPORTED, "Robin order must be in 1..%d", DEO_MAX_BC);
+    std::memset(q, 0, sizeof *q);
+    const std::vector<double> s = fd_weights(1, 1.0, one_to(order + 1));
+    const int m = order;
+    if (ndx == 1) {  // bc_operators.jl:26-39
+        const double h = dx[0];
+        const double dl = l[0] * h / l[1] + s[0], dr = r[0] * h / r[1] - s[0];
+        for (int k = 0; k < m; ++k) q->a_l[k] = -s[1 + k] / dl;
+        for (int k = 0; k < m; ++k) q->a_r[k] = s[m - k] / dr;
+        q->b_l = l[2] / (l[0] + l[1] * s[0] / h);
+        q->b_r = r[2] / (r[0] - r[1] * s[0] / h);
+    } else {  // bc_operators.jl:40-60
+        const int ns = order + 1;
+        if (ndx < ns) return fail(DEO_ERR_BAD_SHAPE, "dx shorter than the Robin stencil");
+        const double* xl = dx;
+        const double* xr = dx + (ndx - ns);
+        const double dl = l[0] + l[1] * s[0] / xl[0];
+        const double dr = r[0] - r[1] * s[0] / xr[ns - 1];
+        for (int k = 0; k < m; ++k) q->a_l[k] = -l[1] * s[1 + k] / (dl * xl[1 + k]);
+        for (int k = 0; k < m; ++k) q->a_r[k] = r[1] * s[m - k] / (dr * xr[k]);
+        q->b_l = l[2] / dl;
+        q->b_r = r[2] / dr;
+    }
+    q->m_l = q->m_r = m;
+    q->kind = DEO_BC_AFFINE;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_general_bc(const double* al, int nl, const double* ar, int nr, const double* dx, int ndx,
+                                     int order, deo_bc* q) {
+    if (!al || !ar || !dx || !q) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (nl < 3 || nr < 3) return fail(DEO_ERR_BAD_ARG, "GeneralBC needs at least 3 coefficients per side");
+    const int wl = order + nl - 2, wr = order + nr - 2;
+    if (order < 1 || wl - 1 > DEO_MAX_BC || wr - 1 > DEO_MAX_BC) return fail(DEO_ERR_UNSUPPORTED, "GeneralBC stencil too long");
+    if (ndx != 1 && (ndx < wl || ndx < wr)) return fail(DEO_ERR_BAD_SHAPE, "dx shorter than the GeneralBC stencil");
+    std::memset(q, 0, sizeof *q);
+    // S rows: weights of derivative i at the boundary, divided by dx^i
+    // (per point dx_l[k]^i on a non-uniform grid, bc_operators.jl:139-144).
+    std::vector<std::vector<double>> Sl(nl - 2, std::vector<double>(wl, 0.0)), Sr(nr - 2, std::vector<double>(wr, 0.0));
+    for (int i = 1; i <= nl - 2; ++i) {
+        const std::vector<double> w = fd_weights(i, 1.0, one_to(order + i));
+        for (int k = 0; k < wl; ++k)
+            Sl[i - 1][k] = (k < (int)w.size() ? w[k] : 0.0) / pow_int(ndx == 1 ? dx[0] : dx[k], i);
+    }
+    for (int i = 1; i <= nr - 2; ++i) {
+        const std::vector<double> w = fd_weights(i, (double)(order + i), one_to(order + i));
+        for (int k = 0; k < wr; ++k)
+            Sr[i - 1][k] = (k < (int)w.size() ? w[k] : 0.0) / pow_int(ndx == 1 ? dx[0] : dx[ndx - 1 - k], i);
+    }
+    double sl = 0.0, sr = 0.0;
+    for (int i = 0; i < nl - 2; ++i) sl = (i == 0) ? al[2] * Sl[0][0] : sl + al[2 + i] * Sl[i][0];
+    for (int i = 0; i < nr - 2; ++i) sr = (i == 0) ? ar[2] * Sr[0][wr - 1] : sr + ar[2 + i] * Sr[i][wr - 1];
+    const double denl = al[1] + sl, denr = ar[1] + sr;
+    q->m_l = wl - 1;
+    for (int k = 0; k < wl - 1; ++k) {
+        double acc = 0.0;
+        for (int i = 0; i < nl - 2; ++i) acc = (i == 0) ? al[2] * Sl[0][1 + k] : acc + al[2 + i] * Sl[i][1 + k];
+        q->a_l[k] = -acc / denl;
+    }
+    q->m_r = wr - 1;
+    for (int k = 0; k < wr - 1; ++k) {
+        // column k of Sr = S_r[:, end-1-k]; a_r is the reversal
+        double acc = 0.0;
+        for (int i = 0; i < nr - 2; ++i) acc = (i == 0) ? ar[2] * Sr[0][wr - 2 - k] : acc + ar[2 + i] * Sr[i][wr - 2 - k];
+        q->a_r[wr - 2 - k] = -acc / denr;
+    }
+    q->b_l = -al[0] / denl;
+    q->b_r = -ar[0] / denr;
+    q->kind = DEO_BC_AFFINE;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_dirichlet_bc(double l, double r, deo_bc* q) {
+    const double L[3] = {1.0, 0.0, l}, R[3] = {1.0, 0.0, r}, one = 1.0;
+    return deo_robin_bc(L, R, &one, 1, 2, q);
+}
+
+extern "C" deo_status deo_neumann_bc(double l, double r, const double* dx, int ndx, int order, deo_bc* q) {
+    const double L[3] = {0.0, 1.0, l}, R[3] = {0.0, 1.0, r};
+    return deo_robin_bc(L, R, dx, ndx, order, q);
+}
+
+extern "C" deo_status deo_periodic_bc(deo_bc* q) {
+    if (!q) return fail(DEO_ERR_BAD_ARG, "null argument");
+    std::memset(q, 0, sizeof *q);
+    q->kind = DEO_BC_PERIODIC;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_bc_array(const deo_bc* b, int N, double* QL, double* Qb) {
+    if (!b || !QL || !Qb || N < 1) return fail(DEO_ERR_BAD_ARG, "bad argument");
+    const long R = N + 2;
+    std::fill(QL, QL + R * N, 0.0);
+    std::fill(Qb, Qb + R, 0.0);
+    for (long i = 0; i < N; ++i) QL[i * R + i + 1] = 1.0;
+    if (b->kind == DEO_BC_PERIODIC) {
+        QL[(N - 1) * R] = 1.0;
+        QL[N + 1] = 1.0;
+        return DEO_OK;
+    }
+    if (b->m_l > N || b->m_r > N) return fail(DEO_ERR_BAD_SHAPE, "BC stencil longer than N");
+    for (int j = 0; j < b->m_l; ++j) QL[j * R] = b->a_l[j];
+    for (int j = 0; j < b->m_r; ++j) QL[(N - b->m_r + j) * R + N + 1] = b->a_r[j];
+    Qb[0] = b->b_l;
+    Qb[N + 1] = b->b_r;
+    return DEO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Array(L): concretization.jl:8-52 (centred) and :556-671 (upwind)
+// ---------------------------------------------------------------------------
+extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
+    if (!op || !M) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const long N = op->len;
+    std::fill(M, M + N * (N + 2), 0.0);
+    auto set = [&](long i, long j, double v) {
+        if (i >= 1 && i <= N && j >= 1 && j <= N + 2) M[(j - 1) * N + (i - 1)] = v;
+    };
+    const int bl = op->bpc, stl = op->stl, bstl = op->bstl, off = op->off;
+    auto c = [&](long i) { return op->coeff[i - 1]; };
+    if (!op->wind) {
+        const int pivot = stl / 2;
+        for (int i = 1; i <= bl; ++i)
+            for (int k = 0; k < bstl; ++k) set(i, 1 + k, c(i) * op->Lo(i - 1)[k]);
+        for (long i = bl + 1; i <= N - bl; ++i) {
+            const double* s = op->uniform ? op->S(0) : op->S((int)(i - bl - 1));
+            for (int k = 0; k < stl; ++k) set(i, i + 1 - pivot + k, c(i) * s[k]);
+        }
+        for (long i = N - bl + 1; i <= N; ++i)
+            for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, c(i) * op->Hi((int)(i - N + bl - 1))[k]);
+        return DEO_OK;
+    }
+    const double sg = (op->d % 2 == 0) ? 1.0 : -1.0;
+    if (op->uniform) {
+        const double* S = op->S(0);
+        for (int i = 1; i <= bl; ++i) {
+            if (c(i) >= 0 && i + stl <= N + 2 && i >= off)
+                for (int k = 0; k < stl; ++k) set(i, i + 1 - off + k, c(i) * S[k]);
+            else
+                for (int k = 0; k < bstl; ++k) set(i, 1 + k, c(i) * op->Lo(i - 1)[k]);
+        }
+        for (long i = bl + 1; i <= N - bl - off; ++i) {
+            if (c(i) >= 0)
+                for (int k = 0; k < stl; ++k) set(i, i + 1 - off + k, c(i) * S[k]);
+            else
+                for (int k = 0; k < stl; ++k) set(i, i - stl + 2 + off + k, c(i) * (sg * S[stl - 1 - k]));
+        }
+        for (int r = 1; r <= bl + off; ++r) {
+            const long i = N - bl + r - off;
+            const double ci = c(i);
+            if (ci < 0 && N + 2 - stl - bl + r >= 1 && r <= bl + 1)
+                for (int k = 0; k < stl; ++k) set(i, r + N - stl - bl + 2 + k, ci * (sg * S[stl - 1 - k]));
+            else if (ci < 0 && N + 2 - stl - bl + r >= 1 && r > bl + 1) {
+                const double* h = op->Hi(bl + off + 1 - r - 1);
+                for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, ci * (sg * h[bstl - 1 - k]));
+            } else if (ci >= 0 && r < off + 1)
+                for (int k = 0; k < stl; ++k) set(i, N - stl + r - off + 3 + k, ci * S[k]);
+            else
+                for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, ci * op->Hi(r - 1)[k]);
+        }
+        return DEO_OK;
+    }
+    for (int i = 1; i <= bl; ++i) {
+        if (c(i) >= 0 && off == 0)
+            for (int k = 0; k < stl; ++k) set(i, i + 1 + k, c(i) * op->Lo(i - 1, 0)[k]);
+        else if (c(i) >= 0 && i < off)
+            for (int k = 0; k < stl; ++k) set(i, 1 + k, c(i) * op->Lo(i - 1, 0)[k]);
+        else if (c(i) >= 0 && i >= off)
+            for (int k = 0; k < stl; ++k) set(i, i + 1 - off + k, c(i) * op->Lo(i - 1, 0)[k]);
+        else
+            for (int k = 0; k < bstl; ++k) set(i, 1 + k, c(i) * op->Lo(i - 1, 1)[k]);
+    }
+    for (long i = bl + 1; i <= N - bl - off; ++i) {
+        if (c(i) >= 0)
+            for (int k = 0; k < stl; ++k) set(i, i + 1 - off + k, c(i) * op->S((int)(i - bl - 1), 0)[k]);
+        else
+            for (int k = 0; k < stl; ++k) set(i, i - stl + 2 + off + k, c(i) * op->S((int)(i - bl - 1), 1)[k]);
+    }
+    for (long i = N - bl + 1 - off; i <= N; ++i) {
+        const int hr = (int)(i - N + bl + off - 1);
+        if (c(i) < 0 && i <= N - off)
+            for (int k = 0; k < stl; ++k) set(i, i - stl + 2 + off + k, c(i) * op->Hi(hr, 1)[k]);
+        else if (c(i) < 0)
+            for (int k = 0; k < stl; ++k) set(i, N - stl + 3 + k, c(i) * op->Hi(hr, 1)[k]);
+        else if (i <= N - bl)
+            for (int k = 0; k < stl; ++k) set(i, i - bstl + 2 + off + k, c(i) * op->S((int)(i - bl - 1), 0)[k]);
+        else
+            for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, c(i) * op->Hi(hr, 0)[k]);
+    }
+    return DEO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Row-table compiler.  build_row() resolves, for output row i, which branch
+// of the reference's convolve_* loops runs and returns its window and
+// weights W[k] = coefficient * stencil[k] (the reference's first product).
+//   mode 1: BoundaryPaddedVector methods (convolutions.jl:367-730)
+//   mode 0: generic AbstractVector methods (convolutions.jl:27-362)
+//   scaled: W = c*s with the operator's own coefficients; otherwise the
+//           weights are left unscaled (a coefficient field multiplies them on
+//           the device) and `sgn` (+1 / -1) stands in for the coefficient in
+//           the sign tests.
+// ---------------------------------------------------------------------------
+struct RowSpec {
+    int p0, nk, cidx;
+    double w[DEO_MAX_NW];
+};
+
+static void row_fill(RowSpec& r, int p0, int nk, int cidx, double c, const double* s, double sg = 1.0,
+                     bool reversed = false) {
+    r.p0 = p0; r.nk = nk; r.cidx = cidx;
+    for (int k = 0; k < nk; ++k) {
+        double sk = reversed ? sg * s[nk - 1 - k] : s[k];
+        r.w[k] = c * sk;
+    }
+}
+
+static RowSpec build_row(const deo_operator& A, int mode, bool scaled, double sgn, long i) {
+    RowSpec r;
+    const long len = A.len;
+    const int stl = A.stl, bstl = A.bstl, bpc = A.bpc, off = A.off;
+    auto coef = [&](long pos) { return scaled ? A.coeff[pos - 1] : sgn; };
+    auto mult = [&](long pos) { return scaled ? A.coeff[pos - 1] : 1.0; };
+    if (!A.wind) {
+        if (i <= bpc) {
+            row_fill(r, 1, bstl, (int)i, mult(i), A.Lo((int)i - 1));
+        } else if (i <= len - bpc) {
+            const long ci = (mode == 1) ? i - bpc : i;
+            const double* s = A.uniform ? A.S(0) : A.S((int)(i - bpc - 1));
+            row_fill(r, (int)(i + 1 - stl / 2), stl, (int)ci, mult(ci), s);
+        } else {
+            const long rr = i - (len - bpc);
+            const long ci = (mode == 1) ? i : rr;  // generic right rows read coeff[1:bpc] (convolutions.jl:109)
+            row_fill(r, (int)(len + 3 - bstl), bstl, (int)ci, mult(ci), A.Hi((int)rr - 1));
+        }
+        return r;
+    }
+    const double sg = (A.d % 2 == 0) ? 1.0 : -1.0;
+    const double c = coef(i), m = mult(i);
+    if (A.uniform) {
+        const double* S = A.S(0);
+        if (i <= bpc) {
+            if (c >= 0 && i + stl <= len + 2 && i >= off) row_fill(r, (int)(i + 1 - off), stl, (int)i, m, S);
+            else row_fill(r, 1, bstl, (int)i, m, A.Lo((int)i - 1));
+        } else if (i <= len - bpc - off) {
+            if (c >= 0) row_fill(r, (int)(i + 1 - off), stl, (int)i, m, S);
+            else row_fill(r, (int)(i - stl + 2 + off), stl, (int)i, m, S, sg, true);
+        } else {
+            const long q = i - (len - bpc - off);
+            if (c < 0 && len + 2 - stl - bpc + q >= 1 && q <= bpc + 1)
+                row_fill(r, (int)(len + 2 - stl - bpc + q), stl, (int)i, m, S, sg, true);
+            else if (c < 0 && len + 2 - stl - bpc + q >= 1 && q > bpc + 1)
+                row_fill(r, (int)(len + 3 - bstl), bstl, (int)i, m, A.Hi((int)(bpc + off + 1 - q - 1)), sg, true);
+            else if (c >= 0 && q < off + 1)
+                row_fill(r, (int)(len + 3 - stl + q - off), stl, (int)i, m, S);
+            else
+                row_fill(r, (int)(len + 3 - bstl), bstl, (int)i, m, A.Hi((int)q - 1));
+        }
+        return r;
+    }
+    // non-uniform upwind
+    if (i <= bpc) {
+        if (c >= 0 && off == 0) row_fill(r, (int)(i + 1), stl, (int)i, m, A.Lo((int)i - 1, 0));
+        else if (c >= 0 && i < off) row_fill(r, 1, stl, (int)i, m, A.Lo((int)i - 1, 0));
+        else if (c >= 0 && i >= off) row_fill(r, (int)(i + 1 - off), stl, (int)i, m, A.Lo((int)i - 1, 0));
+        else row_fill(r, 1, bstl, (int)i, m, A.Lo((int)i - 1, 1));
+    } else if (i <= len - bpc - off) {
+        int half;
+        if (mode == 0 && scaled && A.cfs > 0) half = 0;        // convolutions.jl:234-243
+        else if (mode == 0 && scaled && A.cfs < 0) half = 1;   // convolutions.jl:244-253
+        else half = (c >= 0) ? 0 : 1;
+        if (half == 0) row_fill(r, (int)(i + 1 - off), stl, (int)i, m, A.S((int)(i - bpc - 1), 0));
+        else row_fill(r, (int)(i - stl + 2 + off), stl, (int)i, m, A.S((int)(i - bpc - 1), 1));
+    } else {
+        const int hr = (int)(i - len + bpc + off);
+        if (c < 0) {
+            const int p0 = (i <= len - off) ? (int)(i - stl + 2 + off) : (int)(len - stl + 3);
+            row_fill(r, p0, stl, (int)i, m, A.Hi(hr - 1, 1));
+        } else if (i <= len - bpc) {
+            row_fill(r, (int)(i - stl + 2 + off), stl, (int)i, m, A.S((int)(i - bpc - 1), 0));
+        } else {
+            row_fill(r, (int)(len - bstl + 3), bstl, (int)i, m, A.Hi(hr - 1, 0));
+        }
+    }
+    return r;
+}
+
+static bool same_shape(const RowSpec& a, long ia, const RowSpec& b, long ib) {
+    if (a.nk != b.nk || a.p0 - ia != b.p0 - ib || a.cidx - ia != b.cidx - ib) return false;
+    for (int k = 0; k < a.nk; ++k)
+        if (std::memcmp(&a.w[k], &b.w[k], sizeof(double)) != 0) return false;
+    return true;
+}
+
+struct HostTab {
+    RowTabDev dev{};
+    std::vector<int> p0, nk, cidx;
+    std::vector<double> W;  // [nw][nexp]
+};
+
+static deo_status compile_table(const deo_operator& A, int mode, bool scaled, double sgn, HostTab& T,
+                                std::vector<int>& rlo, std::vector<int>& rhi) {
+    const long len = A.len;
+    // pass 1: longest run of identical rows -> band
+    long best_lo = 1, best_len = 0, run_lo = 1;
+    RowSpec prev = build_row(A, mode, scaled, sgn, 1);
+    for (long i = 1; i <= len; ++i) {
+        RowSpec cur = (i == 1) ? prev : build_row(A, mode, scaled, sgn, i);
+        if (cur.p0 < 1 || cur.p0 + cur.nk - 1 > len + 2 || cur.nk < 1)
+            return fail(DEO_ERR_BAD_SHAPE, "row %ld of the operator reads outside the padded line (len %ld too short)",
+                        i, len);
+        for (int p = cur.p0; p < cur.p0 + cur.nk; ++p) {
+            rlo[p - 1] = std::min(rlo[p - 1], (int)i);
+            rhi[p - 1] = std::max(rhi[p - 1], (int)i);
+        }
+        if (i > 1 && !same_shape(prev, i - 1, cur, i)) run_lo = i;
+        if (i - run_lo + 1 > best_len) {
+            best_len = i - run_lo + 1;
+            best_lo = run_lo;
+        }
+        prev = cur;
+    }
+    RowTabDev& d = T.dev;
+    if (best_len >= 2) {
+        d.ilo = (int)best_lo;
+        d.ihi = (int)(best_lo + best_len - 1);
+        RowSpec b = build_row(A, mode, scaled, sgn, best_lo);
+        d.band_p0_off = (int)(b.p0 - best_lo);
+        d.band_cidx_off = (int)(b.cidx - best_lo);
+        d.band_nk = b.nk;
+        for (int k = 0; k < b.nk; ++k) d.wband[k] = b.w[k];
+    } else {
+        d.ilo = (int)len + 1;
+        d.ihi = (int)len;
+    }
+    // pass 2: explicit rows
+    int nw = 1;
+    std::vector<RowSpec> ex;
+    for (long i = 1; i <= len; ++i) {
+        if (i >= d.ilo && i <= d.ihi) continue;
+        ex.push_back(build_row(A, mode, scaled, sgn, i));
+        nw = std::max(nw, ex.back().nk);
+    }
+    d.nexp = (int)ex.size();
+    d.nw = nw;
+    T.p0.resize(ex.size()); T.nk.resize(ex.size()); T.cidx.resize(ex.size());
+    T.W.assign((size_t)nw * ex.size(), 0.0);
+    for (size_t e = 0; e < ex.size(); ++e) {
+        T.p0[e] = ex[e].p0; T.nk[e] = ex[e].nk; T.cidx[e] = ex[e].cidx;
+        for (int k = 0; k < ex[e].nk; ++k) T.W[(size_t)k * ex.size() + e] = ex[e].w[k];
+    }
+    return DEO_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+struct deo_plan {
+    PlanDev dev{};
+    PlanDev* d_plan = nullptr;  // device copy (batched kernel)
+    std::vector<void*> allocs;
+    size_t table_bytes = 0;
+    void* stage_u = nullptr;
+    void* stage_du = nullptr;
+    ~deo_plan() {
+        for (void* p : allocs) cudaFree(p);
+        if (d_plan) cudaFree(d_plan);
+        if (stage_u) cudaFree(stage_u);
+        if (stage_du) cudaFree(stage_du);
+    }
+};
+
+template <class V>
+static deo_status upload(deo_plan& P, const V& v, const void** dst) {
+    if (v.empty()) {
+        *dst = nullptr;
+        return DEO_OK;
+    }
+    void* p = nullptr;
+    const size_t bytes = v.size() * sizeof(v[0]);
+    CUDA_TRY(cudaMalloc(&p, bytes), "cudaMalloc(plan table)");
+    P.allocs.push_back(p);
+    CUDA_TRY(cudaMemcpy(p, v.data(), bytes, cudaMemcpyHostToDevice), "cudaMemcpy(plan table)");
+    P.table_bytes += bytes;
+    *dst = p;
+    return DEO_OK;
+}
+
+static deo_status upload_tab(deo_plan& P, HostTab& T, int dtype, RowTabDev& out) {
+    out = T.dev;
+    deo_status s;
+    if ((s = upload(P, T.p0, reinterpret_cast<const void**>(&out.p0))) != DEO_OK) return s;
+    if ((s = upload(P, T.nk, reinterpret_cast<const void**>(&out.nk))) != DEO_OK) return s;
+    if ((s = upload(P, T.cidx, reinterpret_cast<const void**>(&out.cidx))) != DEO_OK) return s;
+    if (dtype == DEO_F64) {
+        if ((s = upload(P, T.W, &out.W)) != DEO_OK) return s;
+    } else {
+        std::vector<float> wf(T.W.begin(), T.W.end());
+        if ((s = upload(P, wf, &out.W)) != DEO_OK) return s;
+        float* fb = reinterpret_cast<float*>(out.wband);
+        double tmp[DEO_MAX_NW];
+        std::memcpy(tmp, T.dev.wband, sizeof tmp);
+        std::memset(out.wband, 0, sizeof out.wband);
+        for (int k = 0; k < DEO_MAX_NW; ++k) fb[k] = (float)tmp[k];
+    }
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms,
+                                      const deo_term* terms, deo_plan** out) {
+    if (!out || !sizes || !terms) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
+    if (nterms < 1 || nterms > DEO_MAX_TERMS) return fail(DEO_ERR_BAD_ARG, "nterms must be 1..%d", DEO_MAX_TERMS);
+    if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
+    auto P = std::make_unique<deo_plan>();
+    PlanDev& D = P->dev;
+    D.ndims = ndims;
+    D.nterms = nterms;
+    D.dtype = dtype;
+    int64_t total = 1;
+    for (int k = 0; k < ndims; ++k) {
+        if (sizes[k] < 1) return fail(DEO_ERR_BAD_SHAPE, "size(u, %d) = %lld", k + 1, (long long)sizes[k]);
+        D.sizes[k] = sizes[k];
+        total *= sizes[k];
+    }
+    D.total = total;
+    for (int t = 0; t < nterms; ++t) {
+        const deo_term& tm = terms[t];
+        if (tm.path < DEO_PATH_AUTO || tm.path > DEO_PATH_GENERIC)
+            return fail(DEO_ERR_BAD_ARG, "term %d: unknown path %d", t + 1, tm.path);
+        const int mode = tm.path == DEO_PATH_PADDED ? 1 : tm.path == DEO_PATH_GENERIC ? 0 : (ndims == 1 ? 1 : 0);
+        if (!tm.op || !tm.bc) return fail(DEO_ERR_BAD_ARG, "term %d: null operator or boundary condition", t + 1);
+        const deo_operator& A = *tm.op;
+        const int ax = tm.axis - 1;
+        if (ax < 0 || ax >= ndims) return fail(DEO_ERR_BAD_SHAPE, "term %d: axis %d outside 1..%d", t + 1, tm.axis, ndims);
+        if (sizes[ax] != A.len)
+            return fail(DEO_ERR_BAD_SHAPE, "term %d: size(u, %d) = %lld but the operator has len %d", t + 1, tm.axis,
+                        (long long)sizes[ax], A.len);
+        const deo_bc& q = *tm.bc;
+        if (q.kind == DEO_BC_AFFINE && (q.m_l < 0 || q.m_r < 0 || q.m_l > DEO_MAX_BC || q.m_r > DEO_MAX_BC ||
+                                        q.m_l > A.len || q.m_r > A.len))
+            return fail(DEO_ERR_BAD_SHAPE, "term %d: boundary stencil longer than the line", t + 1);
+        if (!A.wind && A.len < 2 * A.bpc + 1)
+            return fail(DEO_ERR_BAD_SHAPE, "term %d: len %d < 2*boundary_point_count+1", t + 1, A.len);
+        if (A.wind && A.len < 2 * A.bpc + A.off)
+            return fail(DEO_ERR_BAD_SHAPE, "term %d: len %d too short for the upwind boundary rows", t + 1, A.len);
+        TermDev& T = D.t[t];
+        T.axis = ax;
+        T.len = A.len;
+        int64_t stride = 1;
+        for (int k = 0; k < ax; ++k) stride *= sizes[k];
+        T.stride = stride;
+        T.has_field = tm.coeff_field != nullptr;
+        T.field = tm.coeff_field;
+        T.nvar = (T.has_field && A.wind) ? 2 : 1;
+        std::vector<int> rlo(A.len + 2, A.len + 1), rhi(A.len + 2, 0);
+        for (int v = 0; v < T.nvar; ++v) {
+            HostTab H;
+            deo_status s = compile_table(A, mode, !T.has_field, v == 0 ? 1.0 : -1.0, H, rlo, rhi);
+            if (s != DEO_OK) return s;
+            if ((s = upload_tab(*P, H, dtype, T.tab[v])) != DEO_OK) return s;
+        }
+        for (int p = 0; p < A.len + 2; ++p)
+            if (rhi[p] < rlo[p]) { rlo[p] = 1; rhi[p] = 0; }
+        deo_status s;
+        if ((s = upload(*P, rlo, reinterpret_cast<const void**>(&T.rlo))) != DEO_OK) return s;
+        if ((s = upload(*P, rhi, reinterpret_cast<const void**>(&T.rhi))) != DEO_OK) return s;
+        T.bc_kind = q.kind;
+        T.periodic_nd = (q.kind == DEO_BC_PERIODIC && ndims > 1) ? 1 : 0;
+        T.ml = q.kind == DEO_BC_AFFINE ? q.m_l : 0;
+        T.mr = q.kind == DEO_BC_AFFINE ? q.m_r : 0;
+        for (int k = 0; k < DEO_MAX_BC; ++k) { T.al[k] = q.a_l[k]; T.ar[k] = q.a_r[k]; }
+        T.bl = q.b_l;
+        T.br = q.b_r;
+    }
+    CUDA_TRY(cudaMalloc(&P->d_plan, sizeof(PlanDev)), "cudaMalloc(plan)");
+    CUDA_TRY(cudaMemcpy(P->d_plan, &P->dev, sizeof(PlanDev), cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
+    *out = P.release();
+    return DEO_OK;
+}
+
+extern "C" void deo_plan_destroy(deo_plan* p) { delete p; }
+extern "C" size_t deo_plan_table_bytes(const deo_plan* p) { return p ? p->table_bytes : 0; }
+
+static deo_status check_ptrs(const deo_plan* p, const void* a, const void* b) {
+    if (!p) return fail(DEO_ERR_BAD_ARG, "null plan");
+    if (!a || !b) return fail(DEO_ERR_BAD_ARG, "null array");
+    if (a == b) return fail(DEO_ERR_BAD_ARG, "input and output must not alias");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_apply(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
+    deo_status s = check_ptrs(p, u, du);
+    if (s != DEO_OK) return s;
+    const int e = deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_apply launch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_apply_adjoint(const deo_plan* p, const void* d, void* ub, int overwrite, void* stream) {
+    deo_status s = check_ptrs(p, d, ub);
+    if (s != DEO_OK) return s;
+    const int e = deo_k_apply(&p->dev, d, ub, overwrite, 1, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_apply_adjoint launch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_apply_host(deo_plan* p, const void* uh, void* duh, void* stream) {
+    deo_status s = check_ptrs(p, uh, duh);
+    if (s != DEO_OK) return s;
+    const size_t bytes = (size_t)p->dev.total * (p->dev.dtype == DEO_F64 ? 8 : 4);
+    if (!p->stage_u) {
+        CUDA_TRY(cudaMalloc(&p->stage_u, bytes), "cudaMalloc(staging)");
+        CUDA_TRY(cudaMalloc(&p->stage_du, bytes), "cudaMalloc(staging)");
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaMemcpyAsync(p->stage_u, uh, bytes, cudaMemcpyHostToDevice, st), "H2D");
+    const int e = deo_k_apply(&p->dev, p->stage_u, p->stage_du, 1, 0, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_apply_host launch");
+    CUDA_TRY(cudaMemcpyAsync(duh, p->stage_du, bytes, cudaMemcpyDeviceToHost, st), "D2H");
+    CUDA_TRY(cudaStreamSynchronize(st), "synchronize");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double* Ab) {
+    if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const int64_t n = p->dev.total;
+    if (n > 8192) return fail(DEO_ERR_UNSUPPORTED, "concretisation is for checking operators with <= 8192 points");
+    if (p->dev.dtype != DEO_F64) return fail(DEO_ERR_UNSUPPORTED, "concretisation needs a Float64 plan");
+    const int64_t B = std::min<int64_t>(n + 1, 256);
+    double *dU = nullptr, *dD = nullptr;
+    CUDA_TRY(cudaMalloc(&dU, (size_t)(n * B) * 8), "cudaMalloc");
+    if (cudaMalloc(&dD, (size_t)(n * B) * 8) != cudaSuccess) {
+        cudaFree(dU);
+        return fail(DEO_ERR_OOM, "cudaMalloc");
+    }
+    std::vector<double> hU((size_t)(n * B)), hD((size_t)(n * B));
+    std::vector<double> col0(n);
+    deo_status st = DEO_OK;
+    // column j = -1 is the zero vector (gives A_b); columns 0..n-1 unit vectors
+    for (int64_t j0 = -1; j0 < n && st == DEO_OK; j0 += B) {
+        const int64_t nb = std::min<int64_t>(B, n - j0);
+        std::fill(hU.begin(), hU.end(), 0.0);
+        for (int64_t b = 0; b < nb; ++b)
+            if (j0 + b >= 0) hU[(size_t)(b * n + j0 + b)] = 1.0;
+        if (cudaMemcpy(dU, hU.data(), (size_t)(n * nb) * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+            st = fail(DEO_ERR_CUDA, "H2D");
+            break;
+        }
+        for (int64_t b = 0; b < nb; ++b) {
+            const int e = deo_k_apply(&p->dev, dU + b * n, dD + b * n, 1, 0, nullptr);
+            if (e) {
+                st = cuda_fail((cudaError_t)e, "concretize launch");
+                break;
+            }
+        }
+        if (st != DEO_OK) break;
+        if (cudaMemcpy(hD.data(), dD, (size_t)(n * nb) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            st = fail(DEO_ERR_CUDA, "D2H");
+            break;
+        }
+        for (int64_t b = 0; b < nb; ++b) {
+            const int64_t j = j0 + b;
+            const double* c = &hD[(size_t)(b * n)];
+            if (j < 0) {
+                std::copy(c, c + n, col0.begin());
+                std::copy(c, c + n, Ab);
+            } else {
+                for (int64_t i = 0; i < n; ++i) Al[(size_t)(j * n + i)] = c[i] - col0[i];
+            }
+        }
+    }
+    cudaFree(dU);
+    cudaFree(dD);
+    return st;
+}
+
+// ---------------------------------------------------------------------------
+// batched applies: one persistent launch over a work-list of tiles
+// ---------------------------------------------------------------------------
+struct deo_batch {
+    std::vector<deo::InstDev> inst;
+    std::vector<const deo_plan*> plans;
+    int adjoint = 0, dtype = 0;
+    int tile = 0, ctas = 0;
+    int64_t n_items = 0;
+    deo::InstDev* d_inst = nullptr;
+    deo::WorkItem* d_items = nullptr;
+    unsigned int* d_counter = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t cap = nullptr;
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+    }
+    ~deo_batch() {
+        drop_graph();
+        if (cap) cudaStreamDestroy(cap);
+        cudaFree(d_inst);
+        cudaFree(d_items);
+        cudaFree(d_counter);
+    }
+};
+
+static deo_status batch_items(deo_batch& b, int tile) {
+    std::vector<deo::WorkItem> items;
+    for (size_t i = 0; i < b.plans.size(); ++i) {
+        const int64_t n = b.plans[i]->dev.total;
+        for (int64_t s = 0; s < n; s += tile)
+            items.push_back(deo::WorkItem{(int)i, (int)std::min<int64_t>(tile, n - s), s});
+    }
+    // largest tiles first keeps the tail of the persistent launch short
+    std::stable_sort(items.begin(), items.end(),
+                     [](const deo::WorkItem& x, const deo::WorkItem& y) { return x.count > y.count; });
+    cudaFree(b.d_items);
+    b.d_items = nullptr;
+    b.n_items = (int64_t)items.size();
+    if (items.empty()) return DEO_OK;
+    CUDA_TRY(cudaMalloc(&b.d_items, items.size() * sizeof(deo::WorkItem)), "cudaMalloc(work-list)");
+    CUDA_TRY(cudaMemcpy(b.d_items, items.data(), items.size() * sizeof(deo::WorkItem), cudaMemcpyHostToDevice),
+             "cudaMemcpy(work-list)");
+    b.tile = tile;
+    b.drop_graph();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_batch_create(int n, const deo_instance* in, int adjoint, int tile, int ctas,
+                                       deo_batch** out) {
+    if (!out || (n > 0 && !in)) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    auto b = std::make_unique<deo_batch>();
+    b->adjoint = adjoint ? 1 : 0;
+    for (int i = 0; i < n; ++i) {
+        if (!in[i].plan || !in[i].u || !in[i].du) return fail(DEO_ERR_BAD_ARG, "instance %d: null plan or buffer", i);
+        if (in[i].u == in[i].du) return fail(DEO_ERR_BAD_ARG, "instance %d: input and output alias", i);
+        if (i > 0 && in[i].plan->dev.dtype != in[0].plan->dev.dtype)
+            return fail(DEO_ERR_BAD_ARG, "all instances of a batch must share one dtype");
+        b->plans.push_back(in[i].plan);
+        b->inst.push_back(deo::InstDev{in[i].plan->d_plan, in[i].u, in[i].du});
+    }
+    b->dtype = n > 0 ? in[0].plan->dev.dtype : 0;
+    if (n > 0) {
+        CUDA_TRY(cudaMalloc(&b->d_inst, n * sizeof(deo::InstDev)), "cudaMalloc(instances)");
+        CUDA_TRY(cudaMemcpy(b->d_inst, b->inst.data(), n * sizeof(deo::InstDev), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(instances)");
+    }
+    CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)), "cudaMalloc(counter)");
+    b->ctas = ctas > 0 ? ctas : 4;
+    deo_status s = batch_items(*b, tile > 0 ? tile : 8192);
+    if (s != DEO_OK) return s;
+    *out = b.release();
+    return DEO_OK;
+}
+
+static deo_status batch_launch(deo_batch& b, cudaStream_t st) {
+    const int e = deo_k_batch(b.d_inst, b.d_items, b.n_items, b.d_counter, b.dtype, b.adjoint, b.ctas, 256, st);
+    if (e) return cuda_fail((cudaError_t)e, "batched launch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_batch_run(deo_batch* b, int use_graph, void* stream) {
+    if (!b) return fail(DEO_ERR_BAD_ARG, "null batch");
+    if (b->n_items == 0) return DEO_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!use_graph) return batch_launch(*b, st);
+    if (!b->exec) {
+        if (!b->cap) CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking), "cudaStreamCreate");
+        CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+        deo_status s = batch_launch(*b, b->cap);
+        cudaGraph_t g = nullptr;
+        cudaError_t ec = cudaStreamEndCapture(b->cap, &g);
+        if (s != DEO_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+        b->graph = g;
+        CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0), "cudaGraphInstantiate");
+    }
+    CUDA_TRY(cudaGraphLaunch(b->exec, st), "cudaGraphLaunch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_batch_set_buffers(deo_batch* b, int i, const void* u, void* du) {
+    if (!b || i < 0 || i >= (int)b->inst.size() || !u || !du || u == du) return fail(DEO_ERR_BAD_ARG, "bad argument");
+    b->inst[i].u = u;
+    b->inst[i].du = du;
+    CUDA_TRY(cudaMemcpy(b->d_inst + i, &b->inst[i], sizeof(deo::InstDev), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_batch_config(const deo_batch* b, int* tile, int* ctas, int64_t* n_items) {
+    if (!b) return fail(DEO_ERR_BAD_ARG, "null batch");
+    if (tile) *tile = b->tile;
+    if (ctas) *ctas = b->ctas;
+    if (n_items) *n_items = b->n_items;
+    return DEO_OK;
+}
+
+extern "C" void deo_batch_destroy(deo_batch* b) { delete b; }
+
+// Workload signature for the autotuner cache: dtype, direction, instance
+// count and a log2-size histogram of the instances' point counts.
+static std::string batch_signature(const deo_batch& b) {
+    int hist[48] = {0};
+    int64_t total = 0;
+    int maxw = 0;
+    for (const deo_plan* p : b.plans) {
+        int lg = 0;
+        while ((int64_t(1) << (lg + 1)) <= p->dev.total && lg < 47) ++lg;
+        hist[lg]++;
+        total += p->dev.total;
+        for (int t = 0; t < p->dev.nterms; ++t) maxw = std::max(maxw, p->dev.t[t].tab[0].nw);
+    }
+    char buf[64];
+    std::string s;
+    snprintf(buf, sizeof buf, "v1:d%d:a%d:n%zu:w%d:t%lld", b.dtype, b.adjoint, b.plans.size(), maxw, (long long)total);
+    s += buf;
+    for (int i = 0; i < 48; ++i)
+        if (hist[i]) {
+            snprintf(buf, sizeof buf, ":%d=%d", i, hist[i]);
+            s += buf;
+        }
+    return s;
+}
+
+static std::mutex g_tune_mu;
+static std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+extern "C" deo_status deo_batch_autotune(deo_batch* b, const char* cache_path, void* stream) {
+    if (!b) return fail(DEO_ERR_BAD_ARG, "null batch");
+    const std::string key = batch_signature(*b);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (cache_path && g_tune_cache.find(key) == g_tune_cache.end()) {
+            if (FILE* f = fopen(cache_path, "r")) {
+                char k[4096];
+                int t, c;
+                while (fscanf(f, "%4095s %d %d", k, &t, &c) == 3) g_tune_cache[k] = {t, c};
+                fclose(f);
+            }
+        }
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            b->ctas = it->second.second;
+            return batch_items(*b, it->second.first);
+        }
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+    CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+    const int tiles[] = {1024, 2048, 4096, 8192, 16384, 32768, 65536};
+    const int ctas[] = {2, 4, 6, 8};
+    float best = 1e30f;
+    int bt = 8192, bc = 4;
+    deo_status s = DEO_OK;
+    for (int tile : tiles) {
+        if ((s = batch_items(*b, tile)) != DEO_OK) break;
+        for (int c : ctas) {
+            b->ctas = c;
+            if ((s = batch_launch(*b, st)) != DEO_OK) break;  // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < 3 && s == DEO_OK; ++r) s = batch_launch(*b, st);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                s = fail(DEO_ERR_CUDA, "autotune timing failed");
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                bt = tile;
+                bc = c;
+            }
+        }
+        if (s != DEO_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != DEO_OK) return s;
+    b->ctas = bc;
+    s = batch_items(*b, bt);
+    if (s != DEO_OK) return s;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[key] = {bt, bc};
+    if (cache_path) {
+        if (FILE* f = fopen(cache_path, "a")) {
+            fprintf(f, "%s %d %d\n", key.c_str(), bt, bc);
+            fclose(f);
+        }
+    }
+    return DEO_OK;
+}

@@ -1,0 +1,90 @@
+// deo_internal.h -- structures shared by the host compiler (deo_host.cpp)
+// and the CUDA kernels (deo_kernels.cu).
+//
+// Every operator term is lowered on the host to a *row table*: for output row
+// i (1-based position along the differentiated axis) the reference computes
+//     out[i] = sum_k  W_i[k] * x[p0_i + k],   k = 0 .. nk_i-1,
+// where x is the ghost-padded line (x[1] = left ghost, x[len+2] = right ghost)
+// and W_i[k] = coefficient * stencil weight, rounded exactly as the
+// reference's `cur_coeff * cur_stencil[idx]`.  All of the reference's branch
+// logic (boundary rows, upwind direction by coefficient sign, offside,
+// the coefficient-index conventions of the padded and generic methods) is
+// resolved when the table is built, so one device evaluator serves every
+// operator kind.  Rows whose (p0 - i, nk, W) repeat form a "band" stored once.
+#pragma once
+#include <stdint.h>
+
+#define DEO_MAX_NW 16      // widest row (max(stencil_length, boundary_stencil_length))
+#define DEO_MAX_BCW 16
+
+namespace deo {
+
+struct RowTabDev {
+    int ilo, ihi;        // band rows [ilo, ihi] (1-based, inclusive); empty if ilo > ihi
+    int band_p0_off;     // p0 = i + band_p0_off
+    int band_cidx_off;   // coefficient position = i + band_cidx_off
+    int band_nk;
+    int nexp;            // explicit rows: all rows outside the band
+    int nw;              // row stride of W (max nk)
+    int pad_;
+    double wband[DEO_MAX_NW];
+    const int* p0;       // [nexp]
+    const int* nk;       // [nexp]
+    const int* cidx;     // [nexp]
+    const void* W;       // [nw][nexp], element type = plan dtype (k-major: coalesced along rows)
+};
+
+struct TermDev {
+    int64_t stride;      // elements between neighbours along the axis
+    int len;             // points along the axis
+    int axis;            // 0-based
+    int nvar;            // 1, or 2 for an upwind operator with a coefficient field (c>=0 / c<0)
+    int has_field;
+    const void* field;   // coefficient field (same shape/dtype as u) or null
+    RowTabDev tab[2];
+    // adjoint: rows touching padded column p (1..len+2) lie in [rlo[p-1], rhi[p-1]]
+    const int* rlo;
+    const int* rhi;
+    // boundary condition (ghost map)
+    int bc_kind;         // 0 affine, 1 periodic
+    int periodic_nd;     // N-D PeriodicBC pads with the edge planes (multi_dim_bc_operators.jl:221-228)
+    int ml, mr;
+    double al[DEO_MAX_BCW];
+    double ar[DEO_MAX_BCW];
+    double bl, br;
+};
+
+#define DEO_KMAX_TERMS 8
+struct PlanDev {
+    int ndims;
+    int nterms;
+    int dtype;           // 0 f64, 1 f32
+    int pad_;
+    int64_t sizes[8];
+    int64_t total;
+    TermDev t[DEO_KMAX_TERMS];
+};
+
+// Work item of the batched persistent kernel: `count` points starting at
+// flat index `start` of instance `inst`.
+struct WorkItem {
+    int inst;
+    int count;
+    int64_t start;
+};
+
+struct InstDev {
+    const PlanDev* plan;   // device copy of the instance's plan
+    const void* u;
+    void* du;
+};
+
+}  // namespace deo
+
+// Launchers implemented in deo_kernels.cu (return cudaError_t as int).
+extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
+                           void* stream);
+extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items, int64_t n_items,
+                           unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
+                           void* stream);
+extern "C" int deo_k_num_sms(void);

@@ -1,0 +1,17 @@
+"""deo -- DiffEqOperators.jl's stencil-apply path on GB300 (sm_103a).
+
+The public names mirror the reference package (CenteredDifference,
+UpwindDifference, RobinBC, GeneralBC, DirichletBC, Dirichlet0BC, NeumannBC,
+Neumann0BC, PeriodicBC, MultiDimBC, compose, `L*Q*u`, mul!) and run on the
+CUDA kernels of libdeo.so.  There is no CPU fallback.
+"""
+from ._lib import DeoError, DeoArgError, DeoShapeError, LIB_PATH, lib  # noqa: F401
+from .operators import (  # noqa: F401
+    AtomicBC, CenteredDifference, ComposedMultiDimBC, DerivativeOperator, DiffEqOperatorCombination,
+    DimensionMismatch, Dirichlet0BC, DirichletBC, FieldCoefficient, GeneralBC, GhostDerivativeOperator,
+    MultiDimBC, MultiDimDirectionalBC, Neumann0BC, NeumannBC, PeriodicBC, Plan, RobinBC, UpwindDifference,
+    calculate_weights, clear_plan_cache, compose, concretize, fortran_strides, julia_array, mul_,
+    operator_from_tables, plan_for, to_julia_layout, with_field,
+)
+
+mul = mul_

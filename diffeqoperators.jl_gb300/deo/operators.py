@@ -1,0 +1,716 @@
+"""Host-side mirror of DiffEqOperators.jl's operator API over libdeo.
+
+Names, argument meaning and errors follow the reference:
+
+    L  = CenteredDifference(2, 2, h, N)              # CenteredDifference{1}
+    Q  = Dirichlet0BC(np.float64)
+    du = L * Q * u                                    # (L*Q)*u, u a CUDA tensor
+    mul_(du, L * Q, u)                                # mul!(du, L*Q, u)
+
+    Dxx = CenteredDifference(2, 4, h, n, axis=1)      # CenteredDifference{1}
+    Dyy = CenteredDifference(2, 4, h, n, axis=2)      # CenteredDifference{2}
+    Qc  = compose(*RobinBC((1., .5, 0.), (1., .5, 0.), (h, h, h), 1, (n, n, n)))
+    du  = (Dxx + Dyy + Dzz) * Qc * u
+
+Arrays use Julia's layout: an N-D array of size (s1, s2, ...) is a
+column-major (Fortran-ordered) tensor whose axis 1 is contiguous; build one
+with `julia_array(...)` or pass `x.permute(...)` views of that layout.
+Device tensors run on the current torch stream; numpy arrays go through the
+library's host-buffer entry point (copies included).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import numbers
+from typing import Iterable, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import BCStruct, DeoArgError, DeoShapeError, Term, check
+
+_dp = C.POINTER(C.c_double)
+
+
+def _f64(x) -> np.ndarray:
+    return np.ascontiguousarray(np.atleast_1d(np.asarray(x, dtype=np.float64)).ravel())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def calculate_weights(order: int, x0: float, x: Sequence[float]) -> np.ndarray:
+    """Fornberg weights (fornberg.jl:7-62)."""
+    xv = _f64(x)
+    out = np.zeros_like(xv)
+    if order >= len(xv):
+        raise AssertionError("Not enough points for the requested order.")
+    check(L.lib().deo_calculate_weights(int(order), float(x0), _ptr(xv), len(xv), _ptr(out)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# torch / layout helpers
+# ---------------------------------------------------------------------------
+def _torch():
+    import torch
+    return torch
+
+
+def fortran_strides(shape: Sequence[int]) -> tuple:
+    s, out = 1, []
+    for n in shape:
+        out.append(s)
+        s *= n
+    return tuple(out)
+
+
+def julia_array(shape: Sequence[int], dtype=None, device="cuda", fill=None):
+    """A column-major torch tensor of Julia size `shape` (axis 1 contiguous)."""
+    torch = _torch()
+    dtype = dtype or torch.float64
+    t = torch.empty(tuple(reversed(tuple(shape))), dtype=dtype, device=device).permute(
+        *reversed(range(len(shape))))
+    if fill is not None:
+        t.fill_(fill)
+    return t
+
+
+def to_julia_layout(x):
+    """Copy a tensor/ndarray into Julia (column-major) layout, same Julia size."""
+    torch = _torch()
+    if isinstance(x, np.ndarray):
+        return np.asfortranarray(x)
+    out = julia_array(tuple(x.shape), x.dtype, x.device)
+    out.copy_(x)
+    return out
+
+
+def _check_layout(x, what="u"):
+    if tuple(x.stride()) != fortran_strides(x.shape):
+        raise DeoArgError(2, f"{what} must be column-major (Julia layout, axis 1 contiguous); "
+                             f"got strides {tuple(x.stride())} for size {tuple(x.shape)}")
+
+
+def _dtype_code(x) -> int:
+    torch = _torch()
+    if x.dtype == torch.float64:
+        return L.DEO_F64
+    if x.dtype == torch.float32:
+        return L.DEO_F32
+    raise DeoArgError(2, f"unsupported dtype {x.dtype} (Float64 and Float32 only)")
+
+
+def _stream_ptr():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ---------------------------------------------------------------------------
+# Derivative operators
+# ---------------------------------------------------------------------------
+class DerivativeOperator:
+    """DerivativeOperator (derivative_operator.jl:14-29) backed by a deo_operator."""
+
+    __array_ufunc__ = None  # `c * L` with a numpy vector c goes to __rmul__
+
+    def __init__(self, handle: int, axis: int = 1):
+        self._h = C.c_void_p(handle)
+        self.axis = int(axis)
+        self._desc = L.OperatorDesc()
+        self._refresh()
+
+    def _refresh(self):
+        check(L.lib().deo_operator_describe(self._h, C.byref(self._desc)))
+
+    def __del__(self):
+        try:
+            if self._h:
+                L.lib().deo_operator_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    # fields -------------------------------------------------------------
+    derivative_order = property(lambda s: s._desc.derivative_order)
+    approximation_order = property(lambda s: s._desc.approximation_order)
+    len = property(lambda s: s._desc.len)
+    stencil_length = property(lambda s: s._desc.stencil_length)
+    boundary_stencil_length = property(lambda s: s._desc.boundary_stencil_length)
+    boundary_point_count = property(lambda s: s._desc.boundary_point_count)
+    offside = property(lambda s: s._desc.offside)
+    winding = property(lambda s: bool(s._desc.winding))
+    uniform = property(lambda s: bool(s._desc.uniform))
+    coeff_func_sign = property(lambda s: s._desc.coeff_func_sign)
+
+    def _halves(self):
+        return 2 if (self.winding and not self.uniform) else 1
+
+    def _table(self, ptr, rows, width):
+        n = self._halves() * rows * width
+        if n == 0:
+            return np.zeros((self._halves(), rows, width))
+        return np.ctypeslib.as_array(ptr, shape=(n,)).copy().reshape(self._halves(), rows, width)
+
+    @property
+    def stencil_coefs(self):
+        d = self._desc
+        return self._table(d.stencil_coefs, d.n_stencil_rows, d.stencil_length)
+
+    @property
+    def low_boundary_coefs(self):
+        d = self._desc
+        return self._table(d.low_boundary_coefs, d.n_low_rows, d.boundary_stencil_length)
+
+    @property
+    def high_boundary_coefs(self):
+        d = self._desc
+        return self._table(d.high_boundary_coefs, d.n_high_rows, d.boundary_stencil_length)
+
+    @property
+    def coefficients(self):
+        return np.ctypeslib.as_array(self._desc.coefficients, shape=(self.len,)).copy()
+
+    @property
+    def size(self):
+        return (self.len, self.len + 2)
+
+    def copy(self) -> "DerivativeOperator":
+        h = C.c_void_p()
+        check(L.lib().deo_operator_clone(self._h, C.byref(h)))
+        return DerivativeOperator(h.value, self.axis)
+
+    # algebra ------------------------------------------------------------
+    def __rmul__(self, c):
+        """c * L scales the coefficients (derivative_operator_functions.jl:165-197)."""
+        if isinstance(c, numbers.Number) or (isinstance(c, np.ndarray) and c.ndim <= 1):
+            cv = _f64(c)
+            if cv.size not in (1, self.len):
+                raise DimensionMismatch(f"length of c ({cv.size}) must match length of A ({self.len})")
+            out = self.copy()
+            check(L.lib().deo_operator_scale_coefficients(out._h, _ptr(cv), cv.size))
+            out._refresh()
+            return out
+        return NotImplemented
+
+    def __mul__(self, other):
+        if isinstance(other, (AtomicBC, MultiDimensionalBC)):
+            return GhostDerivativeOperator(self, other)
+        if isinstance(other, DerivativeOperator) or isinstance(other, numbers.Number):
+            return NotImplemented
+        return _mul_padded_vector(self, other)
+
+    def __add__(self, other):
+        return DiffEqOperatorCombination([self]) + other
+
+    def __neg__(self):
+        return (-1.0) * self
+
+    def array(self, N: int | None = None) -> np.ndarray:
+        """Array(L): len x (len+2) (concretization.jl:8-52, :556-671)."""
+        M = np.zeros((self.len, self.len + 2), order="F")
+        check(L.lib().deo_operator_array(self._h, M.ctypes.data_as(_dp)))
+        return M
+
+    def banded(self):
+        """BandedMatrix(L) data: (matrix, (lower, upper)) with the reference's
+        bandwidths (bstl-3, bstl-1) for centred operators (concretization.jl:123-128)."""
+        bstl = self.boundary_stencil_length
+        return self.array(), (bstl - 3, bstl - 1)
+
+
+class DimensionMismatch(DeoShapeError):
+    def __init__(self, msg):
+        super().__init__(1, msg)
+
+
+def _apply_coeff(op: DerivativeOperator, coeff_func):
+    """compute_coeffs! on a fresh operator (coefficient_functions.jl:7-46)."""
+    if coeff_func is None:
+        return op
+    if isinstance(coeff_func, numbers.Number):
+        cv = _f64(coeff_func)
+        sign = 1 if coeff_func >= 0 else -1
+    elif callable(coeff_func):
+        cur = op.coefficients * 0.0
+        try:
+            vals = np.asarray(coeff_func(cur), dtype=np.float64)
+            if vals.shape != cur.shape:
+                raise TypeError
+        except TypeError:
+            vals = np.array([coeff_func(c) for c in cur], dtype=np.float64)
+        cv, sign = _f64(vals), 0
+    else:
+        cv, sign = _f64(coeff_func), 0
+        if cv.size != op.len:
+            raise DimensionMismatch(f"coefficient vector has {cv.size} entries, operator len {op.len}")
+    check(L.lib().deo_operator_set_coefficients(op._h, _ptr(cv), cv.size, sign))
+    op._refresh()
+    return op
+
+
+def _dx_args(dx):
+    dxv = _f64(dx)
+    return dxv, dxv.size
+
+
+def CenteredDifference(derivative_order: int, approximation_order: int, dx, len: int, coeff_func=1,
+                       axis: int = 1) -> DerivativeOperator:
+    """CenteredDifference{axis}(d, a, dx, len, coeff_func) (derivative_operator.jl:81-205)."""
+    if approximation_order <= 1:
+        raise AssertionError("approximation_order must be greater than 1.")
+    dxv, n = _dx_args(dx)
+    h = C.c_void_p()
+    check(L.lib().deo_centered_difference(int(derivative_order), int(approximation_order), _ptr(dxv), n,
+                                          int(len), C.byref(h)))
+    return _apply_coeff(DerivativeOperator(h.value, axis), coeff_func)
+
+
+def UpwindDifference(derivative_order: int, approximation_order: int, dx, len: int, coeff_func=1,
+                     offside: int = 0, axis: int = 1) -> DerivativeOperator:
+    """UpwindDifference{axis}(d, a, dx, len, coeff_func; offside) (derivative_operator.jl:454-639)."""
+    if offside < 0:
+        raise AssertionError("Number of offside points should be non-negative")
+    if offside > (derivative_order + approximation_order - 1) // 2:
+        raise AssertionError("Number of offside points should not exceed the primary wind points")
+    dxv, n = _dx_args(dx)
+    h = C.c_void_p()
+    check(L.lib().deo_upwind_difference(int(derivative_order), int(approximation_order), _ptr(dxv), n, int(len),
+                                        int(offside), C.byref(h)))
+    return _apply_coeff(DerivativeOperator(h.value, axis), coeff_func)
+
+
+def operator_from_tables(desc: dict, axis: int = 1) -> DerivativeOperator:
+    """Build from a DerivativeOperator's own fields (what the Julia shim passes)."""
+    keep = {}
+    d = L.OperatorDesc()
+    for k in ("derivative_order", "approximation_order", "len", "stencil_length", "boundary_stencil_length",
+              "boundary_point_count", "offside", "winding", "uniform", "coeff_func_sign", "n_stencil_rows",
+              "n_low_rows", "n_high_rows"):
+        setattr(d, k, int(desc[k]))
+    for k in ("stencil_coefs", "low_boundary_coefs", "high_boundary_coefs", "coefficients"):
+        a = _f64(desc[k])
+        keep[k] = a
+        setattr(d, k, _ptr(a))
+    h = C.c_void_p()
+    check(L.lib().deo_operator_from_tables(C.byref(d), C.byref(h)))
+    return DerivativeOperator(h.value, axis)
+
+
+# ---------------------------------------------------------------------------
+# Boundary conditions
+# ---------------------------------------------------------------------------
+class AtomicBC:
+    """An affine ghost map (RobinBC, GeneralBC, Dirichlet/Neumann) or PeriodicBC."""
+
+    def __init__(self, s: BCStruct, name: str):
+        self._s = s
+        self.name = name
+
+    @property
+    def a_l(self):
+        return np.array(self._s.a_l[: self._s.m_l])
+
+    @property
+    def a_r(self):
+        return np.array(self._s.a_r[: self._s.m_r])
+
+    @property
+    def b_l(self):
+        return self._s.b_l
+
+    @property
+    def b_r(self):
+        return self._s.b_r
+
+    @property
+    def periodic(self):
+        return self._s.kind == L.DEO_BC_PERIODIC
+
+    def array(self, N: int):
+        """Array(Q, N) -> (Q_L, Q_b) (concretization.jl:187-192, :227-230)."""
+        QL = np.zeros((N + 2, N), order="F")
+        Qb = np.zeros(N + 2)
+        check(L.lib().deo_bc_array(C.byref(self._s), int(N), QL.ctypes.data_as(_dp), _ptr(Qb)))
+        return QL, Qb
+
+    def __mul__(self, u):
+        """Q*u -> the padded vector [ghost_l; u; ghost_r] as a numpy array (bc_operators.jl:188-192)."""
+        uv = np.asarray(u, dtype=np.float64)
+        if uv.ndim != 1:
+            raise DeoArgError(2, "Q*u materialises a padded Vector only; apply N-D BCs through L*Q*u")
+        if self.periodic:
+            return np.concatenate([[uv[-1]], uv, [uv[0]]])
+        l = float(np.dot(self.a_l, uv[: self._s.m_l])) + self.b_l
+        r = float(np.dot(self.a_r, uv[len(uv) - self._s.m_r:])) + self.b_r
+        return np.concatenate([[l], uv, [r]])
+
+    def __repr__(self):
+        return f"{self.name}(a_l={self.a_l}, b_l={self.b_l}, a_r={self.a_r}, b_r={self.b_r})"
+
+
+def _bc_call(fn, *args, name=""):
+    s = BCStruct()
+    check(fn(*args, C.byref(s)))
+    return AtomicBC(s, name)
+
+
+def _robin_atomic(l, r, dx, order=1):
+    lv, rv = _f64(l), _f64(r)
+    dxv, n = _dx_args(dx)
+    return _bc_call(L.lib().deo_robin_bc, _ptr(lv), _ptr(rv), _ptr(dxv), n, int(order), name="RobinBC")
+
+
+def _general_atomic(al, ar, dx, order=1):
+    alv, arv = _f64(al), _f64(ar)
+    dxv, n = _dx_args(dx)
+    return _bc_call(L.lib().deo_general_bc, _ptr(alv), alv.size, _ptr(arv), arv.size, _ptr(dxv), n, int(order),
+                    name="GeneralBC")
+
+
+def RobinBC(l, r, dx, order=1, s=None, dim=None):
+    """RobinBC(l, r, dx, order) (bc_operators.jl:26-60); with `s` (domain size)
+    the multi-dimensional form: one MultiDimDirectionalBC per axis with
+    dx = dxyz[axis] (multi_dim_bc_operators.jl:138-149)."""
+    if s is None:
+        return _robin_atomic(l, r, dx, order)
+    if dim is not None:
+        return MultiDimDirectionalBC(_robin_atomic(l, r, dx, order), dim, s)
+    return tuple(MultiDimDirectionalBC(_robin_atomic(l, r, dx[k], order), k + 1, s) for k in range(len(s)))
+
+
+def GeneralBC(al, ar, dx, order=1, s=None, dim=None):
+    """GeneralBC(αl, αr, dx, order) (bc_operators.jl:90-169) / multi-D (multi_dim_bc_operators.jl:151-163)."""
+    if s is None:
+        return _general_atomic(al, ar, dx, order)
+    if dim is not None:
+        return MultiDimDirectionalBC(_general_atomic(al, ar, dx, order), dim, s)
+    return tuple(MultiDimDirectionalBC(_general_atomic(al, ar, dx[k], order), k + 1, s) for k in range(len(s)))
+
+
+def DirichletBC(l: float, r: float, s=None, dim=None):
+    """DirichletBC(αl, αr) = RobinBC((1,0,αl),(1,0,αr),1,2) (bc_operators.jl:175-177)."""
+    q = _bc_call(L.lib().deo_dirichlet_bc, float(l), float(r), name="DirichletBC")
+    if s is None:
+        return q
+    if dim is not None:
+        return MultiDimDirectionalBC(q, dim, s)
+    return tuple(MultiDimDirectionalBC(q, k + 1, s) for k in range(len(s)))
+
+
+def Dirichlet0BC(T=np.float64, s=None, dim=None):
+    return DirichletBC(0.0, 0.0, s, dim)
+
+
+def NeumannBC(alpha, dx, order=1, s=None, dim=None):
+    """NeumannBC((αl, αr), dx, order) = RobinBC((0,1,αl),(0,1,αr),dx,order) (bc_operators.jl:173-174)."""
+    if s is None:
+        dxv, n = _dx_args(dx)
+        return _bc_call(L.lib().deo_neumann_bc, float(alpha[0]), float(alpha[1]), _ptr(dxv), n, int(order),
+                        name="NeumannBC")
+    return RobinBC((0.0, 1.0, alpha[0]), (0.0, 1.0, alpha[1]), dx, order, s, dim)
+
+
+def Neumann0BC(dx, order=1, s=None, dim=None):
+    return NeumannBC((0.0, 0.0), dx, order, s, dim)
+
+
+def PeriodicBC(T=np.float64, s=None, dim=None):
+    """PeriodicBC(T) (bc_operators.jl:17-19); with `s`, the N-D form, which pads
+    with the edge planes themselves (multi_dim_bc_operators.jl:221-228)."""
+    q = _bc_call(L.lib().deo_periodic_bc, name="PeriodicBC")
+    if s is None:
+        return q
+    if dim is not None:
+        return MultiDimDirectionalBC(q, dim, s)
+    return tuple(MultiDimDirectionalBC(q, k + 1, s) for k in range(len(s)))
+
+
+class MultiDimensionalBC:
+    pass
+
+
+class MultiDimDirectionalBC(MultiDimensionalBC):
+    """One atomic BC extended over every line along `axis` (multi_dim_bc_operators.jl:54-57, 97-101)."""
+
+    def __init__(self, bc: AtomicBC, axis: int, s: Sequence[int]):
+        self.bc, self.axis, self.shape = bc, int(axis), tuple(int(n) for n in s)
+
+    def __add__(self, other):
+        return compose(self, other)
+
+    def bc_for(self, axis: int, ndims: int) -> AtomicBC:
+        if axis != self.axis:
+            raise DeoShapeError(1, f"operator differentiates along {axis} but the BC extends dimension {self.axis}")
+        return self.bc
+
+
+class ComposedMultiDimBC(MultiDimensionalBC):
+    """compose(Qx, Qy, ...) (multi_dim_bc_operators.jl:178-192)."""
+
+    def __init__(self, bcs: Sequence[MultiDimDirectionalBC]):
+        self.bcs = {b.axis: b.bc for b in bcs}
+        self.shape = bcs[0].shape
+
+    def bc_for(self, axis: int, ndims: int) -> AtomicBC:
+        return self.bcs[axis]
+
+
+def compose(*bcs):
+    if not bcs:
+        raise DeoArgError(2, "compose needs at least one BC")
+    n = len(bcs[0].shape)
+    if len(bcs) != n:
+        raise DeoArgError(2, "There must be enough BCs to cover every dimension - check that the number of "
+                             "MultiDimBCs == N")
+    axes = [b.axis for b in bcs]
+    if len(set(axes)) != len(axes):
+        raise DeoArgError(2, "There are multiple boundary conditions that extend along the same dimension - make "
+                             "sure every dimension has a unique extension")
+    return ComposedMultiDimBC(sorted(bcs, key=lambda b: b.axis))
+
+
+def MultiDimBC(bc: AtomicBC, s: Sequence[int], dim: int | None = None):
+    """MultiDimBC{dim}(BC, s) / MultiDimBC(BC, s) (multi_dim_bc_operators.jl:93-110)."""
+    if dim is not None:
+        return MultiDimDirectionalBC(bc, dim, s)
+    return tuple(MultiDimDirectionalBC(bc, k + 1, s) for k in range(len(s)))
+
+
+# ---------------------------------------------------------------------------
+# L*Q and combinations
+# ---------------------------------------------------------------------------
+class FieldCoefficient:
+    """An operator whose coefficient is a full field: it acts on each line
+    with coefficients = the field along that line (the reference builds one
+    operator per line for this)."""
+
+    def __init__(self, op: DerivativeOperator, field):
+        self.op, self.field = op, field
+
+    def __mul__(self, Q):
+        return GhostDerivativeOperator(self.op, Q, field=self.field)
+
+    def __add__(self, other):
+        return DiffEqOperatorCombination([self]) + other
+
+
+def with_field(op: DerivativeOperator, field) -> FieldCoefficient:
+    return FieldCoefficient(op, field)
+
+
+class GhostDerivativeOperator:
+    """L*Q (ghost_derivative_operator.jl:1-37)."""
+
+    def __init__(self, Lop: DerivativeOperator, Q, field=None):
+        self.L, self.Q, self.field = Lop, Q, field
+
+    def terms(self):
+        return [self]
+
+    def __add__(self, other):
+        return DiffEqOperatorCombination([self]) + other
+
+    def __mul__(self, u):
+        return _apply_terms(self.terms(), u)
+
+    def size(self):
+        return (self.L.len, self.L.len)
+
+    def array(self, N: int | None = None):
+        """Array(L*Q) = (Array(L)*Q_L, Array(L)*Q_b) (concretization.jl:914-918), 1-D."""
+        if not isinstance(self.Q, AtomicBC):
+            raise DeoArgError(2, "Array(L*Q) is defined here for atomic BCs; use concretize() for N-D")
+        A = self.L.array()
+        QL, Qb = self.Q.array(self.L.len)
+        return A @ QL, A @ Qb
+
+
+class DiffEqOperatorCombination:
+    """L1 + L2 + ... (composite_operators.jl:15-83)."""
+
+    def __init__(self, ops: list):
+        self.ops = list(ops)
+
+    def __add__(self, other):
+        if isinstance(other, DiffEqOperatorCombination):
+            return DiffEqOperatorCombination(self.ops + other.ops)
+        if isinstance(other, (DerivativeOperator, GhostDerivativeOperator, FieldCoefficient)):
+            return DiffEqOperatorCombination(self.ops + [other])
+        return NotImplemented
+
+    def __mul__(self, other):
+        if isinstance(other, (AtomicBC, MultiDimensionalBC)):
+            # L*Q for a combination: sum(op -> op*Q, ops) (ghost_derivative_operator.jl:11-13)
+            return DiffEqOperatorCombination([op * other for op in self.ops])
+        if all(isinstance(o, GhostDerivativeOperator) for o in self.ops):
+            return _apply_terms(self.ops, other)
+        raise DeoArgError(2, "apply a boundary condition first: (A*Q)*u")
+
+    def terms(self):
+        return self.ops
+
+
+# ---------------------------------------------------------------------------
+# plans and application
+# ---------------------------------------------------------------------------
+class Plan:
+    """A compiled deo_plan for (terms, Julia size, dtype)."""
+
+    def __init__(self, ghosts: Sequence[GhostDerivativeOperator], shape: Sequence[int], dtype_code: int,
+                 path: int = L.DEO_PATH_AUTO):
+        nd = len(shape)
+        terms = (Term * len(ghosts))()
+        self._keep = []
+        self.shape = tuple(int(n) for n in shape)
+        self.dtype_code = dtype_code
+        self.fields = []
+        for i, g in enumerate(ghosts):
+            ax = g.L.axis
+            if isinstance(g.Q, AtomicBC):
+                if nd > 1 and ax != 1:
+                    raise DeoShapeError(1, "an atomic BC on an N-D array extends dimension 1 "
+                                           "(multi_dim_bc_operators.jl:210); use MultiDimBC for other axes")
+                bc = g.Q
+            else:
+                if tuple(g.Q.shape) != self.shape:
+                    raise DeoShapeError(1, f"BC built for size {g.Q.shape}, array has size {self.shape}")
+                bc = g.Q.bc_for(ax, nd)
+            self._keep.append(bc)
+            terms[i].op = g.L._h
+            terms[i].axis = ax
+            terms[i].bc = C.pointer(bc._s)
+            terms[i].path = path
+            if g.field is not None:
+                f = g.field
+                _check_layout(f, "coefficient field")
+                if tuple(f.shape) != self.shape:
+                    raise DeoShapeError(1, "coefficient field must have the array's size")
+                self.fields.append(f)
+                terms[i].coeff_field = C.c_void_p(f.data_ptr())
+            else:
+                terms[i].coeff_field = None
+        sizes = (C.c_int64 * nd)(*self.shape)
+        h = C.c_void_p()
+        check(L.lib().deo_plan_create(nd, sizes, dtype_code, len(ghosts), terms, C.byref(h)))
+        self._h = h
+        self._ops = [g.L for g in ghosts]  # keep operators alive
+
+    def __del__(self):
+        try:
+            if self._h:
+                L.lib().deo_plan_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def table_bytes(self) -> int:
+        return int(L.lib().deo_plan_table_bytes(self._h))
+
+    def _check(self, u, du):
+        if tuple(u.shape) != self.shape or tuple(du.shape) != self.shape:
+            raise DeoShapeError(1, f"plan is for size {self.shape}; got {tuple(u.shape)} -> {tuple(du.shape)}")
+        _check_layout(u, "u")
+        _check_layout(du, "du")
+        if _dtype_code(u) != self.dtype_code or _dtype_code(du) != self.dtype_code:
+            raise DeoArgError(2, "dtype does not match the plan")
+        if not (u.is_cuda and du.is_cuda):
+            raise DeoArgError(2, "device tensors required (use apply_host for host arrays)")
+
+    def apply(self, u, du, overwrite: bool = True):
+        self._check(u, du)
+        check(L.lib().deo_apply(self._h, C.c_void_p(u.data_ptr()), C.c_void_p(du.data_ptr()), int(bool(overwrite)),
+                                _stream_ptr()))
+        return du
+
+    def adjoint(self, dbar, ubar, overwrite: bool = True):
+        self._check(dbar, ubar)
+        check(L.lib().deo_apply_adjoint(self._h, C.c_void_p(dbar.data_ptr()), C.c_void_p(ubar.data_ptr()),
+                                        int(bool(overwrite)), _stream_ptr()))
+        return ubar
+
+    def apply_host(self, u: np.ndarray, du: np.ndarray, stream=None):
+        assert u.flags.f_contiguous and du.flags.f_contiguous
+        check(L.lib().deo_apply_host(self._h, C.c_void_p(u.ctypes.data), C.c_void_p(du.ctypes.data),
+                                     stream if stream is not None else _stream_ptr()))
+        return du
+
+    def concretize(self):
+        n = int(np.prod(self.shape))
+        Al = np.zeros((n, n), order="F")
+        Ab = np.zeros(n)
+        check(L.lib().deo_plan_concretize(self._h, Al.ctypes.data_as(_dp), _ptr(Ab)))
+        return Al, Ab
+
+
+_plan_cache: dict = {}
+
+
+def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO) -> Plan:
+    key = (tuple(id(g) for g in ghosts), tuple(shape), dtype_code, path,
+           tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts))
+    p = _plan_cache.get(key)
+    if p is None:
+        p = Plan(ghosts, shape, dtype_code, path)
+        # keep the ghosts alive with the plan so ids stay unique
+        p._ghosts = list(ghosts)
+        _plan_cache[key] = p
+    return p
+
+
+def clear_plan_cache():
+    _plan_cache.clear()
+
+
+def _apply_terms(ghosts, u, du=None, overwrite=True):
+    if isinstance(u, np.ndarray):
+        uf = np.asfortranarray(u, dtype=np.float64 if u.dtype != np.float32 else np.float32)
+        code = L.DEO_F64 if uf.dtype == np.float64 else L.DEO_F32
+        p = plan_for(ghosts, uf.shape, code)
+        out = np.zeros(uf.shape, dtype=uf.dtype, order="F") if du is None else du
+        if not overwrite:
+            raise DeoArgError(2, "host arrays support overwrite=True only")
+        return p.apply_host(uf, out)
+    p = plan_for(ghosts, tuple(u.shape), _dtype_code(u))
+    if du is None:
+        du = julia_array(tuple(u.shape), u.dtype, u.device)
+    return p.apply(u, du, overwrite)
+
+
+def mul_(du, A, u, overwrite: bool = True):
+    """mul!(du, A, u) for A = L*Q or a combination of L*Q terms
+    (ghost_derivative_operator.jl:15-24, composite_operators.jl:76-83)."""
+    return _apply_terms(A.terms(), u, du, overwrite)
+
+
+def _mul_padded_vector(op: DerivativeOperator, x):
+    """L*x for an already padded Vector x of length len+2 (generic methods,
+    convolutions.jl:17-22): the ghosts are x[0] and x[end]."""
+    torch = _torch()
+    if isinstance(x, np.ndarray) or x.dim() != 1:
+        raise DeoArgError(2, "L*x takes a 1-D device vector of length len+2")
+    if x.shape[0] != op.len + 2:
+        raise DeoShapeError(1, f"length(x) = {x.shape[0]} but the operator needs len+2 = {op.len + 2}")
+    xs = x.detach().to("cpu", torch.float64)
+    s = BCStruct()
+    s.kind = L.DEO_BC_AFFINE
+    s.m_l = s.m_r = 0
+    s.b_l, s.b_r = float(xs[0]), float(xs[-1])
+    q = AtomicBC(s, "padding")
+    g = GhostDerivativeOperator(op, q)
+    p = Plan([g], (op.len,), _dtype_code(x), L.DEO_PATH_GENERIC)
+    u = x[1:-1].contiguous()
+    du = torch.empty_like(u)
+    return p.apply(u, du)
+
+
+def concretize(A, shape, dtype=np.float64):
+    """(A_l, A_b) of u -> A*u on the device by unit-vector probes (checking only)."""
+    ghosts = A.terms()
+    p = Plan(ghosts, shape, L.DEO_F64)
+    return p.concretize()

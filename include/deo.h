@@ -1,0 +1,221 @@
+/*
+ * deo.h -- C ABI of libdeo, a GB300 (sm_103a) implementation of the
+ * stencil-apply path of DiffEqOperators.jl (`L*Q*u`, `mul!`).
+ *
+ * Conventions
+ *   - Arrays are column-major with axis 1 contiguous, exactly as Julia lays
+ *     out an Array/CuArray.  `sizes[k]` is Julia's `size(u, k+1)`.
+ *   - Device buffers are plain device pointers (CuArray's pointer, a torch
+ *     tensor's data_ptr).  Streams are passed as `void*` (a cudaStream_t;
+ *     NULL = legacy default stream).
+ *   - Every entry point returns a deo_status; no exception or device trap
+ *     crosses the ABI.  deo_last_error() gives a per-thread message.
+ *   - Operators (deo_operator) and boundary conditions (deo_bc) are host
+ *     objects built either by the constructors below (which restate the
+ *     reference's constructors) or from the tables a Julia DerivativeOperator
+ *     already holds (deo_operator_from_tables).
+ *   - A plan binds terms (operator, axis, boundary condition) to an array
+ *     shape and dtype, uploads its tables once, and is immutable afterwards:
+ *     it may be shared by host threads and used on any stream.  deo_apply
+ *     allocates nothing and does not synchronise.
+ */
+#ifndef DEO_H
+#define DEO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DEO_ABI_VERSION 1
+#define DEO_MAX_BC 16      /* longest ghost stencil a_l / a_r */
+#define DEO_MAX_TERMS 8    /* terms in one plan */
+#define DEO_MAX_DIMS 8
+
+typedef enum {
+    DEO_OK = 0,
+    DEO_ERR_BAD_SHAPE = 1,   /* reference: AssertionError / DimensionMismatch */
+    DEO_ERR_BAD_ARG = 2,     /* reference: AssertionError / ArgumentError */
+    DEO_ERR_UNSUPPORTED = 3,
+    DEO_ERR_CUDA = 4,
+    DEO_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+    DEO_ERR_OOM = 6,
+    DEO_ERR_NOT_READY = 7,   /* serving: result not finished yet */
+    DEO_ERR_REJECTED = 8     /* serving: admission refused */
+} deo_status;
+
+typedef enum { DEO_F64 = 0, DEO_F32 = 1 } deo_dtype;
+
+typedef struct deo_operator deo_operator;
+typedef struct deo_plan deo_plan;
+
+/* Per-thread message of the last failing call ("" if none). */
+const char* deo_last_error(void);
+int deo_abi_version(void);
+
+/* ------------------------------------------------------------------------
+ * Finite-difference weights.
+ * Replaces calculate_weights(order, x0, x), src/derivative_operators/fornberg.jl:7-62
+ * (Fornberg's recurrence with the centre row-sum correction).
+ * ---------------------------------------------------------------------- */
+deo_status deo_calculate_weights(int order, double x0, const double* x, int n, double* out);
+
+/* ------------------------------------------------------------------------
+ * Operators.  dx has ndx = 1 entry (uniform grid) or len+1 entries.
+ * ---------------------------------------------------------------------- */
+/* CenteredDifference{N}(d, a, dx, len), derivative_operator.jl:81-135 (uniform), :150-205 (non-uniform) */
+deo_status deo_centered_difference(int derivative_order, int approximation_order, const double* dx,
+                                   int ndx, int len, deo_operator** out);
+/* UpwindDifference{N}(d, a, dx, len; offside), derivative_operator.jl:454-512 (uniform), :515-639 (non-uniform) */
+deo_status deo_upwind_difference(int derivative_order, int approximation_order, const double* dx, int ndx,
+                                 int len, int offside, deo_operator** out);
+
+/* The fields of a DerivativeOperator (derivative_operator.jl:14-29), flattened.
+ * Tables are row-major [halves][rows][width]; halves = 2 only for a
+ * non-uniform UpwindDifference (row 1 upwind, row 2 downwind, as its
+ * SMatrix stencils are stored), else 1. */
+typedef struct {
+    int derivative_order;
+    int approximation_order;
+    int len;
+    int stencil_length;
+    int boundary_stencil_length;
+    int boundary_point_count;
+    int offside;
+    int winding;          /* 0 CenteredDifference, 1 UpwindDifference */
+    int uniform;          /* 1: dx::Number (one stencil row), 0: dx::Vector */
+    int coeff_func_sign;  /* +1 coeff_func is a Number >= 0, -1 a Number < 0, 0 otherwise */
+    int n_stencil_rows;   /* rows per half */
+    int n_low_rows;
+    int n_high_rows;
+    const double* stencil_coefs;
+    const double* low_boundary_coefs;
+    const double* high_boundary_coefs;
+    const double* coefficients; /* [len] */
+} deo_operator_desc;
+
+/* Build an operator from a DerivativeOperator's own tables (the Julia shim
+ * passes L.stencil_coefs etc.); the tables are copied. */
+deo_status deo_operator_from_tables(const deo_operator_desc* desc, deo_operator** out);
+/* Pointers in *desc stay valid until the operator is modified or destroyed. */
+deo_status deo_operator_describe(const deo_operator* op, deo_operator_desc* desc);
+/* coefficients = 0 .+ c  (compute_coeffs!, coefficient_functions.jl:7-15); n = 1 or len */
+deo_status deo_operator_set_coefficients(deo_operator* op, const double* c, int n, int coeff_func_sign);
+/* coefficients = c .* coefficients  (c*L, derivative_operator_functions.jl:165-197); n = 1 or len */
+deo_status deo_operator_scale_coefficients(deo_operator* op, const double* c, int n);
+deo_status deo_operator_clone(const deo_operator* op, deo_operator** out);
+void deo_operator_destroy(deo_operator* op);
+/* Array(L) (concretization.jl:8-52 centred, :556-671 upwind): len x (len+2), column-major. */
+deo_status deo_operator_array(const deo_operator* op, double* out);
+
+/* ------------------------------------------------------------------------
+ * Boundary conditions: the affine ghost map of an AffineBC
+ * (ghost_l = a_l . u[1:m_l] + b_l, ghost_r = a_r . u[end-m_r+1:end] + b_r),
+ * or PeriodicBC.  bc_operators.jl:1-196.
+ * ---------------------------------------------------------------------- */
+#define DEO_BC_AFFINE 0
+#define DEO_BC_PERIODIC 1
+typedef struct {
+    int kind;
+    int m_l, m_r;
+    double a_l[DEO_MAX_BC];
+    double a_r[DEO_MAX_BC];
+    double b_l, b_r;
+} deo_bc;
+
+/* RobinBC(l, r, dx, order), bc_operators.jl:26-60.  l = (α, β, γ). */
+deo_status deo_robin_bc(const double* l, const double* r, const double* dx, int ndx, int order, deo_bc* out);
+/* GeneralBC(αl, αr, dx, order), bc_operators.jl:90-169. */
+deo_status deo_general_bc(const double* alpha_l, int nl, const double* alpha_r, int nr, const double* dx,
+                          int ndx, int order, deo_bc* out);
+/* DirichletBC(l, r) = RobinBC((1,0,l),(1,0,r),1,2), bc_operators.jl:175-177; Dirichlet0BC: l = r = 0. */
+deo_status deo_dirichlet_bc(double l, double r, deo_bc* out);
+/* NeumannBC((l, r), dx, order) = RobinBC((0,1,l),(0,1,r),dx,order), bc_operators.jl:173-174. */
+deo_status deo_neumann_bc(double l, double r, const double* dx, int ndx, int order, deo_bc* out);
+/* PeriodicBC(T), bc_operators.jl:17-19. */
+deo_status deo_periodic_bc(deo_bc* out);
+/* Array(Q, N) -> (Q_L (N+2) x N column-major, Q_b[N+2]), concretization.jl:187-192, :227-230. */
+deo_status deo_bc_array(const deo_bc* bc, int n, double* QL, double* Qb);
+
+/* ------------------------------------------------------------------------
+ * Plans: sum_t (L_t * Q_t) * u over an N-D array.
+ *   ndims == 1 follows the reference's BoundaryPaddedVector methods
+ *   (convolutions.jl:367-730, reached by `L*Q*u` on a Vector); ndims > 1
+ *   follows the per-line generic methods reached through MultiDimBC padding
+ *   (derivative_operator_functions.jl:27-69, convolutions.jl:27-362,
+ *   multi_dim_bc_operators.jl:212-252).  Terms are summed left to right as
+ *   `sum(op -> op*u, ops)` does (composite_operators.jl:64-65).
+ *   coeff_field (device pointer, same shape and dtype as u, or NULL) makes
+ *   term t act on every line with coefficients = the field along that line:
+ *   the reference's one-operator-per-line construction of a field coefficient.
+ * ---------------------------------------------------------------------- */
+#define DEO_PATH_AUTO 0      /* padded-vector methods if ndims == 1, else generic */
+#define DEO_PATH_PADDED 1    /* BoundaryPaddedVector methods (convolutions.jl:367-730) */
+#define DEO_PATH_GENERIC 2   /* AbstractVector methods (convolutions.jl:27-362), e.g. `L*x` on a padded Vector */
+typedef struct {
+    const deo_operator* op;
+    int axis;                 /* 1-based, Julia's N in CenteredDifference{N} */
+    const deo_bc* bc;         /* applied along `axis` to every line */
+    const void* coeff_field;  /* device pointer or NULL */
+    int path;                 /* DEO_PATH_* */
+} deo_term;
+
+deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
+                           deo_plan** out);
+void deo_plan_destroy(deo_plan* plan);
+/* Device bytes held by the plan's tables. */
+size_t deo_plan_table_bytes(const deo_plan* plan);
+
+/* mul!(du, A*Q, u): du = sum_t L_t Q_t u  (overwrite = 1), or du += ... (overwrite = 0,
+ * the reference's `mul!(x, L, M; overwrite=false)`, convolutions.jl:17-22).
+ * Replaces LinearAlgebra.mul!(out, A::GhostDerivativeOperator, u)
+ * (ghost_derivative_operator.jl:15-24) and `(A*Q)*u` (ghost_derivative_operator.jl:26-37,
+ * composite_operators.jl:64-65).  u and du must not overlap. */
+deo_status deo_apply(const deo_plan* plan, const void* u, void* du, int overwrite, void* stream);
+
+/* Same, reading u from host memory and writing du to host memory (copies
+ * through the plan's staging buffers on `stream`; synchronises before return). */
+deo_status deo_apply_host(deo_plan* plan, const void* u_host, void* du_host, void* stream);
+
+/* Adjoint of the linear part: ubar = A_l^T dbar, where (A_l, A_b) = Array(L*Q)
+ * (concretization.jl:914-918) of the map deo_apply computes.  No reference
+ * counterpart (the reference's adjoint(L) returns L, abstract_operator_functions.jl:130-135). */
+deo_status deo_apply_adjoint(const deo_plan* plan, const void* dbar, void* ubar, int overwrite, void* stream);
+
+/* Concretisation on the device: A_l (n x n, column-major, n = prod(sizes)) and
+ * A_b (n) of the affine map, by applying the plan to unit vectors in batches.
+ * For checking small operators (n <= 8192).  Allocates device scratch. */
+deo_status deo_plan_concretize(const deo_plan* plan, double* A_l_host, double* A_b_host);
+
+/* ------------------------------------------------------------------------
+ * Batched applies: many independent (plan, u, du) instances in ONE launch of
+ * a persistent kernel that pulls tiles from a work-list.  No reference
+ * counterpart (the reference applies one operator per call).
+ * ---------------------------------------------------------------------- */
+typedef struct deo_batch deo_batch;
+typedef struct {
+    const deo_plan* plan;
+    const void* u;
+    void* du;
+} deo_instance;
+/* tile = points per work item (0 = autotuned), ctas_per_sm (0 = autotuned). */
+deo_status deo_batch_create(int n, const deo_instance* inst, int adjoint, int tile, int ctas_per_sm,
+                            deo_batch** out);
+/* Runs the batch; with use_graph = 1 the launch is captured once into a CUDA
+ * graph and replayed. */
+deo_status deo_batch_run(deo_batch* b, int use_graph, void* stream);
+/* Re-point instance i at new buffers (same plan); invalidates the graph. */
+deo_status deo_batch_set_buffers(deo_batch* b, int i, const void* u, void* du);
+deo_status deo_batch_config(const deo_batch* b, int* tile, int* ctas_per_sm, int64_t* n_items);
+void deo_batch_destroy(deo_batch* b);
+/* Autotuner: times candidate (tile, ctas_per_sm) pairs on this batch and
+ * keeps the fastest; results are cached per workload signature in the file
+ * `cache_path` (NULL = in-process cache only). */
+deo_status deo_batch_autotune(deo_batch* b, const char* cache_path, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DEO_H */

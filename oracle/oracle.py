@@ -1,0 +1,324 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle restates DiffEqOperators.jl's stencil-apply path in C++
+(``deo_oracle.cpp``).  Only the test-suite, the smoke check and the bench's
+CPU-baseline leg import this module; the product package never does.
+
+Arrays follow Julia's layout: N-D arrays are column-major (axis 1 contiguous),
+so numpy arrays passed here are Fortran-ordered.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libdeo_oracle.so")
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, a few seconds)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "deo_oracle.cpp"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.orc_julia_powi.restype = C.c_double
+        L.orc_julia_powi.argtypes = [C.c_double, C.c_long]
+        L.orc_calculate_weights.argtypes = [C.c_int, C.c_double, _dp, C.c_int, _dp]
+        L.orc_centered.restype = C.c_void_p
+        L.orc_centered.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.c_int]
+        L.orc_upwind.restype = C.c_void_p
+        L.orc_upwind.argtypes = [C.c_int, C.c_int, _dp, C.c_int, C.c_int, C.c_int]
+        L.orc_op_free.argtypes = [C.c_void_p]
+        L.orc_op_abs.restype = C.c_void_p
+        L.orc_op_abs.argtypes = [C.c_void_p]
+        L.orc_op_info.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+        L.orc_op_tables.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.orc_op_set_coeff.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int]
+        L.orc_op_scale_coeff.argtypes = [C.c_void_p, _dp, C.c_int]
+        L.orc_robin.argtypes = [_dp, _dp, _dp, C.c_int, C.c_int, C.c_void_p]
+        L.orc_general.argtypes = [_dp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.c_void_p]
+        L.orc_bc_size.restype = C.c_int
+        L.orc_bc_ghosts.argtypes = [C.c_void_p, _dp, C.c_long, _dp, _dp]
+        L.orc_mul_generic.argtypes = [C.c_void_p, _dp, _dp, C.c_int]
+        L.orc_mul_padded.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp, _dp, C.c_int]
+        L.orc_apply_nd.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
+                                   C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, _dp, C.c_int, C.c_int]
+        L.orc_abs_scale_nd.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
+                                       C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, _dp]
+        L.orc_array_op.argtypes = [C.c_void_p, _dp]
+        L.orc_array_bc.argtypes = [C.c_void_p, C.c_long, _dp, _dp]
+        L.orc_ssprk3.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
+                                 C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, C.c_double, C.c_int, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(x) -> np.ndarray:
+    return np.ascontiguousarray(np.atleast_1d(np.asarray(x, dtype=np.float64)).ravel())
+
+
+def julia_powi(x: float, n: int) -> float:
+    return lib().orc_julia_powi(float(x), int(n))
+
+
+def calculate_weights(order: int, x0: float, x: Sequence[float]) -> np.ndarray:
+    xv = _f64(x)
+    out = np.zeros_like(xv)
+    if lib().orc_calculate_weights(order, float(x0), _ptr(xv), len(xv), _ptr(out)) != 0:
+        raise AssertionError("Not enough points for the requested order.")
+    return out
+
+
+class Op:
+    """A DerivativeOperator built by the oracle's restated constructors."""
+
+    def __init__(self, handle, axis: int):
+        if not handle:
+            raise AssertionError("invalid operator arguments")
+        self.h = C.c_void_p(handle)
+        self.axis = axis
+        info = (C.c_int * 13)()
+        lib().orc_op_info(self.h, info)
+        (self.d, self.a, self.len, self.stl, self.bstl, self.bpc, self.off, wind, uniform,
+         self.n_st, self.n_low, self.n_high, self.coeff_func_sign) = list(info)
+        self.wind, self.uniform = bool(wind), bool(uniform)
+
+    def __del__(self):
+        try:
+            lib().orc_op_free(self.h)
+        except Exception:
+            pass
+
+    def tables(self):
+        halves = 2 if (self.wind and not self.uniform) else 1
+        st = np.zeros(halves * self.n_st * self.stl)
+        lo = np.zeros(max(1, halves * self.n_low * self.bstl))
+        hi = np.zeros(max(1, halves * self.n_high * self.bstl))
+        co = np.zeros(self.len)
+        lib().orc_op_tables(self.h, _ptr(st), _ptr(lo), _ptr(hi), _ptr(co))
+        return (st.reshape(halves, self.n_st, self.stl),
+                lo[: halves * self.n_low * self.bstl].reshape(halves, self.n_low, self.bstl),
+                hi[: halves * self.n_high * self.bstl].reshape(halves, self.n_high, self.bstl),
+                co)
+
+    def set_coefficients(self, c, coeff_func_sign: int = 0):
+        cv = _f64(c)
+        lib().orc_op_set_coeff(self.h, _ptr(cv), len(cv), int(coeff_func_sign))
+        self.coeff_func_sign = int(coeff_func_sign)
+        return self
+
+    def scale(self, c):
+        cv = _f64(c)
+        lib().orc_op_scale_coeff(self.h, _ptr(cv), len(cv))
+        return self
+
+    def abs(self) -> "Op":
+        """|tables| and |coefficients| (for the sum|c_k u_k| tolerance).  Sign
+        decisions of upwind rows follow |coefficients| >= 0, so use this only
+        with the upwind direction frozen (see abs_terms)."""
+        return Op(lib().orc_op_abs(self.h), self.axis)
+
+    def array(self) -> np.ndarray:
+        M = np.zeros((self.len, self.len + 2), order="F")
+        lib().orc_array_op(self.h, M.ctypes.data_as(_dp))
+        return M
+
+    def mul_generic(self, x, out=None, overwrite=True) -> np.ndarray:
+        xv = _f64(x)
+        assert len(xv) == self.len + 2
+        o = np.zeros(self.len) if out is None else out
+        lib().orc_mul_generic(self.h, _ptr(xv), _ptr(o), int(overwrite))
+        return o
+
+    def mul_padded(self, l, u, r, out=None, overwrite=True) -> np.ndarray:
+        uv = _f64(u)
+        o = np.zeros(self.len) if out is None else out
+        lib().orc_mul_padded(self.h, float(l), float(r), _ptr(uv), _ptr(o), int(overwrite))
+        return o
+
+
+def _dx_arg(dx):
+    dxv = _f64(dx)
+    return dxv, len(dxv)
+
+
+def centered(d: int, a: int, dx, length: int, coeff=None, axis: int = 1) -> Op:
+    dxv, n = _dx_arg(dx)
+    op = Op(lib().orc_centered(d, a, _ptr(dxv), n, length), axis)
+    if coeff is not None:
+        op.set_coefficients(coeff, 1 if np.ndim(coeff) == 0 and coeff >= 0 else (-1 if np.ndim(coeff) == 0 else 0))
+    return op
+
+
+def upwind(d: int, a: int, dx, length: int, coeff=None, offside: int = 0, axis: int = 1) -> Op:
+    dxv, n = _dx_arg(dx)
+    op = Op(lib().orc_upwind(d, a, _ptr(dxv), n, length, offside), axis)
+    if coeff is not None:
+        sign = 0
+        if np.ndim(coeff) == 0:
+            sign = 1 if coeff >= 0 else -1
+        op.set_coefficients(coeff, sign)
+    return op
+
+
+class BC(C.Structure):
+    _fields_ = [("kind", C.c_int), ("ml", C.c_int), ("mr", C.c_int),
+                ("al", C.c_double * 32), ("ar", C.c_double * 32),
+                ("bl", C.c_double), ("br", C.c_double)]
+
+    @property
+    def a_l(self):
+        return np.array(self.al[: self.ml])
+
+    @property
+    def a_r(self):
+        return np.array(self.ar[: self.mr])
+
+    def ghosts(self, u):
+        uv = _f64(u)
+        l, r = C.c_double(), C.c_double()
+        lib().orc_bc_ghosts(C.byref(self), _ptr(uv), len(uv), C.byref(l), C.byref(r))
+        return l.value, r.value
+
+    def array(self, N: int):
+        QL = np.zeros((N + 2, N), order="F")
+        Qb = np.zeros(N + 2)
+        lib().orc_array_bc(C.byref(self), N, QL.ctypes.data_as(_dp), _ptr(Qb))
+        return QL, Qb
+
+
+def robin(l, r, dx, order: int = 1) -> BC:
+    q = BC()
+    lv, rv = _f64(l), _f64(r)
+    dxv, n = _dx_arg(dx)
+    if lib().orc_robin(_ptr(lv), _ptr(rv), _ptr(dxv), n, order, C.byref(q)) != 0:
+        raise ValueError("order too large")
+    return q
+
+
+def general(al, ar, dx, order: int = 1) -> BC:
+    q = BC()
+    alv, arv = _f64(al), _f64(ar)
+    dxv, n = _dx_arg(dx)
+    if lib().orc_general(_ptr(alv), len(alv), _ptr(arv), len(arv), _ptr(dxv), n, order, C.byref(q)) != 0:
+        raise ValueError("order too large")
+    return q
+
+
+def dirichlet(l: float, r: float) -> BC:
+    """DirichletBC(αl, αr) = RobinBC((1,0,αl), (1,0,αr), 1.0, 2) (bc_operators.jl:175-177)."""
+    return robin((1.0, 0.0, l), (1.0, 0.0, r), 1.0, 2)
+
+
+def dirichlet0() -> BC:
+    return dirichlet(0.0, 0.0)
+
+
+def neumann(a, dx, order: int = 1) -> BC:
+    return robin((0.0, 1.0, a[0]), (0.0, 1.0, a[1]), dx, order)
+
+
+def neumann0(dx, order: int = 1) -> BC:
+    return neumann((0.0, 0.0), dx, order)
+
+
+def periodic() -> BC:
+    q = BC()
+    q.kind = 1
+    return q
+
+
+class _Args:
+    """ctypes argument block shared by apply / abs_scale / ssprk3."""
+
+    def __init__(self, terms, u: np.ndarray):
+        self.u = np.asfortranarray(u, dtype=np.float64)
+        self.sizes = (C.c_long * self.u.ndim)(*self.u.shape)
+        n = self.n = len(terms)
+        self.ops = (C.c_void_p * n)(*[t[0].h.value for t in terms])
+        self.axes = (C.c_int * n)(*[t[0].axis for t in terms])
+        self.bcs = (BC * n)(*[t[1] for t in terms])
+        self.keep, self.fptrs = [], (_dp * n)()
+        for i, t in enumerate(terms):
+            f = t[2] if len(t) > 2 else None
+            if f is not None:
+                f = np.asfortranarray(f, dtype=np.float64)
+                self.keep.append(f)
+                self.fptrs[i] = f.ctypes.data_as(_dp)
+            else:
+                self.fptrs[i] = _dp()
+
+    def head(self):
+        return (self.n, self.ops, self.axes, C.cast(self.bcs, C.c_void_p), self.fptrs, self.u.ndim, self.sizes)
+
+
+def apply(terms, u: np.ndarray, out: np.ndarray | None = None, overwrite: bool = True,
+          nthreads: int = 1) -> np.ndarray:
+    """sum_t (L_t*Q_t)*u.  terms: list of (Op, BC[, field]); u Fortran-ordered."""
+    a = _Args(terms, u)
+    o = np.zeros(a.u.shape, order="F") if out is None else out
+    rc = lib().orc_apply_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp), int(overwrite),
+                            int(nthreads))
+    if rc != 0:
+        raise AssertionError("size mismatch between operator and array")
+    return o
+
+
+def abs_scale(terms, u: np.ndarray) -> np.ndarray:
+    """sum_k |c_k * u_k| per point, ghost terms expanded (parity tolerance scale)."""
+    a = _Args(terms, u)
+    o = np.zeros(a.u.shape, order="F")
+    if lib().orc_abs_scale_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp)) != 0:
+        raise AssertionError("size mismatch between operator and array")
+    return o
+
+
+def ulp_tolerance(terms, u: np.ndarray, n_ulp: float = 4.0) -> np.ndarray:
+    """Per-point tolerance: n_ulp units in the last place of sum_k |c_k u_k|."""
+    return n_ulp * np.spacing(abs_scale(terms, u))
+
+
+def ssprk3(terms, u0: np.ndarray, dt: float, nsteps: int, nthreads: int = 1) -> np.ndarray:
+    """SSP-RK3 (Shu-Osher) steps of du/dt = sum_t L_t Q_t u."""
+    a = _Args(terms, np.array(u0, dtype=np.float64, order="F", copy=True))
+    rc = lib().orc_ssprk3(*a.head(), a.u.ctypes.data_as(_dp), float(dt), int(nsteps), int(nthreads))
+    if rc != 0:
+        raise AssertionError("size mismatch")
+    return a.u
+
+
+def concretize_probe(terms, shape) -> tuple[np.ndarray, np.ndarray]:
+    """(A_l, A_b) of the affine map u -> sum_t L_t Q_t u, by unit-vector probes
+    (the reference's own convert_by_multiplication test helper,
+    test/DerivativeOperators/derivative_operators_interface.jl:102-117)."""
+    n = int(np.prod(shape))
+    zero = np.zeros(shape, order="F")
+    Ab = apply(terms, zero).ravel(order="F")
+    Al = np.zeros((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        col = apply(terms, e.reshape(shape, order="F")).ravel(order="F")
+        Al[:, j] = col - Ab
+    return Al, Ab

@@ -1,0 +1,132 @@
+"""libdeo host side on the CPU: the library loads, exports every symbol of
+include/deo.h, and its constructors give the oracle's tables bit for bit
+(no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import deo
+import oracle as O
+from deo import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "deo.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(deo_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_symbols_exported():
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    names = header_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(_lib.EXPORTED) | {n for n in names if n not in _lib.EXPORTED and hasattr(lib, n)}
+
+
+def test_abi_version():
+    assert deo.lib().deo_abi_version() == 1
+
+
+def _same(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64)), np.abs(a - b).max()
+
+
+CENTRED = [(d, a) for d in (1, 2, 3, 4) for a in (2, 3, 4, 6, 8)]
+
+
+@pytest.mark.parametrize("d,a", CENTRED)
+@pytest.mark.parametrize("grid", ["uniform", "nonuniform"])
+def test_centred_tables_bitwise(d, a, grid):
+    n = 40
+    dx = 1.0 / 41 if grid == "uniform" else np.random.default_rng(d * 10 + a).uniform(0.5, 1.5, n + 1) / n
+    P = deo.CenteredDifference(d, a, dx, n)
+    Q = O.centered(d, a, dx, n)
+    st, lo, hi, co = Q.tables()
+    _same(P.stencil_coefs, st)
+    _same(P.low_boundary_coefs, lo)
+    _same(P.high_boundary_coefs, hi)
+    _same(P.coefficients, co)
+    _same(P.array(), Q.array())
+
+
+UPWIND = [(d, a, off) for d in (1, 2, 3) for a in (1, 2, 3, 4) for off in (0, 1, 2) if off <= (d + a - 1) // 2]
+
+
+@pytest.mark.parametrize("d,a,off", UPWIND)
+@pytest.mark.parametrize("grid", ["uniform", "nonuniform"])
+def test_upwind_tables_bitwise(d, a, off, grid):
+    n = 30
+    dx = 0.1 if grid == "uniform" else np.random.default_rng(d + 7 * a + off).uniform(0.5, 1.5, n + 1) / n
+    c = np.random.default_rng(11).uniform(-1, 1, n)
+    P = deo.UpwindDifference(d, a, dx, n, c, offside=off)
+    Q = O.upwind(d, a, dx, n, c, offside=off)
+    st, lo, hi, co = Q.tables()
+    _same(P.stencil_coefs, st)
+    _same(P.low_boundary_coefs, lo)
+    _same(P.high_boundary_coefs, hi)
+    _same(P.coefficients, co)
+    _same(P.array(), Q.array())
+
+
+def test_bcs_bitwise():
+    rng = np.random.default_rng(2)
+    for order in (1, 2, 3):
+        l, r = rng.random(3), rng.random(3)
+        for dx in (0.37, rng.uniform(0.5, 1.5, 12)):
+            a = deo.RobinBC(l, r, dx, order)
+            b = O.robin(l, r, dx, order)
+            _same(a.a_l, b.a_l); _same(a.a_r, b.a_r)
+            assert a.b_l == b.bl and a.b_r == b.br
+            al, ar = rng.random(3 + order % 2), rng.random(3)
+            g, h = deo.GeneralBC(al, ar, dx, order), O.general(al, ar, dx, order)
+            _same(g.a_l, h.a_l); _same(g.a_r, h.a_r)
+            assert g.b_l == h.bl and g.b_r == h.br
+    d = deo.Dirichlet0BC()
+    assert list(d.a_l) == [0.0, 0.0] and d.b_l == 0.0
+    QL, Qb = deo.RobinBC(l, r, 0.3, 2).array(7)
+    QL2, Qb2 = O.robin(l, r, 0.3, 2).array(7)
+    _same(QL, QL2); _same(Qb, Qb2)
+
+
+def test_weights_and_errors():
+    _same(deo.calculate_weights(2, 0.0, [-2, -1, 0, 1, 2]), O.calculate_weights(2, 0.0, [-2, -1, 0, 1, 2]))
+    with pytest.raises(AssertionError):
+        deo.calculate_weights(3, 0.0, [0, 1, 2])
+    with pytest.raises(AssertionError):
+        deo.CenteredDifference(2, 1, 1.0, 10)
+    with pytest.raises(AssertionError):
+        deo.UpwindDifference(1, 1, 1.0, 10, offside=3)
+    L = deo.CenteredDifference(2, 2, 1.0, 3)
+    with pytest.raises(AssertionError):   # DimensionMismatch (derivative_operator_functions.jl:182-184)
+        np.ones(10) * L
+
+
+def test_coefficient_scaling_matches_reference_rules():
+    # derivative_operators_interface.jl:418-438
+    A = deo.CenteredDifference(2, 2, 1.0, 3)
+    C = deo.UpwindDifference(1, 1, 1.0, 3, np.array([2.0, 3.0, 4.0]))
+    c = np.array([1.0, 1.0, 3.0])
+    assert list((c * A).coefficients) == list(c)
+    assert list((c * C).coefficients) == [2.0, 3.0, 12.0]
+
+
+def test_operator_from_tables_roundtrip():
+    P = deo.UpwindDifference(2, 3, np.random.default_rng(0).uniform(0.5, 1, 21) / 20, 20, -1.0, offside=1)
+    desc = dict(derivative_order=P.derivative_order, approximation_order=P.approximation_order, len=P.len,
+                stencil_length=P.stencil_length, boundary_stencil_length=P.boundary_stencil_length,
+                boundary_point_count=P.boundary_point_count, offside=P.offside, winding=1, uniform=0,
+                coeff_func_sign=P.coeff_func_sign, n_stencil_rows=P.stencil_coefs.shape[1],
+                n_low_rows=P.low_boundary_coefs.shape[1], n_high_rows=P.high_boundary_coefs.shape[1],
+                stencil_coefs=P.stencil_coefs, low_boundary_coefs=P.low_boundary_coefs,
+                high_boundary_coefs=P.high_boundary_coefs, coefficients=P.coefficients)
+    R = deo.operator_from_tables(desc)
+    _same(R.array(), P.array())
