@@ -712,6 +712,8 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
 // ---------------------------------------------------------------------------
 struct deo_plan {
     PlanDev dev{};
+    deo::UniPlan uni{};
+    int fast_path = 1;
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     std::vector<void*> allocs;
     size_t table_bytes = 0;
@@ -829,6 +831,38 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         T.bl = q.b_l;
         T.br = q.b_r;
     }
+    // fast path for 2-D/3-D plans whose terms all have constant interior rows
+    {
+        deo::UniPlan& U = P->uni;
+        bool ok = (ndims == 2 || ndims == 3) && sizes[0] < (1LL << 30) && sizes[1] < (1LL << 30) &&
+                  (ndims < 3 || sizes[2] < (1LL << 30));
+        int H = 0;
+        for (int t = 0; t < nterms && ok; ++t) {
+            const TermDev& T = D.t[t];
+            const RowTabDev& tb = T.tab[0];
+            if (T.has_field || T.nvar != 1 || tb.ilo > tb.ihi || T.axis > 2) {
+                ok = false;
+                break;
+            }
+            deo::UniTerm& u = U.t[t];
+            u.axis = T.axis;
+            u.nk = tb.band_nk;
+            u.off0 = tb.band_p0_off - 1;
+            u.flo = std::max(tb.ilo, 2 - tb.band_p0_off);
+            u.fhi = std::min(tb.ihi, T.len + 2 - tb.band_nk - tb.band_p0_off);
+            if (u.flo > u.fhi) { u.flo = 1; u.fhi = 0; }
+            std::memcpy(u.w, tb.wband, sizeof u.w);  // already float-packed for Float32 plans
+            H = std::max(H, std::max(std::abs(u.off0), std::abs(u.off0 + u.nk - 1)));
+        }
+        if (ok && H >= 1 && H <= 4) {
+            U.enabled = 1;
+            U.radius = H;
+            U.nterms = nterms;
+            for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
+        } else {
+            U.enabled = 0;
+        }
+    }
     CUDA_TRY(cudaMalloc(&P->d_plan, sizeof(PlanDev)), "cudaMalloc(plan)");
     CUDA_TRY(cudaMemcpy(P->d_plan, &P->dev, sizeof(PlanDev), cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
     *out = P.release();
@@ -845,10 +879,24 @@ static deo_status check_ptrs(const deo_plan* p, const void* a, const void* b) {
     return DEO_OK;
 }
 
+static int launch_forward(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
+    if (p->uni.enabled && p->fast_path)
+        return deo_k_apply_uniform(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+    return deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
+}
+
+extern "C" deo_status deo_plan_set_fast_path(deo_plan* p, int enable) {
+    if (!p) return fail(DEO_ERR_BAD_ARG, "null plan");
+    p->fast_path = enable ? 1 : 0;
+    return DEO_OK;
+}
+
+extern "C" int deo_plan_uses_fast_path(const deo_plan* p) { return p && p->uni.enabled && p->fast_path; }
+
 extern "C" deo_status deo_apply(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
     deo_status s = check_ptrs(p, u, du);
     if (s != DEO_OK) return s;
-    const int e = deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
+    const int e = launch_forward(p, u, du, overwrite, stream);
     if (e) return cuda_fail((cudaError_t)e, "deo_apply launch");
     return DEO_OK;
 }
@@ -871,7 +919,7 @@ extern "C" deo_status deo_apply_host(deo_plan* p, const void* uh, void* duh, voi
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     CUDA_TRY(cudaMemcpyAsync(p->stage_u, uh, bytes, cudaMemcpyHostToDevice, st), "H2D");
-    const int e = deo_k_apply(&p->dev, p->stage_u, p->stage_du, 1, 0, stream);
+    const int e = launch_forward(p, p->stage_u, p->stage_du, 1, stream);
     if (e) return cuda_fail((cudaError_t)e, "deo_apply_host launch");
     CUDA_TRY(cudaMemcpyAsync(duh, p->stage_du, bytes, cudaMemcpyDeviceToHost, st), "D2H");
     CUDA_TRY(cudaStreamSynchronize(st), "synchronize");
@@ -935,6 +983,9 @@ extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double*
 // batched applies: one persistent launch over a work-list of tiles
 // ---------------------------------------------------------------------------
 struct deo_batch {
+    int kind = 0;  // 0 apply/adjoint batch, 1 Runge-Kutta stage batch
+    std::vector<deo::StageDev> stages;
+    deo::StageDev* d_stages = nullptr;
     std::vector<deo::InstDev> inst;
     std::vector<const deo_plan*> plans;
     int adjoint = 0, dtype = 0;
@@ -956,6 +1007,7 @@ struct deo_batch {
         drop_graph();
         if (cap) cudaStreamDestroy(cap);
         cudaFree(d_inst);
+        cudaFree(d_stages);
         cudaFree(d_items);
         cudaFree(d_counter);
     }
@@ -1012,8 +1064,42 @@ extern "C" deo_status deo_batch_create(int n, const deo_instance* in, int adjoin
 }
 
 static deo_status batch_launch(deo_batch& b, cudaStream_t st) {
-    const int e = deo_k_batch(b.d_inst, b.d_items, b.n_items, b.d_counter, b.dtype, b.adjoint, b.ctas, 256, st);
+    const int e = b.kind == 1
+                      ? deo_k_stage_batch(b.d_stages, b.d_items, b.n_items, b.d_counter, b.dtype, b.ctas, 256, st)
+                      : deo_k_batch(b.d_inst, b.d_items, b.n_items, b.d_counter, b.dtype, b.adjoint, b.ctas, 256, st);
     if (e) return cuda_fail((cudaError_t)e, "batched launch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_stage_batch_create(int n, const deo_stage* in, int tile, int ctas, deo_batch** out) {
+    if (!out || (n > 0 && !in)) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    auto b = std::make_unique<deo_batch>();
+    b->kind = 1;
+    for (int i = 0; i < n; ++i) {
+        const deo_stage& s = in[i];
+        if (!s.plan || !s.c || !s.out) return fail(DEO_ERR_BAD_ARG, "stage %d: null plan, input or output", i);
+        if (s.c == s.out) return fail(DEO_ERR_BAD_ARG, "stage %d: output must not alias the operator input", i);
+        if ((s.a == nullptr) != (s.alpha == 0.0) && s.a == nullptr)
+            return fail(DEO_ERR_BAD_ARG, "stage %d: alpha != 0 needs a", i);
+        if (s.b == nullptr && s.beta != 0.0) return fail(DEO_ERR_BAD_ARG, "stage %d: beta != 0 needs b", i);
+        if (i > 0 && s.plan->dev.dtype != in[0].plan->dev.dtype)
+            return fail(DEO_ERR_BAD_ARG, "all instances of a batch must share one dtype");
+        b->plans.push_back(s.plan);
+        b->stages.push_back(deo::StageDev{s.plan->d_plan, s.a, s.b, s.c, s.out, s.alpha, s.beta, s.gamma, s.dt,
+                                          s.adjoint ? 1 : 0, 0});
+    }
+    b->dtype = n > 0 ? in[0].plan->dev.dtype : 0;
+    if (n > 0) {
+        CUDA_TRY(cudaMalloc(&b->d_stages, n * sizeof(deo::StageDev)), "cudaMalloc(stages)");
+        CUDA_TRY(cudaMemcpy(b->d_stages, b->stages.data(), n * sizeof(deo::StageDev), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(stages)");
+    }
+    CUDA_TRY(cudaMalloc(&b->d_counter, sizeof(unsigned int)), "cudaMalloc(counter)");
+    b->ctas = ctas > 0 ? ctas : 4;
+    deo_status s = batch_items(*b, tile > 0 ? tile : 8192);
+    if (s != DEO_OK) return s;
+    *out = b.release();
     return DEO_OK;
 }
 
@@ -1041,7 +1127,8 @@ extern "C" deo_status deo_batch_run(deo_batch* b, int use_graph, void* stream) {
 }
 
 extern "C" deo_status deo_batch_set_buffers(deo_batch* b, int i, const void* u, void* du) {
-    if (!b || i < 0 || i >= (int)b->inst.size() || !u || !du || u == du) return fail(DEO_ERR_BAD_ARG, "bad argument");
+    if (!b || b->kind != 0 || i < 0 || i >= (int)b->inst.size() || !u || !du || u == du)
+        return fail(DEO_ERR_BAD_ARG, "bad argument");
     b->inst[i].u = u;
     b->inst[i].du = du;
     CUDA_TRY(cudaMemcpy(b->d_inst + i, &b->inst[i], sizeof(deo::InstDev), cudaMemcpyHostToDevice), "cudaMemcpy");

@@ -65,6 +65,29 @@ struct PlanDev {
     TermDev t[DEO_KMAX_TERMS];
 };
 
+// Fast path of a plan whose terms all have constant interior rows (uniform
+// grid, constant coefficient along the axis) on a 2-D/3-D array: the CTA
+// stages a rolling window of (2H+1) planes of (TY+2H) x (TX+2H) points in
+// shared memory and evaluates interior points from it with the band weights;
+// points whose row along some term's axis lies outside [flo, fhi] (they read
+// ghosts or use boundary rows) take the generic evaluator.
+struct UniTerm {
+    int axis;        // 0, 1, 2
+    int nk;          // taps
+    int off0;        // offset of tap 0 from the point along the axis
+    int flo, fhi;    // rows (1-based) evaluated from the band without ghosts
+    int pad_;
+    double w[DEO_MAX_NW];  // band weights (float-packed for Float32 plans)
+};
+struct UniPlan {
+    int enabled;
+    int radius;      // H = max |offset| over terms
+    int nterms;
+    int pad_;
+    int64_t n[3];    // sizes along axes 1..3 (1 for absent axes)
+    UniTerm t[DEO_KMAX_TERMS];
+};
+
 // Work item of the batched persistent kernel: `count` points starting at
 // flat index `start` of instance `inst`.
 struct WorkItem {
@@ -79,12 +102,31 @@ struct InstDev {
     void* du;
 };
 
+// One Runge-Kutta stage of one instance:
+//   out = alpha*a + beta*b + gamma*(c + dt*Op(c)),  Op = plan (or its adjoint)
+// a / b may be null (their term is then absent).  Applied point-wise, out may
+// alias a (each point reads a[idx] before writing out[idx]) but not c.
+struct StageDev {
+    const PlanDev* plan;
+    const void* a;
+    const void* b;
+    const void* c;
+    void* out;
+    double alpha, beta, gamma, dt;
+    int adjoint;
+    int pad_;
+};
+
 }  // namespace deo
 
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
                            void* stream);
+extern "C" int deo_k_apply_uniform(const deo::UniPlan* up, const deo::PlanDev* d_plan, int dtype, const void* u,
+                                   void* du, int overwrite, void* stream);
 extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items, int64_t n_items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
+extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
+                                 unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);

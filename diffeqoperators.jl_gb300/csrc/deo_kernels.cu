@@ -48,6 +48,16 @@ __device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__
     return d + T(t.br);
 }
 
+// The reference adds `!overwrite * x_temp[i]` (a strong zero) to every tap
+// sum, which turns -0.0 into +0.0 and is otherwise exact.  Applied once to the
+// final sum it has the same effect; done on the bits to spend no FP64 issue.
+__device__ __forceinline__ double zero_fix(double x) {
+    return __double_as_longlong(x) == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+__device__ __forceinline__ float zero_fix(float x) {
+    return __float_as_uint(x) == 0x80000000u ? 0.0f : x;
+}
+
 struct RowInfo {
     int p0, nk, e;
     bool band;
@@ -111,7 +121,7 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
         if (t.has_field) w = c * w;
         acc = fma(w, x, acc);
     }
-    return acc + T(0);
+    return acc;
 }
 
 // Column p of one term's L (padded space) dotted with dbar along the line.
@@ -159,7 +169,7 @@ __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ 
         const T r = ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
         acc = (tt == 0) ? r : acc + r;
     }
-    return acc;
+    return ADJ ? acc : zero_fix(acc);
 }
 
 template <typename T, bool ADJ>
@@ -195,9 +205,161 @@ __global__ void __launch_bounds__(256) k_batch(const InstDev* __restrict__ inst,
     }
 }
 
+// Batched Runge-Kutta stage: same work-list scheme; each instance may run
+// the forward operator or its adjoint (uniform per work item).
+template <typename T>
+__global__ void __launch_bounds__(256) k_stage(const StageDev* __restrict__ st, const WorkItem* __restrict__ items,
+                                               int64_t n_items, unsigned int* counter) {
+    __shared__ int64_t s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int64_t)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int64_t it = s_item;
+        __syncthreads();
+        if (it >= n_items) return;
+        const WorkItem w = items[it];
+        const StageDev S = st[w.inst];
+        const PlanDev& P = *S.plan;
+        const T* a = reinterpret_cast<const T*>(S.a);  // may alias out
+        const T* b = reinterpret_cast<const T*>(S.b);
+        const T* __restrict__ c = reinterpret_cast<const T*>(S.c);
+        T* out = reinterpret_cast<T*>(S.out);
+        const T al = T(S.alpha), be = T(S.beta), ga = T(S.gamma), dt = T(S.dt);
+        for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
+            const int64_t idx = w.start + q;
+            const T f = S.adjoint ? eval_point<T, true>(P, c, idx) : eval_point<T, false>(P, c, idx);
+            const T t = fma(dt, f, c[idx]);
+            T acc = a ? al * a[idx] : T(0);
+            if (b) acc = fma(be, b[idx], acc);
+            out[idx] = fma(ga, t, acc);
+        }
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T uni_w(const UniTerm& t, int k);
+template <>
+__device__ __forceinline__ double uni_w<double>(const UniTerm& t, int k) { return t.w[k]; }
+template <>
+__device__ __forceinline__ float uni_w<float>(const UniTerm& t, int k) {
+    return reinterpret_cast<const float*>(t.w)[k];
+}
+
+// Uniform fused apply (see UniPlan).  Block = TX x TY threads; each CTA
+// marches ZC planes along axis 3 keeping a rolling window of 2H+1 planes.
+template <typename T, int H, int TX, int TY, int ZC>
+__global__ void __launch_bounds__(TX * TY) k_uni3(const __grid_constant__ UniPlan U, const PlanDev* __restrict__ P,
+                                                  const T* __restrict__ u, T* __restrict__ du, int overwrite) {
+    constexpr int W = 2 * H + 1;
+    constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
+    __shared__ T sm[W][SY][SX];
+    const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int x = x0 + tx, y = y0 + ty;
+    const int z0 = blockIdx.z * ZC;
+    const int z1 = min(z0 + ZC, nz);
+    const int64_t sxy = (int64_t)nx * ny;
+
+    auto load_plane = [&](int z) {
+        T(*pl)[SX] = sm[((z % W) + W) % W];
+        const bool zin = (z >= 0 && z < nz);
+        for (int q = tid; q < SX * SY; q += TX * TY) {
+            const int yy = q / SX, xx = q - yy * SX;
+            const int gx = x0 + xx - H, gy = y0 + yy - H;
+            T v = T(0);
+            if (zin && gx >= 0 && gx < nx && gy >= 0 && gy < ny) v = __ldg(u + (int64_t)z * sxy + (int64_t)gy * nx + gx);
+            pl[yy][xx] = v;
+        }
+    };
+    for (int z = z0 - H; z < z0 + H; ++z) load_plane(z);
+    for (int z = z0; z < z1; ++z) {
+        load_plane(z + H);
+        __syncthreads();
+        if (x < nx && y < ny) {
+            const int64_t idx = (int64_t)z * sxy + (int64_t)y * nx + x;
+            bool fast = true;
+            for (int t = 0; t < U.nterms; ++t) {
+                const int ax = U.t[t].axis;
+                const int r = (ax == 0 ? x : (ax == 1 ? y : z)) + 1;
+                fast = fast && r >= U.t[t].flo && r <= U.t[t].fhi;
+            }
+            T total;
+            if (fast) {
+                total = T(0);
+                for (int t = 0; t < U.nterms; ++t) {
+                    const UniTerm& tm = U.t[t];
+                    T acc = T(0);
+                    for (int k = 0; k < tm.nk; ++k) {
+                        const int o = tm.off0 + k;
+                        T v;
+                        if (tm.axis == 0) v = sm[z % W][ty + H][tx + H + o];
+                        else if (tm.axis == 1) v = sm[z % W][ty + H + o][tx + H];
+                        else v = sm[(z + o + W) % W][ty + H][tx + H];
+                        acc = fma(uni_w<T>(tm, k), v, acc);
+                    }
+                    total = (t == 0) ? acc : total + acc;
+                }
+                total = zero_fix(total);
+            } else {
+                total = eval_point<T, false>(*P, u, idx);
+            }
+            du[idx] = overwrite ? total : total + du[idx];
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace deo
 
 using namespace deo;
+
+template <typename T, int H>
+static int launch_uni(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int overwrite, cudaStream_t st) {
+    constexpr int TX = 32, TY = 8, ZC = 32;
+    dim3 grid((unsigned)((up->n[0] + TX - 1) / TX), (unsigned)((up->n[1] + TY - 1) / TY),
+              (unsigned)((up->n[2] + ZC - 1) / ZC));
+    k_uni3<T, H, TX, TY, ZC><<<grid, dim3(TX, TY), 0, st>>>(*up, dp, (const T*)u, (T*)du, overwrite);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int deo_k_apply_uniform(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du,
+                                   int overwrite, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int H = up->radius;
+    if (dtype == 0) {
+        switch (H) {
+            case 1: return launch_uni<double, 1>(up, dp, u, du, overwrite, st);
+            case 2: return launch_uni<double, 2>(up, dp, u, du, overwrite, st);
+            case 3: return launch_uni<double, 3>(up, dp, u, du, overwrite, st);
+            case 4: return launch_uni<double, 4>(up, dp, u, du, overwrite, st);
+        }
+    } else {
+        switch (H) {
+            case 1: return launch_uni<float, 1>(up, dp, u, du, overwrite, st);
+            case 2: return launch_uni<float, 2>(up, dp, u, du, overwrite, st);
+            case 3: return launch_uni<float, 3>(up, dp, u, du, overwrite, st);
+            case 4: return launch_uni<float, 4>(up, dp, u, du, overwrite, st);
+        }
+    }
+    return (int)cudaErrorInvalidValue;
+}
+
+extern "C" int deo_k_num_sms(void);
+
+extern "C" int deo_k_stage_batch(const StageDev* st, const WorkItem* items, int64_t n_items, unsigned int* counter,
+                                 int dtype, int ctas_per_sm, int threads, void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int sms = deo_k_num_sms();
+    int64_t grid = (int64_t)sms * (ctas_per_sm > 0 ? ctas_per_sm : 4);
+    if (grid > n_items) grid = n_items;
+    if (grid <= 0) return 0;
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
+    if (e != cudaSuccess) return (int)e;
+    if (dtype == 0) k_stage<double><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+    else k_stage<float><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+    return (int)cudaGetLastError();
+}
 
 extern "C" int deo_k_apply(const PlanDev* p, const void* u, void* du, int overwrite, int adjoint, void* stream) {
     const int threads = 256;

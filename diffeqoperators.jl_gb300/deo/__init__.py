@@ -15,3 +15,6 @@ from .operators import (  # noqa: F401
 )
 
 mul = mul_
+from . import autodiff, batch  # noqa: E402,F401
+from .autodiff import rrule  # noqa: E402,F401
+from .batch import Batch, StageBatch  # noqa: E402,F401

@@ -63,6 +63,12 @@ class Instance(C.Structure):
     _fields_ = [("plan", _vp), ("u", _vp), ("du", _vp)]
 
 
+class Stage(C.Structure):
+    _fields_ = [("plan", _vp), ("a", _vp), ("b", _vp), ("c", _vp), ("out", _vp),
+                ("alpha", C.c_double), ("beta", C.c_double), ("gamma", C.c_double), ("dt", C.c_double),
+                ("adjoint", C.c_int)]
+
+
 _lib = None
 
 
@@ -102,11 +108,14 @@ def lib():
     proto("deo_plan_create", st, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(Term), C.POINTER(_vp))
     proto("deo_plan_destroy", None, _vp)
     proto("deo_plan_table_bytes", C.c_size_t, _vp)
+    proto("deo_plan_set_fast_path", st, _vp, C.c_int)
+    proto("deo_plan_uses_fast_path", C.c_int, _vp)
     proto("deo_apply", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_apply_host", st, _vp, _vp, _vp, _vp)
     proto("deo_apply_adjoint", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_plan_concretize", st, _vp, _dp, _dp)
     proto("deo_batch_create", st, C.c_int, C.POINTER(Instance), C.c_int, C.c_int, C.c_int, C.POINTER(_vp))
+    proto("deo_stage_batch_create", st, C.c_int, C.POINTER(Stage), C.c_int, C.c_int, C.POINTER(_vp))
     proto("deo_batch_run", st, _vp, C.c_int, _vp)
     proto("deo_batch_set_buffers", st, _vp, C.c_int, _vp, _vp)
     proto("deo_batch_config", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64))
@@ -134,7 +143,7 @@ EXPORTED = [
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
     "deo_operator_destroy", "deo_operator_array", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
-    "deo_plan_table_bytes", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
-    "deo_batch_create", "deo_batch_run", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
+    "deo_plan_table_bytes", "deo_plan_set_fast_path", "deo_plan_uses_fast_path", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
+    "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune",
 ]

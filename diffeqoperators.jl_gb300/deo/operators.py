@@ -612,6 +612,14 @@ class Plan:
     def table_bytes(self) -> int:
         return int(L.lib().deo_plan_table_bytes(self._h))
 
+    def set_fast_path(self, enable: bool):
+        check(L.lib().deo_plan_set_fast_path(self._h, int(bool(enable))))
+        return self
+
+    @property
+    def uses_fast_path(self) -> bool:
+        return bool(L.lib().deo_plan_uses_fast_path(self._h))
+
     def _check(self, u, du):
         if tuple(u.shape) != self.shape or tuple(du.shape) != self.shape:
             raise DeoShapeError(1, f"plan is for size {self.shape}; got {tuple(u.shape)} -> {tuple(du.shape)}")

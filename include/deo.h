@@ -167,6 +167,11 @@ deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int
 void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
+/* 2-D/3-D plans whose terms all have constant interior rows run a shared-
+ * memory tiled kernel for interior points; enable = 0 forces the generic
+ * row-table kernel (same arithmetic, same bits; for checking). */
+deo_status deo_plan_set_fast_path(deo_plan* plan, int enable);
+int deo_plan_uses_fast_path(const deo_plan* plan);
 
 /* mul!(du, A*Q, u): du = sum_t L_t Q_t u  (overwrite = 1), or du += ... (overwrite = 0,
  * the reference's `mul!(x, L, M; overwrite=false)`, convolutions.jl:17-22).
@@ -210,6 +215,23 @@ deo_status deo_batch_run(deo_batch* b, int use_graph, void* stream);
 deo_status deo_batch_set_buffers(deo_batch* b, int i, const void* u, void* du);
 deo_status deo_batch_config(const deo_batch* b, int* tile, int* ctas_per_sm, int64_t* n_items);
 void deo_batch_destroy(deo_batch* b);
+/* Batched Runge-Kutta stage over many instances in one persistent launch:
+ *   out = alpha*a + beta*b + gamma*(c + dt*Op(c))
+ * with Op the instance's plan (adjoint = 0) or its adjoint (adjoint = 1);
+ * a or b may be NULL (term absent); out may alias a, not c.  Three of these
+ * make one SSP-RK3 step for every active instance.  No reference counterpart
+ * (the reference leaves time stepping to OrdinaryDiffEq). */
+typedef struct {
+    const deo_plan* plan;
+    const void* a;
+    const void* b;
+    const void* c;
+    void* out;
+    double alpha, beta, gamma, dt;
+    int adjoint;
+} deo_stage;
+deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int ctas_per_sm, deo_batch** out);
+
 /* Autotuner: times candidate (tile, ctas_per_sm) pairs on this batch and
  * keeps the fastest; results are cached per workload signature in the file
  * `cache_path` (NULL = in-process cache only). */

@@ -57,6 +57,10 @@ def make_term(t, shape, rng):
     else:
         P = deo.UpwindDifference(t["d"], t["a"], dx, n, 1 if cvec is None else cvec, offside=off, axis=ax)
         Q = O.upwind(t["d"], t["a"], dx, n, 1.0 if cvec is None else cvec, offside=off, axis=ax)
+    if field is not None:
+        # a field is one operator per line built from a coefficient Vector:
+        # coeff_func is not a Number, so no coeff_func-sign branch applies
+        Q.set_coefficients(np.ones(n), 0)
     bcp, bco = make_bc(t.get("bc", ("dirichlet0",)), dx)
     return P, Q, bcp, bco, field
 

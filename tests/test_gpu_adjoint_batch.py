@@ -1,0 +1,234 @@
+"""GPU: adjoint kernel, rrule, fast path vs generic path, batched launches,
+SSP-RK3 stages and the time-integration adjoint."""
+import numpy as np
+import pytest
+
+import deo
+import oracle as O
+from cases import build, to_device, to_host
+from test_gpu_parity import ND, ONE_D, T
+
+pytestmark = pytest.mark.gpu
+EPS = np.finfo(np.float64).eps
+
+
+def _plan(A, shape):
+    return deo.plan_for(A.terms(), shape, 0)
+
+
+ADJ_CASES = [ONE_D[0], ONE_D[5], ONE_D[17], ONE_D[40], ONE_D[70], ONE_D[-1], ONE_D[-7],
+             dict(ND[0], shape=(9, 8, 7)), dict(ND[1], shape=(6, 7, 8)), dict(ND[2], shape=(6, 5, 7)),
+             dict(ND[3], shape=(14, 12)), dict(ND[4], shape=(7, 8, 9, 10)), ND[5], ND[6]]
+
+
+@pytest.mark.parametrize("case", ADJ_CASES, ids=lambda c: "x".join(map(str, c["shape"])) + f"-s{c['seed']}")
+def test_adjoint_matches_concretized_transpose(cuda, case):
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    Al, Ab = O.concretize_probe(oterms, shape)
+    rng = np.random.default_rng(5)
+    v = np.asfortranarray(rng.standard_normal(shape))
+    p = _plan(A, shape)
+    ub = deo.julia_array(shape)
+    p.adjoint(to_device(v), ub)
+    got = to_host(ub).ravel(order="F")
+    ref = Al.T @ v.ravel(order="F")
+    scale = np.abs(Al).T @ np.abs(v.ravel(order="F"))
+    assert np.all(np.abs(got - ref) <= 64 * EPS * scale + 1e-300)
+    # the device concretisation is the same matrix
+    Dl, Db = p.concretize()
+    assert np.allclose(Dl, Al, rtol=1e-12, atol=1e-12 * np.abs(Al).max())
+    assert np.allclose(Db, Ab, rtol=1e-12, atol=1e-12 * max(1.0, np.abs(Ab).max()))
+
+
+@pytest.mark.parametrize("d,a,bc", [(2, 2, ("robin", (1.0, 0.5, 0.2), (0.7, 0.3, -0.1), 1)), (1, 4, ("dirichlet0",)),
+                                    (2, 4, ("general", (-1.0, 1.0, 0.5), (0.5, 1.0, 0.25), 2)), (4, 2, ("periodic",))])
+def test_adjoint_against_reference_concretization(cuda, d, a, bc):
+    # transpose of Array(L*Q) = (Array(L)*Q_L, Array(L)*Q_b) (concretization.jl:914-918)
+    case = dict(shape=(33,), terms=[T("centered", d, a, bc=bc)], seed=d + a)
+    A, oterms, u = build(case)
+    Lo, qo, _ = oterms[0]
+    QL, Qb = qo.array(33)
+    Al = Lo.array() @ QL
+    v = np.random.default_rng(3).standard_normal(33)
+    ub = deo.julia_array((33,))
+    _plan(A, (33,)).adjoint(to_device(v), ub)
+    assert np.allclose(to_host(ub), Al.T @ v, rtol=1e-11, atol=1e-11 * np.abs(Al).max() * np.abs(v).max())
+
+
+def test_rrule_and_autograd_fd(cuda):
+    import torch
+    case = ND[3]
+    A, oterms, u = build(case)
+    ud = to_device(u)
+    y, pb = deo.rrule(A, ud)
+    w = to_device(np.asfortranarray(np.random.default_rng(1).standard_normal(u.shape)))
+    _, _, ubar = pb(w)
+    v = to_device(np.asfortranarray(np.random.default_rng(2).standard_normal(u.shape)))
+    eps = 1e-3
+    lp = float((w * (A * (ud + eps * v))).sum())
+    lm = float((w * (A * (ud - eps * v))).sum())
+    fd = (lp - lm) / (2 * eps)
+    ad = float((ubar * v).sum())
+    assert abs(fd - ad) <= 1e-8 * max(1.0, abs(ad)), (fd, ad)
+    # torch autograd through the same kernels
+    ut = ud.clone().requires_grad_(True)
+    loss = (deo.autodiff.apply(A, ut) * w).sum()
+    loss.backward()
+    assert torch.equal(ut.grad, ubar)
+
+
+def test_dot_product_identity_full_size(cuda):
+    # <A_l u, v> = <u, A_l^T v> on the 256^3 Laplacian (size-independent check)
+    import torch
+    n = 256
+    h = 1.0 / (n + 1)
+    A = sum((deo.CenteredDifference(2, 4, h, n, axis=k) for k in (1, 2, 3)), deo.DiffEqOperatorCombination([]))
+    Q = deo.compose(*deo.RobinBC((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), (h, h, h), 1, (n, n, n)))
+    AQ = A * Q
+    p = _plan(AQ, (n, n, n))
+    g = torch.Generator(device="cuda").manual_seed(0)
+    u = deo.julia_array((n, n, n)); u.copy_(torch.randn(n, n, n, generator=g, device="cuda", dtype=torch.float64))
+    v = deo.julia_array((n, n, n)); v.copy_(torch.randn(n, n, n, generator=g, device="cuda", dtype=torch.float64))
+    z = deo.julia_array((n, n, n), fill=0.0)
+    Au, A0, Atv = deo.julia_array((n, n, n)), deo.julia_array((n, n, n)), deo.julia_array((n, n, n))
+    p.apply(u, Au)
+    p.apply(z, A0)  # affine part (zero for this BC)
+    p.adjoint(v, Atv)
+    lhs = float(((Au - A0) * v).sum())
+    rhs = float((u * Atv).sum())
+    assert abs(lhs - rhs) <= 1e-12 * float((Au.abs() * v.abs()).sum())
+
+
+@pytest.mark.parametrize("case", [ND[0], ND[1], ND[2], dict(ND[0], shape=(70, 45, 33)),
+                                  dict(shape=(64, 50), terms=[T("centered", 2, 6, axis=1, bc=("dirichlet0",)),
+                                                              T("centered", 1, 8, axis=2, bc=("periodic",)),
+                                                              T("upwind", 1, 2, axis=1, coeff=0.7,
+                                                                bc=("dirichlet0",))], seed=31)],
+                         ids=["lap3d", "d0", "periodic", "odd", "2d-mixed"])
+def test_fast_path_bitwise_equals_generic(cuda, case):
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    p = deo.Plan(A.terms(), shape, 0)
+    assert p.uses_fast_path
+    ud = to_device(u)
+    fast = deo.julia_array(shape)
+    slow = deo.julia_array(shape)
+    p.apply(ud, fast)
+    p.set_fast_path(False)
+    p.apply(ud, slow)
+    import torch
+    assert torch.equal(fast, slow)
+    ref = O.apply(oterms, u)
+    tol = 4 * np.spacing(O.abs_scale(oterms, u))
+    assert (np.abs(to_host(fast) - ref) <= tol).all()
+
+
+def _mixed_instances(seed=0, n=40):
+    rng = np.random.default_rng(seed)
+    inst = []
+    for k in range(n):
+        if rng.random() < 0.7:
+            N = int(np.exp(rng.uniform(np.log(64), np.log(4096))))
+            case = dict(shape=(N,), terms=[T("centered", int(rng.integers(1, 5)), int(rng.choice([2, 4, 6, 8])),
+                                             grid="uniform" if rng.random() < 0.5 else "nonuniform",
+                                             bc=("robin", (1.0, 0.5, 0.1), (1.0, 0.5, -0.1), 1)
+                                             if rng.random() < 0.5 else ("dirichlet0",))], seed=k)
+        else:
+            s = (int(np.exp(rng.uniform(np.log(32), np.log(200)))), int(np.exp(rng.uniform(np.log(32), np.log(200)))))
+            d, a = int(rng.integers(1, 5)), int(rng.choice([2, 4, 6, 8]))
+            g = "uniform" if rng.random() < 0.5 else "nonuniform"
+            case = dict(shape=s, terms=[T("centered", d, a, axis=1, grid=g, bc=("dirichlet0",)),
+                                        T("centered", d, a, axis=2, grid=g, bc=("dirichlet0",))], seed=k)
+        inst.append(case)
+    return inst
+
+
+@pytest.mark.parametrize("adjoint", [False, True])
+def test_batched_equals_individual(cuda, adjoint):
+    import torch
+    cases = _mixed_instances()
+    plans, us, outs, refs = [], [], [], []
+    for c in cases:
+        A, oterms, u = build(c)
+        shape = tuple(c["shape"])
+        p = _plan(A, shape)
+        ud = to_device(u)
+        r = deo.julia_array(shape)
+        (p.adjoint if adjoint else p.apply)(ud, r)
+        plans.append(p); us.append(ud); refs.append(r); outs.append(deo.julia_array(shape))
+    b = deo.Batch(list(zip(plans, us, outs)), adjoint=adjoint)
+    b.run(use_graph=False)
+    torch.cuda.synchronize()
+    for o, r in zip(outs, refs):
+        assert torch.equal(o, r)
+    for o in outs:
+        o.zero_()
+    b.run(use_graph=True)
+    b.run(use_graph=True)  # graph replay
+    torch.cuda.synchronize()
+    for o, r in zip(outs, refs):
+        assert torch.equal(o, r)
+    cfg = b.autotune()
+    assert cfg["tile"] > 0 and cfg["work_items"] > 0
+    for o in outs:
+        o.zero_()
+    b.run(use_graph=True)
+    torch.cuda.synchronize()
+    for o, r in zip(outs, refs):
+        assert torch.equal(o, r)
+
+
+def _advection_diffusion(shape, nu, c, a=2):
+    """nu * sum_k D2_k + UpwindDifference(1, a, h, n, -c) along axis 1, Dirichlet0 on every face."""
+    terms_p, terms_o = [], []
+    for k, n in enumerate(shape):
+        h = 1.0 / (n + 1)
+        P = nu * deo.CenteredDifference(2, 2, h, n, axis=k + 1)
+        Qo = O.centered(2, 2, h, n, axis=k + 1).scale(nu)
+        terms_p.append(P)
+        terms_o.append(Qo)
+    h = 1.0 / (shape[0] + 1)
+    terms_p.append(deo.UpwindDifference(1, a, h, shape[0], -c, axis=1))
+    terms_o.append(O.upwind(1, a, h, shape[0], -c, axis=1))
+    bc = deo.Dirichlet0BC()
+    if len(shape) == 1:
+        A = deo.DiffEqOperatorCombination([P * bc for P in terms_p])
+    else:
+        A = deo.DiffEqOperatorCombination([P * deo.MultiDimDirectionalBC(bc, P.axis, shape) for P in terms_p])
+    oterms = [(Q, O.dirichlet0()) for Q in terms_o]
+    return A, oterms
+
+
+@pytest.mark.parametrize("shape", [(200,), (40, 30), (12, 11, 10)])
+def test_ssprk3_matches_oracle(cuda, shape):
+    A, oterms = _advection_diffusion(shape, 0.05, 0.6)
+    rng = np.random.default_rng(8)
+    u0 = np.asfortranarray(rng.standard_normal(shape))
+    h = 1.0 / (shape[0] + 1)
+    dt = 0.4 * min(h / 0.6, h * h / (2 * 0.05 * len(shape)))
+    K = 25
+    got = to_host(deo.autodiff.ssprk3_solve(A, to_device(u0), dt, K))
+    ref = O.ssprk3(oterms, u0, dt, K)
+    assert np.allclose(got, ref, rtol=0, atol=1e-12 * K * np.abs(ref).max())
+
+
+def test_ssprk3_gradient_fd_and_checkpointing(cuda):
+    import torch
+    shape = (30, 20)
+    A, oterms = _advection_diffusion(shape, 0.02, -0.4)
+    rng = np.random.default_rng(9)
+    u0 = to_device(np.asfortranarray(rng.standard_normal(shape)))
+    h = 1.0 / 31
+    dt = 0.4 * min(h / 0.4, h * h / (2 * 0.02 * 2))
+    K = 17
+    uT, g = deo.autodiff.ssprk3_grad_norm2(A, u0, dt, K)
+    uT2, g2 = deo.autodiff.ssprk3_grad_norm2(A, u0, dt, K, checkpoint="sqrtK")
+    assert torch.equal(uT, uT2) and torch.equal(g, g2)
+    v = to_device(np.asfortranarray(rng.standard_normal(shape)))
+    eps = 1e-4
+    fp = float((deo.autodiff.ssprk3_solve(A, u0 + eps * v, dt, K) ** 2).sum())
+    fm = float((deo.autodiff.ssprk3_solve(A, u0 - eps * v, dt, K) ** 2).sum())
+    fd = (fp - fm) / (2 * eps)
+    ad = float((g * v).sum())
+    assert abs(fd - ad) <= 1e-7 * max(1.0, abs(ad)), (fd, ad)
