@@ -297,6 +297,214 @@ def run_ours(args, ws, rank):
     return line
 
 
+# ---------------------------------------------------------------------------
+# secondary workloads (each prints its own JSON line; the default stays lap3d)
+# ---------------------------------------------------------------------------
+def _event_time(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps / 1e3
+
+
+def run_line1d(args):
+    """1-D N=1024, CenteredDifference(2,2,1/1025,1024), Dirichlet0BC: launch-latency bound."""
+    import torch
+
+    import deo
+    N = 1024
+    h = 1.0 / (N + 1)
+    rng = np.random.default_rng(SEED)
+    u = np.sin(2 * np.pi * np.arange(1, N + 1) * h) + 0.01 * rng.standard_normal(N)
+    AQ = deo.CenteredDifference(2, 2, h, N) * deo.Dirichlet0BC(np.float64)
+    plan = deo.plan_for(AQ.terms(), (N,), 0)
+    ud = torch.from_numpy(u).cuda()
+    du = torch.empty_like(ud)
+    s = _event_time(lambda: plan.apply(ud, du), args.steps, args.warmup)
+    # CUDA-graph replay of 100 applies (how a solver loop would issue them)
+    g = torch.cuda.CUDAGraph()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st):
+        plan.apply(ud, du)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g, stream=st):
+            for _ in range(100):
+                plan.apply(ud, du)
+    torch.cuda.current_stream().wait_stream(st)
+    sg = _event_time(lambda: g.replay(), max(3, args.steps // 100), 2) / 100
+    return {"metric": "grid-pts/s (1-D N=1024 apply)", "workload": "line1d_1024_f64_d2a2_dirichlet0",
+            "value": N / s, "unit": "grid-pts/s", "us_per_apply": s * 1e6, "us_per_apply_graph": sg * 1e6,
+            "value_graph": N / sg, "dtype": "f64"}
+
+
+def nonuniform2d_ops(n, field_dev=None):
+    import deo
+    i = np.arange(n + 1)
+    dx = 1.0 + 0.5 * np.sin(2 * np.pi * i / n)
+    dx = dx / dx.sum()
+    rng = np.random.default_rng(SEED + 7)
+    al, ar = rng.uniform(-1, 1, 3), rng.uniform(-1, 1, 3)
+    al[1] = abs(al[1]) + 0.5
+    ar[1] = abs(ar[1]) + 0.5
+    s = (n, n)
+    q = {k: deo.MultiDimDirectionalBC(deo.GeneralBC(al, ar, dx, 1), k, s) for k in (1, 2)}
+    ops = [deo.CenteredDifference(1, 6, dx, n, axis=1) * q[1], deo.CenteredDifference(1, 6, dx, n, axis=2) * q[2],
+           deo.CenteredDifference(2, 6, dx, n, axis=1) * q[1], deo.CenteredDifference(2, 6, dx, n, axis=2) * q[2]]
+    if field_dev is not None:
+        ops.append(deo.with_field(deo.UpwindDifference(1, 3, dx, n, axis=1), field_dev) * q[1])
+    return ops, (al, ar, dx)
+
+
+def run_nonuniform2d(args):
+    """2048^2 non-uniform grid: centred d1/d2 a6 on both axes + upwind d1 a3
+    with the field a(x,y) = cos(2 pi x) sin(2 pi y), GeneralBC; per op and fused."""
+    import torch
+
+    import deo
+    n = 2048
+    x = np.cumsum(np.r_[0.0, np.ones(n)]) / n
+    a = np.asfortranarray(np.cos(2 * np.pi * x[1:, None]) * np.sin(2 * np.pi * x[None, 1:]))
+    fdev = deo.julia_array((n, n)); fdev.copy_(torch.from_numpy(a))
+    ops, _ = nonuniform2d_ops(n, fdev)
+    rng = np.random.default_rng(SEED + 3)
+    u = rng.standard_normal((n, n))
+    for _ in range(5):  # Jacobi smoothing
+        u[1:-1, 1:-1] = 0.25 * (u[:-2, 1:-1] + u[2:, 1:-1] + u[1:-1, :-2] + u[1:-1, 2:])
+    ud = deo.julia_array((n, n)); ud.copy_(torch.from_numpy(np.asfortranarray(u)))
+    outs = [deo.julia_array((n, n)) for _ in range(2)]
+    res = {"metric": "grid-pts/s (2-D 2048^2 non-uniform)", "workload": "nonuniform2d_2048_f64", "dtype": "f64",
+           "per_op": {}}
+    names = ["D1x", "D1y", "D2x", "D2y", "Upwind1x_field"]
+    hbm, _ = peaks()
+    for nm, g in zip(names, ops):
+        p = deo.plan_for([g], (n, n), 0)
+        t = _event_time(lambda: p.apply(ud, outs[0]), args.steps, args.warmup)
+        b = (24 if g.field is not None else 16) * n * n
+        res["per_op"][nm] = {"grid_pts_per_s": n * n / t, "ms": t * 1e3, "GBps": b / t / 1e9, "frac_hbm": b / t / 1e9 / hbm}
+    p = deo.plan_for(ops, (n, n), 0)
+    t = _event_time(lambda: p.apply(ud, outs[1]), args.steps, args.warmup)
+    res["value"] = n * n / t
+    res["unit"] = "grid-pts/s"
+    res["fused_ms"] = t * 1e3
+    res["fused_GBps"] = 24 * n * n / t / 1e9
+    res["fused_frac_hbm"] = res["fused_GBps"] / hbm
+    return res
+
+
+def batch_instances(count=4096, seed=SEED, scale=1.0):
+    """4096 instances: 70% 1-D (N log-uniform [64, 65536]), 30% 2-D (sides
+    log-uniform [32, 1024]); d in 1..4, a in {2,4,6,8}; uniform or graded grid
+    50/50; Dirichlet or Robin per instance."""
+    import deo
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        d, a = int(rng.integers(1, 5)), int(rng.choice([2, 4, 6, 8]))
+        graded = rng.random() < 0.5
+        robin = rng.random() < 0.5
+        if rng.random() < 0.7:
+            shape = (max(16, int(np.exp(rng.uniform(np.log(64), np.log(65536))) * scale)),)
+        else:
+            shape = tuple(max(16, int(np.exp(rng.uniform(np.log(32), np.log(1024))) * scale)) for _ in range(2))
+        terms = []
+        for ax, n in enumerate(shape):
+            if graded:
+                i = np.arange(n + 1)
+                dx = 1.0 + 0.5 * np.sin(2 * np.pi * i / (n + 1))
+                dx = dx / dx.sum()
+                bc = deo.RobinBC((1.0, 0.5, 0.1), (1.0, 0.5, -0.1), dx, 1) if robin else deo.DirichletBC(0.1, -0.2)
+            else:
+                dx = 1.0 / (n + 1)
+                bc = deo.RobinBC((1.0, 0.5, 0.1), (1.0, 0.5, -0.1), dx, 1) if robin else deo.DirichletBC(0.1, -0.2)
+            L = deo.CenteredDifference(d, a, dx, n, axis=ax + 1)
+            terms.append(L * (bc if len(shape) == 1 else deo.MultiDimDirectionalBC(bc, ax + 1, shape)))
+        out.append((shape, terms))
+    return out
+
+
+def run_batch(args):
+    import torch
+
+    import deo
+    inst = batch_instances()
+    plans, us, fw, bw, ones = [], [], [], [], []
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    total = 0
+    for shape, terms in inst:
+        p = deo.Plan(terms, shape, 0)
+        u = deo.julia_array(shape)
+        u.copy_(torch.randn(tuple(reversed(shape)), generator=g, device="cuda", dtype=torch.float64).permute(
+            *reversed(range(len(shape)))))
+        plans.append(p); us.append(u); fw.append(deo.julia_array(shape)); bw.append(deo.julia_array(shape))
+        ones.append(deo.julia_array(shape))
+        total += int(np.prod(shape))
+    bf = deo.Batch(list(zip(plans, us, fw)))
+    ba = deo.Batch(list(zip(plans, fw, bw)), adjoint=True)
+    cfg_f = bf.autotune(os.path.join(ROOT, "gpurun_out", "autotune.cache") if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else None)
+    cfg_a = ba.autotune()
+
+    def batched():
+        bf.run(True)
+        ba.run(True)
+
+    def one_by_one():
+        for p, u, o, b in zip(plans, us, ones, bw):
+            p.apply(u, o)
+        for p, o, b in zip(plans, ones, bw):
+            p.adjoint(o, b)
+
+    t_b = _event_time(batched, max(3, args.steps // 50), 2)
+    t_1 = _event_time(one_by_one, max(2, args.steps // 200), 1)
+    # results agree bit for bit
+    torch.cuda.synchronize()
+    same = all(torch.equal(a, b) for a, b in zip(fw, ones))
+    hbm, _ = peaks()
+    byts = 2 * 16 * total
+    return {"metric": "solves/s (4096 batched forward+adjoint applies)", "workload": "batched_4096_mixed_f64",
+            "value": len(inst) / t_b, "unit": "solves/s", "dtype": "f64", "total_points": total,
+            "ms_per_pass": t_b * 1e3, "one_launch_per_instance_solves_per_s": len(inst) / t_1,
+            "one_launch_per_instance_ms": t_1 * 1e3, "speedup_vs_one_launch_per_instance": t_1 / t_b,
+            "GBps": byts / t_b / 1e9, "frac_hbm": byts / t_b / 1e9 / hbm, "forward_bitwise_equal": same,
+            "autotune_forward": cfg_f, "autotune_adjoint": cfg_a, "gpu_launches_per_pass": 2}
+
+
+def run_serve(args):
+    import torch
+
+    import deo
+    from deo.serve import Server, poisson_requests
+    reqs = poisson_requests(args.requests, 2000.0, seed=SEED, size_scale=args.size_scale,
+                            k_range=(10, args.kmax))
+    srv = Server(hbm_budget_bytes=120e9)
+    st = srv.run(reqs)
+    work = sum(r.npts * r.K * (2 if r.want_grad else 1) for r in reqs)
+    # baseline: the same requests one at a time, one launch per stage per request
+    base = None
+    if args.serve_baseline:
+        reqs2 = poisson_requests(args.requests, 2000.0, seed=SEED, size_scale=args.size_scale,
+                                 k_range=(10, args.kmax))
+        srv2 = Server(hbm_budget_bytes=120e9, max_active=1)
+        base = srv2.run(reqs2)
+    out = {"metric": "served solves/s (Poisson 2000 req/s, SSP-RK3 MOL)", "workload": "serve_mol_f64",
+           "value": st["solves_per_s"], "unit": "solves/s", "dtype": "f64", "p50_s": st["p50_s"],
+           "p99_s": st["p99_s"], "requests": st["requests"], "completed": st["completed"],
+           "makespan_s": st["makespan_s"], "point_steps": work, "ticks": st["ticks"], "rebuilds": st["rebuilds"],
+           "size_scale": args.size_scale, "kmax": args.kmax}
+    if base is not None:
+        out["one_at_a_time"] = {k: base[k] for k in ("solves_per_s", "p50_s", "p99_s", "makespan_s")}
+        out["speedup_vs_one_at_a_time"] = st["solves_per_s"] / base["solves_per_s"]
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
@@ -340,10 +548,22 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "lap3d_f32"])
+    ap.add_argument("--workload", default="lap3d",
+                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--requests", type=int, default=64)
+    ap.add_argument("--size-scale", type=float, default=1.0)
+    ap.add_argument("--kmax", type=int, default=1000)
+    ap.add_argument("--serve-baseline", action="store_true")
     args = ap.parse_args()
+    if args.workload in ("line1d", "nonuniform2d", "batch", "serve"):
+        import torch
+        torch.cuda.set_device(0)
+        fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "batch": run_batch,
+              "serve": run_serve}[args.workload]
+        print(json.dumps(fn(args)), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -858,6 +858,10 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             U.enabled = 1;
             U.radius = H;
             U.nterms = nterms;
+            // centred-band specialisation: term t on axis t, 2H+1 taps from -H
+            U.lap = (nterms == ndims);
+            for (int t = 0; t < nterms && U.lap; ++t)
+                U.lap = U.t[t].axis == t && U.t[t].nk == 2 * H + 1 && U.t[t].off0 == -H;
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
             U.enabled = 0;

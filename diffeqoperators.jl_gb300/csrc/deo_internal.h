@@ -83,7 +83,7 @@ struct UniPlan {
     int enabled;
     int radius;      // H = max |offset| over terms
     int nterms;
-    int pad_;
+    int lap;         // 1: term t acts on axis t with a centred band of 2H+1 taps (k_lap)
     int64_t n[3];    // sizes along axes 1..3 (1 for absent axes)
     UniTerm t[DEO_KMAX_TERMS];
 };
