@@ -1,0 +1,172 @@
+"""
+    DeoGB300
+
+Julia-side shim that routes DiffEqOperators.jl's stencil applies on `CuArray`s
+to libdeo (include/deo.h) through `ccall`.  It adds methods for `mul!` and `*`
+on the reference's own types when the array is a `CuArray{Float64}` or
+`CuArray{Float32}`; CPU arrays keep the reference's methods.
+
+The operator's tables are passed as they are stored in the reference's
+`DerivativeOperator` (deo_operator_from_tables), so the device applies use
+exactly the reference's coefficients.
+
+Not exercised in this repository's test-suite: no Julia toolchain is available
+where it was built.  The same C ABI is exercised from Python (deo/_lib.py).
+"""
+module DeoGB300
+
+using LinearAlgebra
+using CUDA
+using DiffEqOperators
+using DiffEqOperators: DerivativeOperator, GhostDerivativeOperator, DiffEqOperatorCombination,
+                       AffineBC, PeriodicBC, MultiDimDirectionalBC, ComposedMultiDimBC
+
+const libdeo = get(ENV, "DEO_LIB", joinpath(@__DIR__, "..", "libdeo.so"))
+const DEO_MAX_BC = 16
+
+# ---- C structs (layouts match include/deo.h) --------------------------------
+struct DeoOperatorDesc
+    derivative_order::Cint
+    approximation_order::Cint
+    len::Cint
+    stencil_length::Cint
+    boundary_stencil_length::Cint
+    boundary_point_count::Cint
+    offside::Cint
+    winding::Cint
+    uniform::Cint
+    coeff_func_sign::Cint
+    n_stencil_rows::Cint
+    n_low_rows::Cint
+    n_high_rows::Cint
+    stencil_coefs::Ptr{Cdouble}
+    low_boundary_coefs::Ptr{Cdouble}
+    high_boundary_coefs::Ptr{Cdouble}
+    coefficients::Ptr{Cdouble}
+end
+
+struct DeoBC
+    kind::Cint
+    m_l::Cint
+    m_r::Cint
+    a_l::NTuple{DEO_MAX_BC,Cdouble}
+    a_r::NTuple{DEO_MAX_BC,Cdouble}
+    b_l::Cdouble
+    b_r::Cdouble
+end
+
+struct DeoTerm
+    op::Ptr{Cvoid}
+    axis::Cint
+    bc::Ptr{DeoBC}
+    coeff_field::Ptr{Cvoid}
+    path::Cint
+end
+
+# ---- errors: deo_status -> the reference's exception types ------------------
+function check(status::Cint)
+    status == 0 && return nothing
+    msg = unsafe_string(ccall((:deo_last_error, libdeo), Cstring, ()))
+    status == 1 && throw(DimensionMismatch(msg))          # DEO_ERR_BAD_SHAPE
+    status == 2 && throw(ArgumentError(msg))              # DEO_ERR_BAD_ARG
+    error("libdeo status $status: $msg")
+end
+
+# ---- operators: flatten a DerivativeOperator's fields ------------------------
+_flat(v::AbstractVector{<:AbstractVector}) = Float64.(reduce(vcat, collect.(v); init = Float64[]))
+_flat(v::AbstractVector{<:Real}) = Float64.(collect(v))
+function _flat(m::AbstractMatrix)   # non-uniform UpwindDifference: 2 x n SMatrix of SVectors
+    Float64.(vcat(_flat(vec(m[1, :])), _flat(vec(m[2, :]))))
+end
+
+function deo_operator(L::DerivativeOperator{T}) where {T}
+    wind = DiffEqOperators.use_winding(L)
+    uniform = L.dx isa Number
+    st, lo, hi = _flat(L.stencil_coefs), _flat(L.low_boundary_coefs), _flat(L.high_boundary_coefs)
+    halves = (wind && !uniform) ? 2 : 1
+    coeff = L.coefficients === nothing ? ones(Float64, L.len) :
+            L.coefficients isa Number ? fill(Float64(L.coefficients), L.len) : Float64.(L.coefficients)
+    cfs = L.coeff_func isa Number ? (L.coeff_func >= 0 ? 1 : -1) : 0
+    d = DeoOperatorDesc(L.derivative_order, L.approximation_order, L.len, L.stencil_length,
+                        L.boundary_stencil_length, L.boundary_point_count, L.offside, wind, uniform, cfs,
+                        div(length(st), halves * L.stencil_length),
+                        div(length(lo), max(1, halves * L.boundary_stencil_length)),
+                        div(length(hi), max(1, halves * L.boundary_stencil_length)),
+                        pointer(st), pointer(lo), pointer(hi), pointer(coeff))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve st lo hi coeff check(ccall((:deo_operator_from_tables, libdeo), Cint,
+                                            (Ref{DeoOperatorDesc}, Ref{Ptr{Cvoid}}), d, h))
+    return h[]
+end
+
+_pad(v) = ntuple(i -> i <= length(v) ? Float64(v[i]) : 0.0, DEO_MAX_BC)
+deo_bc(Q::AffineBC) = DeoBC(0, length(Q.a_l), length(Q.a_r), _pad(Q.a_l), _pad(Q.a_r), Q.b_l, Q.b_r)
+deo_bc(::PeriodicBC) = DeoBC(1, 0, 0, _pad(()), _pad(()), 0.0, 0.0)
+_axis(::DerivativeOperator{T, N}) where {T, N} = N
+
+# BC acting on axis `ax` of an N-D array
+_bc_for(Q::Union{AffineBC, PeriodicBC}, ax) = Q
+_bc_for(Q::MultiDimDirectionalBC, ax) = first(Q.BCs)      # one BC per axis (filled)
+_bc_for(Q::ComposedMultiDimBC, ax) = first(Q.BCs[ax])
+
+_ghosts(A::GhostDerivativeOperator) = (A,)
+_ghosts(A::DiffEqOperatorCombination) = Tuple(op for op in A.ops)
+
+# ---- plans (cached per operator object, size and element type) --------------
+const PLANS = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
+
+function plan_for(A, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
+    cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), PLANS, A)
+    get!(cache, (sz, T)) do
+        gs = _ghosts(A)
+        ops = [deo_operator(g.L) for g in gs]
+        bcs = [deo_bc(_bc_for(g.Q, _axis(g.L))) for g in gs]
+        terms = [DeoTerm(ops[i], _axis(gs[i].L), pointer(bcs, i), C_NULL, 0) for i in eachindex(gs)]
+        sizes = Int64[sz...]
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        GC.@preserve bcs sizes terms check(ccall((:deo_plan_create, libdeo), Cint,
+                                                 (Cint, Ptr{Int64}, Cint, Cint, Ptr{DeoTerm}, Ref{Ptr{Cvoid}}),
+                                                 length(sz), sizes, T === Float64 ? 0 : 1, length(terms), terms, h))
+        foreach(op -> ccall((:deo_operator_destroy, libdeo), Cvoid, (Ptr{Cvoid},), op), ops)
+        h[]
+    end
+end
+
+_stream() = CUDA.stream().handle
+
+# mul!(du, A*Q, u) and (A*Q)*u on the GPU (ghost_derivative_operator.jl:15-37,
+# composite_operators.jl:64-83)
+const DeoOp = Union{GhostDerivativeOperator, DiffEqOperatorCombination}
+
+function LinearAlgebra.mul!(du::CuArray{T}, A::DeoOp, u::CuArray{T}; overwrite = true) where {T <: Union{Float32, Float64}}
+    size(du) == size(u) || throw(DimensionMismatch("du and u differ in size"))
+    p = plan_for(A, size(u), T)
+    check(ccall((:deo_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Cint, Ptr{Cvoid}),
+                p, u, du, overwrite, _stream()))
+    return du
+end
+
+function Base.:*(A::DeoOp, u::CuArray{T}) where {T <: Union{Float32, Float64}}
+    du = similar(u)
+    return mul!(du, A, u)
+end
+
+# (L)(du, u, p, t) right-hand-side interface (DiffEqOperators.jl:67-76)
+(A::GhostDerivativeOperator)(du::CuArray, u::CuArray, p, t) = mul!(du, A, u)
+
+# ---- ChainRulesCore.rrule: pullback = adjoint kernel ------------------------
+using ChainRulesCore
+function ChainRulesCore.rrule(::typeof(*), A::DeoOp, u::CuArray{T}) where {T <: Union{Float32, Float64}}
+    y = A * u
+    p = plan_for(A, size(u), T)
+    function pullback(ȳ)
+        ū = similar(u)
+        ȳc = CuArray{T}(unthunk(ȳ))
+        check(ccall((:deo_apply_adjoint, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Cint, Ptr{Cvoid}),
+                    p, ȳc, ū, 1, _stream()))
+        return NoTangent(), NoTangent(), ū
+    end
+    return y, pullback
+end
+
+end # module
