@@ -18,6 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = {
     "deo_kernels.o": ("nvcc", "deo_kernels.cu"),
+    "deo_tma.o": ("nvcc", "deo_tma.cu"),
     "deo_host.o": ("cxx", "deo_host.cpp"),
 }
 
@@ -36,7 +37,8 @@ def _cmd(kind: str, src: str, obj: str, verbose_ptxas: bool) -> list[str]:
 def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
-    deps = [src, os.path.join(CSRC, "deo_internal.h"), os.path.join(HERE, "..", "include", "deo.h"),
+    deps = [src, os.path.join(CSRC, "deo_internal.h"), os.path.join(CSRC, "deo_eval.cuh"),
+            os.path.join(HERE, "..", "include", "deo.h"),
             os.path.abspath(__file__)]
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))

@@ -1,0 +1,176 @@
+// deo_eval.cuh -- device-side evaluators shared by the kernels: one output
+// row of one term from its row table (forward), one column of the transposed
+// operator (adjoint), the multi-term point sum, and small helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "deo_internal.h"
+
+namespace deo {
+
+template <typename T>
+__device__ __forceinline__ T band_w(const RowTabDev& tb, int k);
+template <>
+__device__ __forceinline__ double band_w<double>(const RowTabDev& tb, int k) {
+    return tb.wband[k];
+}
+template <>
+__device__ __forceinline__ float band_w<float>(const RowTabDev& tb, int k) {
+    return reinterpret_cast<const float*>(tb.wband)[k];
+}
+
+template <typename T>
+__device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ line) {
+    const int64_t s = t.stride;
+    if (t.bc_kind == 1) return t.periodic_nd ? line[0] : line[(int64_t)(t.len - 1) * s];
+    T d = T(0);
+    for (int j = 0; j < t.ml; ++j) d = (j == 0) ? T(t.al[0]) * line[0] : fma(T(t.al[j]), line[(int64_t)j * s], d);
+    return d + T(t.bl);
+}
+
+template <typename T>
+__device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__ line) {
+    const int64_t s = t.stride;
+    if (t.bc_kind == 1) return t.periodic_nd ? line[(int64_t)(t.len - 1) * s] : line[0];
+    T d = T(0);
+    const int64_t o = (int64_t)(t.len - t.mr);
+    for (int j = 0; j < t.mr; ++j)
+        d = (j == 0) ? T(t.ar[0]) * line[o * s] : fma(T(t.ar[j]), line[(o + j) * s], d);
+    return d + T(t.br);
+}
+
+// The reference adds `!overwrite * x_temp[i]` (a strong zero) to every tap
+// sum, which turns -0.0 into +0.0 and is otherwise exact.  Applied once to the
+// final sum it has the same effect; done on the bits to spend no FP64 issue.
+__device__ __forceinline__ double zero_fix(double x) {
+    return __double_as_longlong(x) == (long long)0x8000000000000000ULL ? 0.0 : x;
+}
+__device__ __forceinline__ float zero_fix(float x) {
+    return __float_as_uint(x) == 0x80000000u ? 0.0f : x;
+}
+
+struct RowInfo {
+    int p0, nk, e;
+    bool band;
+};
+
+__device__ __forceinline__ RowInfo row_info(const RowTabDev& tb, int i) {
+    RowInfo r;
+    r.band = (i >= tb.ilo) && (i <= tb.ihi);
+    if (r.band) {
+        r.p0 = i + tb.band_p0_off;
+        r.nk = tb.band_nk;
+        r.e = 0;
+    } else {
+        r.e = (i < tb.ilo) ? i - 1 : (tb.ilo - 1) + (i - tb.ihi - 1);
+        r.p0 = __ldg(tb.p0 + r.e);
+        r.nk = __ldg(tb.nk + r.e);
+    }
+    return r;
+}
+
+__device__ __forceinline__ int row_cidx(const RowTabDev& tb, int i) {
+    if (i >= tb.ilo && i <= tb.ihi) return i + tb.band_cidx_off;
+    const int e = (i < tb.ilo) ? i - 1 : (tb.ilo - 1) + (i - tb.ihi - 1);
+    return __ldg(tb.cidx + e);
+}
+
+template <typename T>
+__device__ __forceinline__ T row_w(const RowTabDev& tb, const RowInfo& r, int k) {
+    return r.band ? band_w<T>(tb, k) : __ldg(reinterpret_cast<const T*>(tb.W) + (int64_t)k * tb.nexp + r.e);
+}
+
+// Coefficient and table variant of row i on the line starting at `base`.
+template <typename T>
+__device__ __forceinline__ const RowTabDev& row_variant(const TermDev& t, int64_t base, int i, T& c) {
+    c = T(1);
+    if (!t.has_field) return t.tab[0];
+    const int ci = row_cidx(t.tab[0], i);
+    c = __ldg(reinterpret_cast<const T*>(t.field) + base + (int64_t)(ci - 1) * t.stride);
+    if (t.nvar == 2 && !(c >= T(0))) return t.tab[1];
+    return t.tab[0];
+}
+
+// One term, one output row: the reference's per-point tap loop.
+template <typename T>
+__device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u, int64_t idx, int i) {
+    const int64_t s = t.stride;
+    const int64_t base = idx - (int64_t)(i - 1) * s;
+    const T* __restrict__ line = u + base;
+    T c;
+    const RowTabDev& tb = row_variant<T>(t, base, i, c);
+    const RowInfo r = row_info(tb, i);
+    const int L2 = t.len + 2;
+    T gl = T(0), gr = T(0);
+    if (r.p0 == 1) gl = ghost_left<T>(t, line);
+    if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line);
+    T acc = T(0);
+    for (int k = 0; k < r.nk; ++k) {
+        const int p = r.p0 + k;
+        const T x = (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
+        T w = row_w<T>(tb, r, k);
+        if (t.has_field) w = c * w;
+        acc = fma(w, x, acc);
+    }
+    return acc;
+}
+
+// Column p of one term's L (padded space) dotted with dbar along the line.
+template <typename T>
+__device__ __forceinline__ T adj_column(const TermDev& t, const T* __restrict__ d, int64_t base, int p) {
+    const int64_t s = t.stride;
+    const int lo = __ldg(t.rlo + (p - 1)), hi = __ldg(t.rhi + (p - 1));
+    T acc = T(0);
+    for (int i = lo; i <= hi; ++i) {
+        T c;
+        const RowTabDev& tb = row_variant<T>(t, base, i, c);
+        const RowInfo r = row_info(tb, i);
+        const int k = p - r.p0;
+        if (k < 0 || k >= r.nk) continue;
+        T w = row_w<T>(tb, r, k);
+        if (t.has_field) w = c * w;
+        acc = fma(w, __ldg(d + base + (int64_t)(i - 1) * s), acc);
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ T adj_term(const TermDev& t, const T* __restrict__ d, int64_t idx, int j) {
+    const int64_t base = idx - (int64_t)(j - 1) * t.stride;
+    const int L = t.len;
+    T w = adj_column<T>(t, d, base, j + 1);
+    if (t.bc_kind == 0) {
+        if (j <= t.ml) w = fma(T(t.al[j - 1]), adj_column<T>(t, d, base, 1), w);
+        if (j > L - t.mr) w = fma(T(t.ar[j - 1 - (L - t.mr)]), adj_column<T>(t, d, base, L + 2), w);
+    } else {
+        const int jl = t.periodic_nd ? 1 : L;  // column receiving the left ghost
+        const int jr = t.periodic_nd ? L : 1;
+        if (j == jl) w += adj_column<T>(t, d, base, 1);
+        if (j == jr) w += adj_column<T>(t, d, base, L + 2);
+    }
+    return w;
+}
+
+template <typename T, bool ADJ>
+__device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ u, int64_t idx) {
+    T acc = T(0);
+    for (int tt = 0; tt < P.nterms; ++tt) {
+        const TermDev& t = P.t[tt];
+        const int i = (int)((idx / t.stride) % t.len) + 1;
+        const T r = ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
+        acc = (tt == 0) ? r : acc + r;
+    }
+    return ADJ ? acc : zero_fix(acc);
+}
+
+template <typename T>
+__device__ __forceinline__ T uni_w(const UniTerm& t, int k);
+template <>
+__device__ __forceinline__ double uni_w<double>(const UniTerm& t, int k) { return t.w[k]; }
+template <>
+__device__ __forceinline__ float uni_w<float>(const UniTerm& t, int k) {
+    return reinterpret_cast<const float*>(t.w)[k];
+}
+
+}  // namespace deo

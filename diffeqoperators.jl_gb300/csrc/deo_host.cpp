@@ -713,7 +713,9 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
 struct deo_plan {
     PlanDev dev{};
     deo::UniPlan uni{};
-    int fast_path = 1;
+    int fast_path = 1;   // DEO_OPT_FAST_PATH
+    int use_tma = 1;     // DEO_OPT_TMA
+    int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     std::vector<void*> allocs;
     size_t table_bytes = 0;
@@ -862,6 +864,22 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             U.lap = (nterms == ndims);
             for (int t = 0; t < nterms && U.lap; ++t)
                 U.lap = U.t[t].axis == t && U.t[t].nk == 2 * H + 1 && U.t[t].off0 == -H;
+            // exact neighbour sums: Float64, one symmetric band shared by every term
+            U.ens = U.lap && dtype == DEO_F64;
+            for (int t = 0; t < nterms && U.ens; ++t)
+                U.ens = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
+            for (int k = 1; k <= H && U.ens; ++k)
+                U.ens = std::memcmp(&U.t[0].w[H - k], &U.t[0].w[H + k], sizeof(double)) == 0;
+            if (U.ens) {
+                const double w0 = U.t[0].w[H];
+                for (int mask = 0; mask < 8; ++mask) {
+                    double c = 0.0;
+                    for (int t = 0; t < 3; ++t)
+                        if (mask & (1 << t)) c = c + w0;  // 2*w0 is exact, so 3*w0 rounds once
+                    U.ens_c0[mask] = c;
+                }
+                for (int k = 1; k <= H; ++k) U.ens_w[k] = U.t[0].w[H + k];
+            }
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
             U.enabled = 0;
@@ -884,18 +902,42 @@ static deo_status check_ptrs(const deo_plan* p, const void* a, const void* b) {
 }
 
 static int launch_forward(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
-    if (p->uni.enabled && p->fast_path)
+    if (p->uni.enabled && p->fast_path) {
+        if (p->uni.lap && p->use_tma) {
+            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream);
+            if (e != (int)cudaErrorNotSupported) return e;
+        }
         return deo_k_apply_uniform(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+    }
     return deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
 }
 
-extern "C" deo_status deo_plan_set_fast_path(deo_plan* p, int enable) {
+extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
     if (!p) return fail(DEO_ERR_BAD_ARG, "null plan");
-    p->fast_path = enable ? 1 : 0;
-    return DEO_OK;
+    switch (option) {
+        case DEO_OPT_FAST_PATH: p->fast_path = value ? 1 : 0; return DEO_OK;
+        case DEO_OPT_TMA: p->use_tma = value ? 1 : 0; return DEO_OK;
+        case DEO_OPT_EXACT_SUMS: p->exact_sums = value ? 1 : 0; return DEO_OK;
+    }
+    return fail(DEO_ERR_BAD_ARG, "unknown plan option %d", option);
 }
 
-extern "C" int deo_plan_uses_fast_path(const deo_plan* p) { return p && p->uni.enabled && p->fast_path; }
+extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
+    if (!p) return -1;
+    switch (option) {
+        case DEO_OPT_FAST_PATH: return p->fast_path && p->uni.enabled;
+        case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
+        case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && p->uni.ens;
+    }
+    return -1;
+}
+
+extern "C" deo_status deo_device_status(unsigned int* status) {
+    if (!status) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const int e = deo_k_read_status(status);
+    if (e) return cuda_fail((cudaError_t)e, "deo_device_status");
+    return *status ? fail(DEO_ERR_TIMEOUT, "a bounded device wait gave up (status 0x%x)", *status) : DEO_OK;
+}
 
 extern "C" deo_status deo_apply(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
     deo_status s = check_ptrs(p, u, du);

@@ -86,6 +86,13 @@ struct UniPlan {
     int lap;         // 1: term t acts on axis t with a centred band of 2H+1 taps (k_lap)
     int64_t n[3];    // sizes along axes 1..3 (1 for absent axes)
     UniTerm t[DEO_KMAX_TERMS];
+    // Exact-neighbour-sum evaluation (Float64, all terms share one symmetric
+    // band): r = c0[mask]*u0 + sum_k w[k] * S_k, where S_k = the exact sum of
+    // the 2*|mask| neighbours at distance k, rounded once.
+    int ens;
+    int pad2_;
+    double ens_c0[8];             // merged centre weight for each mask of axes
+    double ens_w[DEO_MAX_NW];     // weight at distance k = 1..H (index k)
 };
 
 // Work item of the batched persistent kernel: `count` points starting at
@@ -128,5 +135,10 @@ extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
+// TMA-fed fast path (deo_tma.cu); returns cudaErrorNotSupported when the
+// array does not meet the tensor-map alignment rules (caller falls back).
+extern "C" int deo_k_apply_tma(const deo::UniPlan* up, const deo::PlanDev* d_plan, int dtype, const void* u,
+                               void* du, int overwrite, int use_ens, void* stream);
+extern "C" int deo_k_read_status(unsigned int* status);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
                                  unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);

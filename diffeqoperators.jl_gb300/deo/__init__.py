@@ -5,7 +5,16 @@ UpwindDifference, RobinBC, GeneralBC, DirichletBC, Dirichlet0BC, NeumannBC,
 Neumann0BC, PeriodicBC, MultiDimBC, compose, `L*Q*u`, mul!) and run on the
 CUDA kernels of libdeo.so.  There is no CPU fallback.
 """
-from ._lib import DeoError, DeoArgError, DeoShapeError, LIB_PATH, lib  # noqa: F401
+from ._lib import (DEO_OPT_EXACT_SUMS, DEO_OPT_FAST_PATH, DEO_OPT_TMA, DeoArgError, DeoError,  # noqa: F401
+                   DeoShapeError, LIB_PATH, lib)
+
+
+def device_status() -> int:
+    """Device-side error flags since the last call (bit 0: a bounded wait gave up)."""
+    import ctypes
+    v = ctypes.c_uint(0)
+    lib().deo_device_status(ctypes.byref(v))
+    return v.value
 from .operators import (  # noqa: F401
     AtomicBC, CenteredDifference, ComposedMultiDimBC, DerivativeOperator, DiffEqOperatorCombination,
     DimensionMismatch, Dirichlet0BC, DirichletBC, FieldCoefficient, GeneralBC, GhostDerivativeOperator,

@@ -18,6 +18,7 @@ STATUS_NAMES = {0: "OK", 1: "BAD_SHAPE", 2: "BAD_ARG", 3: "UNSUPPORTED", 4: "CUD
 DEO_F64, DEO_F32 = 0, 1
 DEO_BC_AFFINE, DEO_BC_PERIODIC = 0, 1
 DEO_PATH_AUTO, DEO_PATH_PADDED, DEO_PATH_GENERIC = 0, 1, 2
+DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS = 1, 2, 3
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)
@@ -108,8 +109,9 @@ def lib():
     proto("deo_plan_create", st, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(Term), C.POINTER(_vp))
     proto("deo_plan_destroy", None, _vp)
     proto("deo_plan_table_bytes", C.c_size_t, _vp)
-    proto("deo_plan_set_fast_path", st, _vp, C.c_int)
-    proto("deo_plan_uses_fast_path", C.c_int, _vp)
+    proto("deo_plan_set_option", st, _vp, C.c_int, C.c_int)
+    proto("deo_plan_get_option", C.c_int, _vp, C.c_int)
+    proto("deo_device_status", st, C.POINTER(C.c_uint))
     proto("deo_apply", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_apply_host", st, _vp, _vp, _vp, _vp)
     proto("deo_apply_adjoint", st, _vp, _vp, _vp, C.c_int, _vp)
@@ -143,7 +145,7 @@ EXPORTED = [
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
     "deo_operator_destroy", "deo_operator_array", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
-    "deo_plan_table_bytes", "deo_plan_set_fast_path", "deo_plan_uses_fast_path", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
+    "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune",
 ]

@@ -612,13 +612,23 @@ class Plan:
     def table_bytes(self) -> int:
         return int(L.lib().deo_plan_table_bytes(self._h))
 
-    def set_fast_path(self, enable: bool):
-        check(L.lib().deo_plan_set_fast_path(self._h, int(bool(enable))))
+    def set_option(self, option: int, value: bool):
+        check(L.lib().deo_plan_set_option(self._h, int(option), int(bool(value))))
         return self
+
+    def get_option(self, option: int) -> bool:
+        return L.lib().deo_plan_get_option(self._h, int(option)) == 1
+
+    def set_fast_path(self, enable: bool):
+        return self.set_option(L.DEO_OPT_FAST_PATH, enable)
 
     @property
     def uses_fast_path(self) -> bool:
-        return bool(L.lib().deo_plan_uses_fast_path(self._h))
+        return self.get_option(L.DEO_OPT_FAST_PATH)
+
+    @property
+    def uses_exact_sums(self) -> bool:
+        return self.get_option(L.DEO_OPT_EXACT_SUMS)
 
     def _check(self, u, du):
         if tuple(u.shape) != self.shape or tuple(du.shape) != self.shape:

@@ -167,11 +167,28 @@ deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int
 void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
-/* 2-D/3-D plans whose terms all have constant interior rows run a shared-
- * memory tiled kernel for interior points; enable = 0 forces the generic
- * row-table kernel (same arithmetic, same bits; for checking). */
-deo_status deo_plan_set_fast_path(deo_plan* plan, int enable);
-int deo_plan_uses_fast_path(const deo_plan* plan);
+/* Plan options (defaults 1):
+ *   DEO_OPT_FAST_PATH: 2-D/3-D plans whose terms all have constant interior
+ *     rows use tiled kernels for interior points; 0 forces the generic
+ *     row-table kernel.
+ *   DEO_OPT_TMA: Laplacian-type plans (term t a centred band on axis t) stream
+ *     planes with TMA into a shared-memory ring; 0 uses the register-queue kernel.
+ *   DEO_OPT_EXACT_SUMS: Float64 plans whose terms share one symmetric band sum
+ *     the equal-weight neighbours exactly in integer arithmetic and round once
+ *     (H+1 FP64 instructions per point instead of NT*(2H+1)+NT-1; result within
+ *     a few ulp of sum|c_k u_k| of the reference's order).  0 keeps the
+ *     reference's per-term tap order, bit-identical to the generic kernel.
+ * No reference counterpart (execution choices only). */
+#define DEO_OPT_FAST_PATH 1
+#define DEO_OPT_TMA 2
+#define DEO_OPT_EXACT_SUMS 3
+deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
+/* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
+int deo_plan_get_option(const deo_plan* plan, int option);
+/* Device-side error flags raised since the last call (bit 0: a bounded wait
+ * in a kernel gave up; the kernel returned without finishing).  Synchronises.
+ * Returns DEO_ERR_TIMEOUT if any flag was set. */
+deo_status deo_device_status(unsigned int* status);
 
 /* mul!(du, A*Q, u): du = sum_t L_t Q_t u  (overwrite = 1), or du += ... (overwrite = 0,
  * the reference's `mul!(x, L, M; overwrite=false)`, convolutions.jl:17-22).

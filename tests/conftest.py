@@ -4,7 +4,7 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-for sub in ("diffeqoperators.jl_gb300", "oracle", os.path.join("tests", "golden"), "tests"):
+for sub in ("", "diffeqoperators.jl_gb300", "oracle", os.path.join("tests", "golden"), "tests"):
     p = os.path.join(ROOT, sub)
     if p not in sys.path:
         sys.path.insert(0, p)

@@ -107,21 +107,28 @@ def test_dot_product_identity_full_size(cuda):
                                                                 bc=("dirichlet0",))], seed=31)],
                          ids=["lap3d", "d0", "periodic", "odd", "2d-mixed"])
 def test_fast_path_bitwise_equals_generic(cuda, case):
+    import torch
     A, oterms, u = build(case)
     shape = tuple(case["shape"])
     p = deo.Plan(A.terms(), shape, 0)
     assert p.uses_fast_path
     ud = to_device(u)
-    fast = deo.julia_array(shape)
-    slow = deo.julia_array(shape)
-    p.apply(ud, fast)
-    p.set_fast_path(False)
-    p.apply(ud, slow)
-    import torch
-    assert torch.equal(fast, slow)
     ref = O.apply(oterms, u)
     tol = 4 * np.spacing(O.abs_scale(oterms, u))
-    assert (np.abs(to_host(fast) - ref) <= tol).all()
+    outs = {}
+    # (fast path, TMA ring, exact neighbour sums)
+    for name, opts in {"tma-ens": (1, 1, 1), "tma-fma": (1, 1, 0), "queue": (1, 0, 0), "generic": (0, 0, 0)}.items():
+        p.set_option(deo.DEO_OPT_FAST_PATH, opts[0])
+        p.set_option(deo.DEO_OPT_TMA, opts[1])
+        p.set_option(deo.DEO_OPT_EXACT_SUMS, opts[2])
+        o = deo.julia_array(shape)
+        p.apply(ud, o)
+        outs[name] = o
+        assert (np.abs(to_host(o) - ref) <= tol).all(), name
+    # the reference-order paths agree bit for bit
+    assert torch.equal(outs["tma-fma"], outs["generic"])
+    assert torch.equal(outs["queue"], outs["generic"])
+    assert deo.device_status() == 0
 
 
 def _mixed_instances(seed=0, n=40):
@@ -232,3 +239,44 @@ def test_ssprk3_gradient_fd_and_checkpointing(cuda):
     fd = (fp - fm) / (2 * eps)
     ad = float((g * v).sum())
     assert abs(fd - ad) <= 1e-7 * max(1.0, abs(ad)), (fd, ad)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_full_size_laplacian_against_oracle(cuda, dtype):
+    """The 256^3 Robin Laplacian (the benchmark configuration) against the
+    oracle at full size: Float64 within 4 ulp of sum|c_k u_k| in every mode;
+    Float32 error against the Float64 oracle reported and bounded."""
+    import json
+    import os
+    import torch
+    import bench
+    n = 256
+    h = 1.0 / (n + 1)
+    u = bench.fourier_field(n)
+    q = O.robin((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), h, 1)
+    terms = [(O.centered(2, 4, h, n, axis=k), q) for k in (1, 2, 3)]
+    ref = O.apply(terms, u, nthreads=os.cpu_count() or 1)
+    scale = O.abs_scale(terms, u)
+    _, plan, tdt = bench.lap3d_setup(n, dtype)
+    ud = deo.julia_array((n, n, n), tdt)
+    ud.copy_(torch.from_numpy(u).to(tdt))
+    report = {}
+    modes = {"exact-sums": 1, "reference-order": 0} if dtype == "f64" else {"default": 1}
+    for name, ens in modes.items():
+        plan.set_option(deo.DEO_OPT_EXACT_SUMS, ens)
+        du = deo.julia_array((n, n, n), tdt)
+        plan.apply(ud, du)
+        got = du.to(torch.float64).cpu().numpy()
+        ulps = np.abs(got - ref) / np.spacing(scale)
+        report[name] = {"max_ulp_of_scale": float(ulps.max()), "mean_ulp_of_scale": float(ulps.mean()),
+                        "max_rel_to_scale": float((np.abs(got - ref) / scale).max())}
+        if dtype == "f64":
+            assert ulps.max() <= 4.0, (name, report[name])
+        else:
+            assert report[name]["max_rel_to_scale"] < 64 * 2.0 ** -24
+    plan.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
+    assert deo.device_status() == 0
+    out = os.path.join(os.path.dirname(os.path.dirname(__file__)), "gpurun_out")
+    if os.path.isdir(out):
+        with open(os.path.join(out, f"parity_256_{dtype}.json"), "w") as f:
+            json.dump(report, f)
