@@ -152,12 +152,25 @@ __device__ __forceinline__ T adj_term(const TermDev& t, const T* __restrict__ d,
     return w;
 }
 
+__device__ __forceinline__ uint32_t fast_div(uint32_t n, const FastDiv& d) {
+    return (__umulhi(n, d.mul) + n) >> d.shr;
+}
+
+// 1-based row of flat index idx along term t's axis
+__device__ __forceinline__ int term_row(const PlanDev& P, const TermDev& t, int64_t idx) {
+    if (P.fastdiv) {
+        const uint32_t q = fast_div((uint32_t)idx, t.div_stride);
+        return (int)(q - fast_div(q, t.div_len) * (uint32_t)t.len) + 1;
+    }
+    return (int)((idx / t.stride) % t.len) + 1;
+}
+
 template <typename T, bool ADJ>
 __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ u, int64_t idx) {
     T acc = T(0);
     for (int tt = 0; tt < P.nterms; ++tt) {
         const TermDev& t = P.t[tt];
-        const int i = (int)((idx / t.stride) % t.len) + 1;
+        const int i = term_row(P, t, idx);
         const T r = ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
         acc = (tt == 0) ? r : acc + r;
     }

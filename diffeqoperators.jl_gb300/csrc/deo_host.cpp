@@ -710,6 +710,20 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
 // ---------------------------------------------------------------------------
 // plans
 // ---------------------------------------------------------------------------
+// Granlund-Montgomery constants for n / d with n < 2^31: l = ceil(log2 d),
+// mul = floor(2^32 (2^l - d) / d) + 1, q = (umulhi(n, mul) + n) >> l.
+static deo::FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && (1ULL << l) < d) ++l;
+    const unsigned long long m = ((1ULL << 32) * ((1ULL << l) - d)) / d + 1;
+    return deo::FastDiv{(uint32_t)m, l};
+}
+
+extern "C" int deo_fastdiv_probe(uint32_t n, uint32_t d) {  // host check of the constants (tests)
+    const deo::FastDiv f = make_fastdiv(d);
+    const uint32_t t = (uint32_t)(((unsigned long long)n * f.mul) >> 32);
+    return (int)((t + n) >> f.shr);
+}
 struct deo_plan {
     PlanDev dev{};
     deo::UniPlan uni{};
@@ -784,6 +798,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         total *= sizes[k];
     }
     D.total = total;
+    D.fastdiv = total < (1LL << 31) ? 1 : 0;
     for (int t = 0; t < nterms; ++t) {
         const deo_term& tm = terms[t];
         if (tm.path < DEO_PATH_AUTO || tm.path > DEO_PATH_GENERIC)
@@ -810,6 +825,10 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         int64_t stride = 1;
         for (int k = 0; k < ax; ++k) stride *= sizes[k];
         T.stride = stride;
+        if (total < (1LL << 31)) {
+            T.div_stride = make_fastdiv((uint32_t)stride);
+            T.div_len = make_fastdiv((uint32_t)A.len);
+        }
         T.has_field = tm.coeff_field != nullptr;
         T.field = tm.coeff_field;
         T.nvar = (T.has_field && A.wind) ? 2 : 1;
@@ -864,12 +883,10 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             U.lap = (nterms == ndims);
             for (int t = 0; t < nterms && U.lap; ++t)
                 U.lap = U.t[t].axis == t && U.t[t].nk == 2 * H + 1 && U.t[t].off0 == -H;
-            // exact neighbour sums: Float64, one symmetric band shared by every term
+            // exact neighbour sums: Float64, one band shared by every term
             U.ens = U.lap && dtype == DEO_F64;
             for (int t = 0; t < nterms && U.ens; ++t)
                 U.ens = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
-            for (int k = 1; k <= H && U.ens; ++k)
-                U.ens = std::memcmp(&U.t[0].w[H - k], &U.t[0].w[H + k], sizeof(double)) == 0;
             if (U.ens) {
                 const double w0 = U.t[0].w[H];
                 for (int mask = 0; mask < 8; ++mask) {
@@ -878,7 +895,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
                         if (mask & (1 << t)) c = c + w0;  // 2*w0 is exact, so 3*w0 rounds once
                     U.ens_c0[mask] = c;
                 }
-                for (int k = 1; k <= H; ++k) U.ens_w[k] = U.t[0].w[H + k];
+                for (int k = 0; k < 2 * H + 1; ++k) U.ens_w[k] = U.t[0].w[k];  // weight at offset k - H
             }
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
@@ -1106,6 +1123,16 @@ extern "C" deo_status deo_batch_create(int n, const deo_instance* in, int adjoin
     deo_status s = batch_items(*b, tile > 0 ? tile : 8192);
     if (s != DEO_OK) return s;
     *out = b.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_apply_each(int n, const deo_instance* in, int adjoint, void* stream) {
+    if (n > 0 && !in) return fail(DEO_ERR_BAD_ARG, "null argument");
+    for (int i = 0; i < n; ++i) {
+        deo_status s = adjoint ? deo_apply_adjoint(in[i].plan, in[i].u, in[i].du, 1, stream)
+                               : deo_apply(in[i].plan, in[i].u, in[i].du, 1, stream);
+        if (s != DEO_OK) return s;
+    }
     return DEO_OK;
 }
 

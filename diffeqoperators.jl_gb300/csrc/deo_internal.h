@@ -34,10 +34,19 @@ struct RowTabDev {
     const void* W;       // [nw][nexp], element type = plan dtype (k-major: coalesced along rows)
 };
 
+// Division by a runtime constant for 31-bit dividends (Granlund-Montgomery):
+// q = (umulhi(n, mul) + n) >> shr.  Built on the host by make_fastdiv.
+struct FastDiv {
+    uint32_t mul;
+    uint32_t shr;
+};
+
 struct TermDev {
     int64_t stride;      // elements between neighbours along the axis
     int len;             // points along the axis
     int axis;            // 0-based
+    FastDiv div_stride;  // valid when PlanDev::fastdiv
+    FastDiv div_len;
     int nvar;            // 1, or 2 for an upwind operator with a coefficient field (c>=0 / c<0)
     int has_field;
     const void* field;   // coefficient field (same shape/dtype as u) or null
@@ -59,7 +68,7 @@ struct PlanDev {
     int ndims;
     int nterms;
     int dtype;           // 0 f64, 1 f32
-    int pad_;
+    int fastdiv;         // total < 2^31: row indices by FastDiv instead of 64-bit division
     int64_t sizes[8];
     int64_t total;
     TermDev t[DEO_KMAX_TERMS];
@@ -86,13 +95,13 @@ struct UniPlan {
     int lap;         // 1: term t acts on axis t with a centred band of 2H+1 taps (k_lap)
     int64_t n[3];    // sizes along axes 1..3 (1 for absent axes)
     UniTerm t[DEO_KMAX_TERMS];
-    // Exact-neighbour-sum evaluation (Float64, all terms share one symmetric
-    // band): r = c0[mask]*u0 + sum_k w[k] * S_k, where S_k = the exact sum of
-    // the 2*|mask| neighbours at distance k, rounded once.
+    // Exact-neighbour-sum evaluation (Float64, all terms share one band):
+    // r = c0[mask]*u0 + sum_{o != 0} w[o] * S_o, where S_o = the exact sum of
+    // the |mask| neighbours at offset o (one per axis), rounded once.
     int ens;
     int pad2_;
     double ens_c0[8];             // merged centre weight for each mask of axes
-    double ens_w[DEO_MAX_NW];     // weight at distance k = 1..H (index k)
+    double ens_w[DEO_MAX_NW];     // band weight at offset k - H (index k)
 };
 
 // Work item of the batched persistent kernel: `count` points starting at

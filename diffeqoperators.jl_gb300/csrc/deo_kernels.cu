@@ -30,19 +30,41 @@ __global__ void __launch_bounds__(256) k_apply(const __grid_constant__ PlanDev P
 
 // Persistent batched kernel: CTAs pull work items from a global counter until
 // the list is exhausted (no waiting on other CTAs, so no spin loops).
+// The instance's plan is staged into shared memory when a work item belongs to
+// a different instance than the previous one (items are instance-contiguous
+// within a size class, so consecutive pulls usually share it).
+struct PlanCache {
+    static_assert(sizeof(PlanDev) % 8 == 0, "PlanDev copied in 8-byte words");
+    unsigned long long words[sizeof(PlanDev) / 8];
+    const PlanDev* src;
+};
+
+__device__ __forceinline__ const PlanDev& stage_plan(PlanCache& c, const PlanDev* p) {
+    if (p != c.src) {  // uniform across the CTA
+        const unsigned long long* s = reinterpret_cast<const unsigned long long*>(p);
+        for (int q = threadIdx.x; q < (int)(sizeof(PlanDev) / 8); q += blockDim.x) c.words[q] = s[q];
+        __syncthreads();
+        if (threadIdx.x == 0) c.src = p;
+    }
+    return *reinterpret_cast<const PlanDev*>(c.words);
+}
+
 template <typename T, bool ADJ>
 __global__ void __launch_bounds__(256) k_batch(const InstDev* __restrict__ inst, const WorkItem* __restrict__ items,
                                                int64_t n_items, unsigned int* counter) {
     __shared__ int64_t s_item;
+    __shared__ __align__(16) PlanCache cache;
+    if (threadIdx.x == 0) cache.src = nullptr;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int64_t)atomicAdd(counter, 1u);
         __syncthreads();
         const int64_t it = s_item;
+        const bool stale = it < n_items && inst[items[it].inst].plan != cache.src;
         __syncthreads();
         if (it >= n_items) return;
         const WorkItem w = items[it];
         const InstDev in = inst[w.inst];
-        const PlanDev& P = *in.plan;
+        const PlanDev& P = stale ? stage_plan(cache, in.plan) : *reinterpret_cast<const PlanDev*>(cache.words);
         const T* __restrict__ u = reinterpret_cast<const T*>(in.u);
         T* __restrict__ du = reinterpret_cast<T*>(in.du);
         for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
@@ -58,15 +80,18 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_stage(const StageDev* __restrict__ st, const WorkItem* __restrict__ items,
                                                int64_t n_items, unsigned int* counter) {
     __shared__ int64_t s_item;
+    __shared__ __align__(16) PlanCache cache;
+    if (threadIdx.x == 0) cache.src = nullptr;
     for (;;) {
         if (threadIdx.x == 0) s_item = (int64_t)atomicAdd(counter, 1u);
         __syncthreads();
         const int64_t it = s_item;
+        const bool stale = it < n_items && st[items[it].inst].plan != cache.src;
         __syncthreads();
         if (it >= n_items) return;
         const WorkItem w = items[it];
         const StageDev S = st[w.inst];
-        const PlanDev& P = *S.plan;
+        const PlanDev& P = stale ? stage_plan(cache, S.plan) : *reinterpret_cast<const PlanDev*>(cache.words);
         const T* a = reinterpret_cast<const T*>(S.a);  // may alias out
         const T* b = reinterpret_cast<const T*>(S.b);
         const T* __restrict__ c = reinterpret_cast<const T*>(S.c);

@@ -14,14 +14,14 @@
 // Interior points (band rows along every axis) are evaluated from the ring:
 //   * FMA mode: the reference's per-term tap order, bit-identical to the
 //     generic row-table evaluator;
-//   * ENS mode (Float64, all terms share one symmetric band): the 2*NT
-//     neighbours at each distance k have the same weight w_k, so
-//       r = c0 * u0 + sum_k w_k * S_k,
-//     where S_k is their sum computed exactly in 64-bit integer arithmetic
-//     (aligned to the largest of the 2*NT exponents; bits below 2^-59 of that
-//     value are dropped) and rounded once.  This takes H + 1 FP64 instructions
-//     per point instead of NT*(2H+1) + NT - 1, which is what bounds a Float64
-//     stencil on this part (1.68 DFMA/clk/SM).
+//   * ENS mode (Float64, all terms share one band): the NT neighbours at
+//     offset o (one per axis) have the same weight w[o], so
+//       r = c0 * u0 + sum_{o != 0} w[o] * S_o,
+//     where S_o is their sum computed exactly in 64-bit integer arithmetic
+//     (aligned to the largest of the NT exponents; bits below 2^-59 of that
+//     value are dropped) and rounded once.  This takes 2H + 1 FP64
+//     instructions per point instead of NT*(2H+1) + NT - 1, which is what
+//     bounds a Float64 stencil on this part (1.68 DFMA/clk/SM).
 // Points on boundary rows use the generic evaluator for the affected terms.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -201,25 +201,44 @@ __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtenso
                     bool ok = true;
 #pragma unroll
                     for (int k = 1; k <= H; ++k) {
-                        double v[2 * NT];
-                        v[0] = pc[cc - k];
-                        v[1] = pc[cc + k];
-                        v[2] = pc[cc - k * C::BX];
-                        v[3] = pc[cc + k * C::BX];
+                        // the NT neighbours at offset -k share weight w[H-k], those at +k share w[H+k]
+                        double vm[NT], vp[NT];
+                        vm[0] = pc[cc - k];
+                        vp[0] = pc[cc + k];
+                        vm[1] = pc[cc - k * C::BX];
+                        vp[1] = pc[cc + k * C::BX];
                         if constexpr (NT == 3) {
-                            v[4] = plane(jc - k)[cc];
-                            v[5] = plane(jc + k)[cc];
+                            vm[2] = plane(jc - k)[cc];
+                            vp[2] = plane(jc + k)[cc];
                         }
-                        bool okk;
-                        const double s = ens_sum<2 * NT>(v, okk);
-                        ok = ok && okk;
-                        r = fma(U.ens_w[k], s, r);
+                        bool okm, okp;
+                        const double sm = ens_sum<NT>(vm, okm);
+                        const double sp = ens_sum<NT>(vp, okp);
+                        ok = ok && okm && okp;
+                        r = fma(U.ens_w[H - k], sm, r);
+                        r = fma(U.ens_w[H + k], sp, r);
                     }
                     if (ok) {
                         total = (T)zero_fix(r);
                         done = true;
                     }
                 }
+            }
+            if (!done && xy_fast && z_fast) {
+                // interior: every term's band from the ring, the reference's tap order
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int k = 0; k < 2 * H + 1; ++k) {
+                        const int o = k - H;
+                        const T v = t == 0 ? pc[cc + o] : (t == 1 ? pc[cc + o * C::BX] : plane(jc + o)[cc]);
+                        acc = fma(uni_w<T>(U.t[t], k), v, acc);
+                    }
+                    total = (t == 0) ? acc : total + acc;
+                }
+                total = zero_fix(total);
+                done = true;
             }
             if (!done) {
                 // per term: band rows from the ring, boundary rows through the row tables

@@ -35,6 +35,12 @@ class Batch:
         check(L.lib().deo_batch_create(n, arr, int(bool(adjoint)), int(tile), int(ctas_per_sm), C.byref(h)))
         self._h = h
         self.adjoint = adjoint
+        self._arr, self._n = arr, n
+
+    def run_one_launch_each(self, stream=None):
+        """The same instances with one launch per instance (native host loop)."""
+        check(L.lib().deo_apply_each(self._n, self._arr, int(bool(self.adjoint)),
+                                     stream if stream is not None else _stream_ptr()))
 
     def __del__(self):
         try:

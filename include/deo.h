@@ -173,11 +173,12 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     row-table kernel.
  *   DEO_OPT_TMA: Laplacian-type plans (term t a centred band on axis t) stream
  *     planes with TMA into a shared-memory ring; 0 uses the register-queue kernel.
- *   DEO_OPT_EXACT_SUMS: Float64 plans whose terms share one symmetric band sum
- *     the equal-weight neighbours exactly in integer arithmetic and round once
- *     (H+1 FP64 instructions per point instead of NT*(2H+1)+NT-1; result within
- *     a few ulp of sum|c_k u_k| of the reference's order).  0 keeps the
- *     reference's per-term tap order, bit-identical to the generic kernel.
+ *   DEO_OPT_EXACT_SUMS: Float64 Laplacian-type plans whose terms share one
+ *     band sum the equal-weight neighbours (one per axis at each offset)
+ *     exactly in integer arithmetic and round once (2H+1 FP64 instructions per
+ *     point instead of NT*(2H+1)+NT-1; result within a few ulp of
+ *     sum|c_k u_k| of the reference's order).  0 keeps the reference's
+ *     per-term tap order, bit-identical to the generic kernel.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
@@ -225,6 +226,9 @@ typedef struct {
 /* tile = points per work item (0 = autotuned), ctas_per_sm (0 = autotuned). */
 deo_status deo_batch_create(int n, const deo_instance* inst, int adjoint, int tile, int ctas_per_sm,
                             deo_batch** out);
+/* The same instances with one launch each, issued from a host loop: the
+ * baseline the batched launch is measured against. */
+deo_status deo_apply_each(int n, const deo_instance* inst, int adjoint, void* stream);
 /* Runs the batch; with use_graph = 1 the launch is captured once into a CUDA
  * graph and replayed. */
 deo_status deo_batch_run(deo_batch* b, int use_graph, void* stream);

@@ -130,3 +130,18 @@ def test_operator_from_tables_roundtrip():
                 high_boundary_coefs=P.high_boundary_coefs, coefficients=P.coefficients)
     R = deo.operator_from_tables(desc)
     _same(R.array(), P.array())
+
+
+def test_fast_division_constants():
+    # the kernels derive row indices with (umulhi(n, mul) + n) >> shr for 31-bit n
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    lib.deo_fastdiv_probe.restype = ctypes.c_int
+    lib.deo_fastdiv_probe.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    rng = np.random.default_rng(0)
+    ds = [1, 2, 3, 5, 7, 256, 257, 1023, 1025, 65535, 65537, (1 << 20) + 1, 1 << 30, (1 << 31) - 1]
+    ds += [int(d) for d in rng.integers(1, 1 << 31, 300)]
+    for d in ds:
+        ns = [0, 1, d - 1, d, d + 1, 2 * d - 1, (1 << 31) - 1] + [int(n) for n in rng.integers(0, 1 << 31, 64)]
+        for n in ns:
+            if 0 <= n < (1 << 31):
+                assert lib.deo_fastdiv_probe(n, d) == n // d, (n, d)
