@@ -19,6 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "deo_kernels.o": ("nvcc", "deo_kernels.cu"),
     "deo_tma.o": ("nvcc", "deo_tma.cu"),
+    "deo_static.o": ("nvcc", "deo_static.cu"),
     "deo_host.o": ("cxx", "deo_host.cpp"),
 }
 

@@ -909,6 +909,12 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
 }
 
 extern "C" void deo_plan_destroy(deo_plan* p) { delete p; }
+
+// internal accessors used by deo_static.cu
+extern "C" const PlanDev* deo_plan_device_copy(const deo_plan* p) { return p->d_plan; }
+extern "C" int64_t deo_plan_points(const deo_plan* p) { return p->dev.total; }
+extern "C" int deo_plan_dtype_code(const deo_plan* p) { return p->dev.dtype; }
+extern "C" deo_status deo_set_error(deo_status s, const char* msg) { return fail(s, "%s", msg); }
 extern "C" size_t deo_plan_table_bytes(const deo_plan* p) { return p ? p->table_bytes : 0; }
 
 static deo_status check_ptrs(const deo_plan* p, const void* a, const void* b) {

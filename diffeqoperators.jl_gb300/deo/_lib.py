@@ -120,6 +120,7 @@ def lib():
     proto("deo_stage_batch_create", st, C.c_int, C.POINTER(Stage), C.c_int, C.c_int, C.POINTER(_vp))
     proto("deo_batch_run", st, _vp, C.c_int, _vp)
     proto("deo_apply_each", st, C.c_int, C.POINTER(Instance), C.c_int, _vp)
+    proto("deo_batch_apply_noalloc", st, C.c_int, C.POINTER(Instance), C.c_int, C.c_int, _vp)
     proto("deo_batch_set_buffers", st, _vp, C.c_int, _vp, _vp)
     proto("deo_batch_config", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64))
     proto("deo_batch_destroy", None, _vp)
@@ -147,6 +148,6 @@ EXPORTED = [
     "deo_operator_destroy", "deo_operator_array", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
-    "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
+    "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune",
 ]

@@ -253,6 +253,27 @@ typedef struct {
 } deo_stage;
 deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int ctas_per_sm, deo_batch** out);
 
+/* Batched apply that allocates no device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc -- a stream being
+ * captured into a CUDA graph, a host application that owns every device
+ * allocation, a server that must not grow its device footprint after
+ * admitting a request -- this runs the same persistent kernel as
+ * deo_batch_run with its instance table, work-list and counter in one static
+ * device array of DEO_NOALLOC_SCRATCH_BYTES (1 MiB) that every GPU loading
+ * libdeo holds until process exit.  The plans (created earlier, where
+ * allocation was possible) and the instances' buffers are the caller's.
+ * Limit: 256 + 24*n (rounded up to 256) + 16*ceil(points_i / tile) summed over
+ * instances bytes; larger batches return DEO_ERR_UNSUPPORTED.  tile = 0 means
+ * 8192 points per work item.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  Each call copies its work-list from host memory, which
+ * waits for earlier work on `stream`.  Every call reuses the same array (the
+ * counter is cleared each time), so calls that overlap on the GPU -- on
+ * different streams or host threads -- race and must be serialised by the
+ * caller. */
+#define DEO_NOALLOC_SCRATCH_BYTES (1 << 20)
+deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, int adjoint, int tile, void* stream);
+
 /* Autotuner: times candidate (tile, ctas_per_sm) pairs on this batch and
  * keeps the fastest; results are cached per workload signature in the file
  * `cache_path` (NULL = in-process cache only). */
