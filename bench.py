@@ -165,9 +165,19 @@ def max_over_ranks(x: float, ws: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def shard(n: int, rank: int, ws: int) -> range:
+    """Instances (batched / served workloads) owned by `rank`: a contiguous
+    block, sizes differing by at most one.  Ranks run independent replicas of
+    the path; no collective touches the data."""
+    q, r = divmod(n, ws)
+    lo = rank * q + min(rank, r)
+    return range(lo, lo + q + (1 if rank < r else 0))
 
 
 # ---------------------------------------------------------------------------

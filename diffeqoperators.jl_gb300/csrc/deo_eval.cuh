@@ -102,6 +102,17 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
     const RowTabDev& tb = row_variant<T>(t, base, i, c);
     const RowInfo r = row_info(tb, i);
     const int L2 = t.len + 2;
+    if (r.band && r.p0 >= 2 && r.p0 + r.nk <= L2) {
+        // band row away from the ghosts: straight tap loop (same order and rounding)
+        const T* __restrict__ xp = line + (int64_t)(r.p0 - 2) * s;
+        T acc = T(0);
+        for (int k = 0; k < r.nk; ++k) {
+            T w = band_w<T>(tb, k);
+            if (t.has_field) w = c * w;
+            acc = fma(w, __ldg(xp + (int64_t)k * s), acc);
+        }
+        return acc;
+    }
     T gl = T(0), gr = T(0);
     if (r.p0 == 1) gl = ghost_left<T>(t, line);
     if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line);
@@ -122,6 +133,17 @@ __device__ __forceinline__ T adj_column(const TermDev& t, const T* __restrict__ 
     const int64_t s = t.stride;
     const int lo = __ldg(t.rlo + (p - 1)), hi = __ldg(t.rhi + (p - 1));
     T acc = T(0);
+    if (!t.has_field) {
+        // column inside the band: the touching rows are exactly the band rows
+        // p - off - nk + 1 .. p - off; same row order as the general loop below
+        const RowTabDev& tb = t.tab[0];
+        const int blo = p - tb.band_p0_off - tb.band_nk + 1, bhi = p - tb.band_p0_off;
+        if (lo == blo && hi == bhi && blo >= tb.ilo && bhi <= tb.ihi) {
+            for (int i = lo; i <= hi; ++i)
+                acc = fma(band_w<T>(tb, p - i - tb.band_p0_off), __ldg(d + base + (int64_t)(i - 1) * s), acc);
+            return acc;
+        }
+    }
     for (int i = lo; i <= hi; ++i) {
         T c;
         const RowTabDev& tb = row_variant<T>(t, base, i, c);

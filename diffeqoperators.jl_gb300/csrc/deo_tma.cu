@@ -133,159 +133,174 @@ struct TmaCfg {
     static constexpr int SMEM = P * SLOT;
 };
 
+// Work unit u = (tile x, tile y, z chunk); a persistent grid of G CTAs takes
+// units b, b + G, b + 2G, ... (static, so one plan may run on several streams
+// at once).  Planes stream through the ring with a running count, so slot and
+// mbarrier phase carry over from one unit to the next.
+struct LapGrid {
+    int tiles_x, tiles_y, chunks, zc;
+    int units;
+    int perm;  // coprime with units: unit k of the round-robin is (k * perm) % units,
+               // so one CTA's units are spread over tile columns and z chunks
+};
+
 template <typename T, int H, int NT, bool ENS>
 __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtensorMap tmap,
-                                                 const __grid_constant__ UniPlan U, const PlanDev* __restrict__ Pd,
-                                                 const T* __restrict__ u, T* __restrict__ du, int overwrite, int zc) {
+                                                 const __grid_constant__ UniPlan U, const LapGrid g,
+                                                 const PlanDev* __restrict__ Pd, const T* __restrict__ u,
+                                                 T* __restrict__ du, int overwrite) {
     using C = TmaCfg<T, H>;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t mbar[C::P];
+    constexpr int HZ = NT == 3 ? H : 0;  // z halo (2-D plans stream one plane)
     const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
-    const int x0 = blockIdx.x * C::TX, y0 = blockIdx.y * C::TY;
-    const int x = x0 + tx, y = y0 + ty;
-    const int z0 = blockIdx.z * zc;
-    const int z1 = min(z0 + zc, nz);
-    constexpr int HZ = NT == 3 ? H : 0;  // z halo (2-D plans stream one plane)
-    const int npl = (z1 - z0) + 2 * HZ;  // planes z0-HZ .. z1-1+HZ
-    const bool inxy = x < nx && y < ny;
     const int64_t sxy = (int64_t)nx * ny;
-    const int64_t col = (int64_t)y * nx + x;
     const int cc = (ty + H) * C::BX + tx + C::HR;  // this thread's point inside a plane slot
-
     if (tid == 0) {
         for (int s = 0; s < C::P; ++s) mbar_init(&mbar[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    int issued = 0;
-    if (tid == 0) {
-        const int pre = min(C::P, npl);
-        for (int j = 0; j < pre; ++j) {
-            mbar_expect_tx(&mbar[j], C::PLANE_BYTES);
-            tma_load_3d(smem + j * C::SLOT, &tmap, &mbar[j], x0 - C::HR, y0 - H, z0 - HZ + j);
-        }
-        issued = pre;
-    }
-    auto plane = [&](int j) -> const T* {
-        return reinterpret_cast<const T*>(smem + (j & (C::P - 1)) * C::SLOT);
+    auto slot = [&](int gj) -> const T* {
+        return reinterpret_cast<const T*>(smem + (gj & (C::P - 1)) * C::SLOT);
     };
-    const bool xy_fast = (x0 + 1 >= U.t[0].flo) && (x0 + C::TX <= U.t[0].fhi) && (y0 + 1 >= U.t[1].flo) &&
-                         (y0 + C::TY <= U.t[1].fhi);
-    int waited = 0;
+    int base = 0;        // running plane count of this CTA (ring position of the unit's plane 0)
+    int issued = 0;      // planes issued in the current unit (thread 0)
+    int waited = 0;      // planes of the current unit known complete
     bool aborted = false;
-    for (int z = z0; z < z1; ++z) {
-        const int jc = z - z0 + HZ;
-        bool timeout = false;
-        while (waited <= jc + HZ) {
-            const uint32_t par = (uint32_t)((waited / C::P) & 1);
-            uint32_t it = 0;
-            while (!mbar_try_wait(&mbar[waited & (C::P - 1)], par)) {
-                if (++it > (1u << 22)) {
-                    timeout = true;
-                    break;
-                }
-            }
-            if (timeout) break;
-            ++waited;
-        }
-        if (inxy && !timeout) {
-            const int64_t idx = (int64_t)z * sxy + col;
-            const T* pc = plane(jc);
-            const bool z_fast = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
-            T total;
-            bool done = false;
-            if constexpr (ENS) {
-                if (xy_fast && z_fast) {
-                    double r = U.ens_c0[(1 << NT) - 1] * (double)pc[cc];
-                    bool ok = true;
-#pragma unroll
-                    for (int k = 1; k <= H; ++k) {
-                        // the NT neighbours at offset -k share weight w[H-k], those at +k share w[H+k]
-                        double vm[NT], vp[NT];
-                        vm[0] = pc[cc - k];
-                        vp[0] = pc[cc + k];
-                        vm[1] = pc[cc - k * C::BX];
-                        vp[1] = pc[cc + k * C::BX];
-                        if constexpr (NT == 3) {
-                            vm[2] = plane(jc - k)[cc];
-                            vp[2] = plane(jc + k)[cc];
-                        }
-                        bool okm, okp;
-                        const double sm = ens_sum<NT>(vm, okm);
-                        const double sp = ens_sum<NT>(vp, okp);
-                        ok = ok && okm && okp;
-                        r = fma(U.ens_w[H - k], sm, r);
-                        r = fma(U.ens_w[H + k], sp, r);
-                    }
-                    if (ok) {
-                        total = (T)zero_fix(r);
-                        done = true;
-                    }
-                }
-            }
-            if (!done && xy_fast && z_fast) {
-                // interior: every term's band from the ring, the reference's tap order
-#pragma unroll
-                for (int t = 0; t < NT; ++t) {
-                    T acc = T(0);
-#pragma unroll
-                    for (int k = 0; k < 2 * H + 1; ++k) {
-                        const int o = k - H;
-                        const T v = t == 0 ? pc[cc + o] : (t == 1 ? pc[cc + o * C::BX] : plane(jc + o)[cc]);
-                        acc = fma(uni_w<T>(U.t[t], k), v, acc);
-                    }
-                    total = (t == 0) ? acc : total + acc;
-                }
-                total = zero_fix(total);
-                done = true;
-            }
-            if (!done) {
-                // per term: band rows from the ring, boundary rows through the row tables
-#pragma unroll
-                for (int t = 0; t < NT; ++t) {
-                    const int row = (t == 0 ? x : (t == 1 ? y : z)) + 1;
-                    T acc;
-                    if (row >= U.t[t].flo && row <= U.t[t].fhi) {
-                        acc = T(0);
-#pragma unroll
-                        for (int k = 0; k < 2 * H + 1; ++k) {
-                            const int o = k - H;
-                            const T v = t == 0 ? pc[cc + o] : (t == 1 ? pc[cc + o * C::BX] : plane(jc + o)[cc]);
-                            acc = fma(uni_w<T>(U.t[t], k), v, acc);
-                        }
-                    } else {
-                        acc = eval_term<T>(Pd->t[t], u, idx, row);
-                    }
-                    total = (t == 0) ? acc : total + acc;
-                }
-                total = zero_fix(total);
-            }
-            du[idx] = overwrite ? total : total + du[idx];
-        }
-        if (__syncthreads_or(timeout)) {
-            aborted = true;
-            break;
-        }
-        // plane jc - H has left the window: refill its slot
+    for (int k = blockIdx.x; k < g.units && !aborted; k += gridDim.x) {
+        const int unit = (int)(((long long)k * g.perm) % g.units);
+        const int txi = unit % g.tiles_x;
+        const int rest = unit / g.tiles_x;
+        const int tyi = rest % g.tiles_y;
+        const int ci = rest / g.tiles_y;
+        const int x0 = txi * C::TX, y0 = tyi * C::TY;
+        const int x = x0 + tx, y = y0 + ty;
+        const int z0 = ci * g.zc;
+        const int z1 = min(z0 + g.zc, nz);
+        const int npl = (z1 - z0) + 2 * HZ;
+        const bool inxy = x < nx && y < ny;
+        const int64_t col = (int64_t)y * nx + x;
+        // rows of this thread along x and y, and whether they are band rows without ghosts
+        const bool bx = x + 1 >= U.t[0].flo && x + 1 <= U.t[0].fhi;
+        const bool by = y + 1 >= U.t[1].flo && y + 1 <= U.t[1].fhi;
         if (tid == 0) {
-            const int jn = (jc - HZ) + C::P;
-            if (jn < npl) {
+            const int pre = min(C::P, npl);
+            for (int j = 0; j < pre; ++j) {
+                const int s = (base + j) & (C::P - 1);
                 fence_proxy_async();
-                const int s = jn & (C::P - 1);
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
-                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
-                issued = jn + 1;
+                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
+            }
+            issued = pre;
+        }
+        waited = 0;
+        for (int z = z0; z < z1; ++z) {
+            const int jc = z - z0 + HZ;
+            bool timeout = false;
+            while (waited <= jc + HZ) {
+                const int gj = base + waited;
+                const uint32_t par = (uint32_t)((gj / C::P) & 1);
+                uint32_t it = 0;
+                while (!mbar_try_wait(&mbar[gj & (C::P - 1)], par)) {
+                    if (++it > (1u << 22)) {
+                        timeout = true;
+                        break;
+                    }
+                }
+                if (timeout) break;
+                ++waited;
+            }
+            if (inxy && !timeout) {
+                const int64_t idx = (int64_t)z * sxy + col;
+                const T* pc = slot(base + jc);
+                const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
+                const bool band[3] = {bx, by, bz};
+                T total;
+                bool done = false;
+                if constexpr (ENS) {
+                    // exact sums over the axes whose row is a band row; other axes by their row tables
+                    const int mask = (bx ? 1 : 0) | (by ? 2 : 0) | ((NT == 3 && bz) ? 4 : 0);
+                    if (mask) {
+                        double r = U.ens_c0[mask] * (double)pc[cc];
+                        bool ok = true;
+#pragma unroll
+                        for (int k = 1; k <= H; ++k) {
+                            double vm[NT], vp[NT];
+                            vm[0] = bx ? (double)pc[cc - k] : 0.0;
+                            vp[0] = bx ? (double)pc[cc + k] : 0.0;
+                            vm[1] = by ? (double)pc[cc - k * C::BX] : 0.0;
+                            vp[1] = by ? (double)pc[cc + k * C::BX] : 0.0;
+                            if constexpr (NT == 3) {
+                                vm[2] = bz ? (double)slot(base + jc - k)[cc] : 0.0;
+                                vp[2] = bz ? (double)slot(base + jc + k)[cc] : 0.0;
+                            }
+                            bool okm, okp;
+                            const double sm = ens_sum<NT>(vm, okm);
+                            const double sp = ens_sum<NT>(vp, okp);
+                            ok = ok && okm && okp;
+                            r = fma(U.ens_w[H - k], sm, r);
+                            r = fma(U.ens_w[H + k], sp, r);
+                        }
+                        if (ok) {
+#pragma unroll
+                            for (int t = 0; t < NT; ++t)
+                                if (!band[t]) r = r + (double)eval_term<T>(Pd->t[t], u, idx, (t == 0 ? x : (t == 1 ? y : z)) + 1);
+                            total = (T)zero_fix(r);
+                            done = true;
+                        }
+                    }
+                }
+                if (!done) {
+                    // the reference's per-term tap order: band rows from the ring, others by row tables
+#pragma unroll
+                    for (int t = 0; t < NT; ++t) {
+                        T acc;
+                        if (band[t]) {
+                            acc = T(0);
+#pragma unroll
+                            for (int k = 0; k < 2 * H + 1; ++k) {
+                                const int o = k - H;
+                                const T v = t == 0 ? pc[cc + o]
+                                                   : (t == 1 ? pc[cc + o * C::BX] : slot(base + jc + o)[cc]);
+                                acc = fma(uni_w<T>(U.t[t], k), v, acc);
+                            }
+                        } else {
+                            acc = eval_term<T>(Pd->t[t], u, idx, (t == 0 ? x : (t == 1 ? y : z)) + 1);
+                        }
+                        total = (t == 0) ? acc : total + acc;
+                    }
+                    total = zero_fix(total);
+                }
+                du[idx] = overwrite ? total : total + du[idx];
+            }
+            if (__syncthreads_or(timeout)) {
+                aborted = true;
+                break;
+            }
+            // plane jc - HZ has left the window: refill its slot
+            if (tid == 0) {
+                const int jn = (jc - HZ) + C::P;
+                if (jn < npl) {
+                    const int s = (base + jn) & (C::P - 1);
+                    fence_proxy_async();
+                    mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                    tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
+                    issued = jn + 1;
+                }
             }
         }
+        if (!aborted) base += npl;
     }
     if (aborted && tid == 0) {
         atomicOr(&g_deo_status, 1u);
         // wait (bounded) for this CTA's copies still in flight before its shared memory is released
         for (int j = waited; j < issued; ++j) {
-            const uint32_t par = (uint32_t)((j / C::P) & 1);
+            const int gj = base + j;
+            const uint32_t par = (uint32_t)((gj / C::P) & 1);
             for (uint32_t it = 0; it < (1u << 22); ++it)
-                if (mbar_try_wait(&mbar[j & (C::P - 1)], par)) break;
+                if (mbar_try_wait(&mbar[gj & (C::P - 1)], par)) break;
         }
     }
 }
@@ -326,23 +341,49 @@ static int launch_tma(const UniPlan* up, const PlanDev* dp, const void* u, void*
                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return (int)cudaErrorNotSupported;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
         cudaError_t e = cudaFuncSetAttribute(k_lap_tma<T, H, NT, ENS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              C::SMEM);
         if (e != cudaSuccess) return (int)e;
-        attr_set = true;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lap_tma<T, H, NT, ENS>, C::TX * C::TY, C::SMEM);
+        if (e != cudaSuccess || per_sm < 1) per_sm = 1;
     }
-    const int64_t bx = (nx + C::TX - 1) / C::TX, by = (ny + C::TY - 1) / C::TY;
-    int zc = 1;
+    LapGrid g;
+    g.tiles_x = (int)((nx + C::TX - 1) / C::TX);
+    g.tiles_y = (int)((ny + C::TY - 1) / C::TY);
+    const int64_t G = (int64_t)sms * per_sm;
+    const int64_t tiles = (int64_t)g.tiles_x * g.tiles_y;
+    // z chunk: at least 12 planes (halo overhead 2H/zc), chosen so the units
+    // fill the persistent grid's rounds as evenly as possible
+    g.zc = (int)nz;
     if (NT == 3) {
-        const int64_t want = 152 * 4;  // CTAs for about four per SM
-        const int64_t chunks = std::max<int64_t>(1, (want + bx * by - 1) / (bx * by));
-        zc = (int)std::max<int64_t>(16, (nz + chunks - 1) / chunks);
-        zc = (int)std::min<int64_t>(zc, nz);
+        double best = -1.0;
+        const int zmin = (int)std::min<int64_t>(nz, 12);
+        for (int zc = zmin; zc <= nz; ++zc) {
+            const int64_t units = tiles * ((nz + zc - 1) / zc);
+            const int64_t rounds = (units + G - 1) / G;
+            const double eff = (double)units / (double)(rounds * G) * (double)zc / (double)(zc + 2 * H) *
+                               ((double)nz / (double)(((nz + zc - 1) / zc) * zc));
+            if (eff > best + 1e-9) {
+                best = eff;
+                g.zc = zc;
+            }
+        }
     }
-    dim3 grid((unsigned)bx, (unsigned)by, (unsigned)((nz + zc - 1) / zc));
-    k_lap_tma<T, H, NT, ENS><<<grid, dim3(C::TX, C::TY), C::SMEM, st>>>(map, *up, dp, (const T*)u, (T*)du, ow, zc);
+    g.chunks = (int)((nz + g.zc - 1) / g.zc);
+    g.units = (int)(tiles * g.chunks);
+    g.perm = 1;
+    for (int cand : {7919, 6007, 4099, 2053, 1031, 521, 263, 131, 67, 37, 17}) {
+        int a = cand, b = g.units;
+        while (b) { const int t = a % b; a = b; b = t; }
+        if (a == 1 && cand < g.units) { g.perm = cand; break; }
+    }
+    const int grid = (int)std::min<int64_t>(G, g.units);
+    k_lap_tma<T, H, NT, ENS><<<grid, dim3(C::TX, C::TY), C::SMEM, st>>>(map, *up, g, dp, (const T*)u, (T*)du, ow);
     return (int)cudaGetLastError();
 }
 
