@@ -271,6 +271,8 @@ def run_ours(args, ws, rank):
     hbm, peak_kind = peaks()
     alg_bytes = 2 * esize * npts
     achieved = alg_bytes / (ms_step / 1e3) / 1e9
+    path = ("tma-interior+shell" + ("+exact-sums" if plan.get_option(deo.DEO_OPT_EXACT_SUMS) else "")
+            if plan.get_option(deo.DEO_OPT_TMA) else ("tiled" if plan.uses_fast_path else "generic"))
     traffic = profiled_traffic(f"k_apply_lap3d_{n}_{dtype_name}")
     line = {
         "metric": "grid-pts/s (3-D 256^3 Laplacian apply)",
@@ -289,10 +291,10 @@ def run_ours(args, ws, rank):
                    "operator": "CenteredDifference{1,2,3}(2,4,1/257,256) summed",
                    "bc": "RobinBC((1,.5,0),(1,.5,0),h,1) composed on every face",
                    "l2_policy": f"{nbuf} rotating input/output pairs ({nbuf * 2 * npts * esize / 2**30:.2f} GiB) > L2",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU", "kernel_path": path},
         "e2e": {"value": ws * npts / e2e_s, "unit": "grid-pts/s", "h2d_bytes_per_step": npts * esize,
                 "d2h_bytes_per_step": npts * esize, "path": "deo_apply_host (C ABI, pinned host buffers)"},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (2 if plan.get_option(deo.DEO_OPT_TMA) else 1),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": alg_bytes,
                      "traffic": traffic},

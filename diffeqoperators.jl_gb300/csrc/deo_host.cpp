@@ -887,6 +887,8 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             U.ens = U.lap && dtype == DEO_F64;
             for (int t = 0; t < nterms && U.ens; ++t)
                 U.ens = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
+            for (int k = 0; k < 2 * H + 1 && U.ens; ++k)
+                U.ens = k == H || std::fpclassify(U.t[0].w[k]) == FP_NORMAL;  // scaled through their exponents
             if (U.ens) {
                 const double w0 = U.t[0].w[H];
                 for (int mask = 0; mask < 8; ++mask) {
@@ -940,7 +942,7 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
     switch (option) {
         case DEO_OPT_FAST_PATH: p->fast_path = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_TMA: p->use_tma = value ? 1 : 0; return DEO_OK;
-        case DEO_OPT_EXACT_SUMS: p->exact_sums = value ? 1 : 0; return DEO_OK;
+        case DEO_OPT_EXACT_SUMS: p->exact_sums = (value == 2) ? 2 : (value ? 1 : 0); return DEO_OK;
     }
     return fail(DEO_ERR_BAD_ARG, "unknown plan option %d", option);
 }

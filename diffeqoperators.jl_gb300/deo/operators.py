@@ -612,8 +612,8 @@ class Plan:
     def table_bytes(self) -> int:
         return int(L.lib().deo_plan_table_bytes(self._h))
 
-    def set_option(self, option: int, value: bool):
-        check(L.lib().deo_plan_set_option(self._h, int(option), int(bool(value))))
+    def set_option(self, option: int, value):
+        check(L.lib().deo_plan_set_option(self._h, int(option), int(value)))
         return self
 
     def get_option(self, option: int) -> bool:

@@ -178,7 +178,9 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     exactly in integer arithmetic and round once (2H+1 FP64 instructions per
  *     point instead of NT*(2H+1)+NT-1; result within a few ulp of
  *     sum|c_k u_k| of the reference's order).  0 keeps the reference's
- *     per-term tap order, bit-identical to the generic kernel.
+ *     per-term tap order, bit-identical to the generic kernel.  Value 2 selects
+ *     the earlier exact-sum kernel that decomposes values at every use (for
+ *     comparison). 
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2

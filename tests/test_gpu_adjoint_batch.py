@@ -117,7 +117,8 @@ def test_fast_path_bitwise_equals_generic(cuda, case):
     tol = 4 * np.spacing(O.abs_scale(oterms, u))
     outs = {}
     # (fast path, TMA ring, exact neighbour sums)
-    for name, opts in {"tma-ens": (1, 1, 1), "tma-fma": (1, 1, 0), "queue": (1, 0, 0), "generic": (0, 0, 0)}.items():
+    for name, opts in {"tma-ens": (1, 1, 1), "tma-ens-v1": (1, 1, 2), "tma-fma": (1, 1, 0), "queue": (1, 0, 0),
+                       "generic": (0, 0, 0)}.items():
         p.set_option(deo.DEO_OPT_FAST_PATH, opts[0])
         p.set_option(deo.DEO_OPT_TMA, opts[1])
         p.set_option(deo.DEO_OPT_EXACT_SUMS, opts[2])
@@ -262,7 +263,7 @@ def test_full_size_laplacian_against_oracle(cuda, dtype):
     ud = deo.julia_array((n, n, n), tdt)
     ud.copy_(torch.from_numpy(u).to(tdt))
     report = {}
-    modes = {"exact-sums": 1, "reference-order": 0} if dtype == "f64" else {"default": 1}
+    modes = {"exact-sums": 1, "exact-sums-v1": 2, "reference-order": 0} if dtype == "f64" else {"default": 1}
     for name, ens in modes.items():
         plan.set_option(deo.DEO_OPT_EXACT_SUMS, ens)
         du = deo.julia_array((n, n, n), tdt)
