@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -710,14 +712,7 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
 // ---------------------------------------------------------------------------
 // plans
 // ---------------------------------------------------------------------------
-// Granlund-Montgomery constants for n / d with n < 2^31: l = ceil(log2 d),
-// mul = floor(2^32 (2^l - d) / d) + 1, q = (umulhi(n, mul) + n) >> l.
-static deo::FastDiv make_fastdiv(uint32_t d) {
-    uint32_t l = 0;
-    while (l < 32 && (1ULL << l) < d) ++l;
-    const unsigned long long m = ((1ULL << 32) * ((1ULL << l) - d)) / d + 1;
-    return deo::FastDiv{(uint32_t)m, l};
-}
+using deo::make_fastdiv;
 
 extern "C" int deo_fastdiv_probe(uint32_t n, uint32_t d) {  // host check of the constants (tests)
     const deo::FastDiv f = make_fastdiv(d);
@@ -727,19 +722,31 @@ extern "C" int deo_fastdiv_probe(uint32_t n, uint32_t d) {  // host check of the
 struct deo_plan {
     PlanDev dev{};
     deo::UniPlan uni{};
+    deo::ShellPlan shell{};
     int fast_path = 1;   // DEO_OPT_FAST_PATH
     int use_tma = 1;     // DEO_OPT_TMA
     int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
+    int timing = 0;      // DEO_OPT_LAUNCH_TIMING
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
+    deo::ShellPlan* d_shell = nullptr;  // device copy of `shell` when shell.ok
     std::vector<void*> allocs;
     size_t table_bytes = 0;
     void* stage_u = nullptr;
     void* stage_du = nullptr;
+    // kernels launched by the last forward apply (diagnostics; last writer wins)
+    mutable std::atomic<const char*> last_kernel{""};
+    mutable std::atomic<const char*> last_kernel2{""};
+    // launch timing: events around each launch of the last forward apply
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    mutable int ev_launches = 0;
     ~deo_plan() {
         for (void* p : allocs) cudaFree(p);
         if (d_plan) cudaFree(d_plan);
+        if (d_shell) cudaFree(d_shell);
         if (stage_u) cudaFree(stage_u);
         if (stage_du) cudaFree(stage_du);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -777,6 +784,84 @@ static deo_status upload_tab(deo_plan& P, HostTab& T, int dtype, RowTabDev& out)
         for (int k = 0; k < DEO_MAX_NW; ++k) fb[k] = (float)tmp[k];
     }
     return DEO_OK;
+}
+
+// The rows of term t outside its interior range [flo, fhi] (the range the
+// tiled kernels evaluate; same formulas as the UniPlan setup), copied from its
+// row table for the shell kernel.  Marks sp.ok = -1 if they do not fit.
+// n values into dst as the plan dtype's values: doubles, or floats packed
+// from the start of dst (the layout the shell kernel reads).
+static void pack_values(const double* src, double* dst, int n, int dtype) {
+    double tmp[DEO_MAX_NW > DEO_MAX_BCW ? DEO_MAX_NW : DEO_MAX_BCW];
+    std::memcpy(tmp, src, sizeof(double) * n);
+    std::memset(dst, 0, sizeof(double) * n);
+    for (int k = 0; k < n; ++k) {
+        if (dtype == DEO_F64) dst[k] = tmp[k];
+        else reinterpret_cast<float*>(dst)[k] = (float)tmp[k];
+    }
+}
+
+static void shell_rows(const HostTab& H, int len, int dtype, int t, deo::ShellPlan& sp) {
+    if (t >= 3) return;
+    const RowTabDev& d = H.dev;
+    int flo = std::max(d.ilo, 2 - d.band_p0_off);
+    int fhi = std::min(d.ihi, len + 2 - d.band_nk - d.band_p0_off);
+    if (d.ilo > d.ihi || flo > fhi) { flo = 1; fhi = 0; }
+    deo::ShellTerm& S = sp.t[t];
+    S.len = len;
+    S.nlo = flo > fhi ? len : flo - 1;
+    S.nhi = flo > fhi ? 0 : len - fhi;
+    if (S.nlo > DEO_SHELL_ROWS || S.nhi > DEO_SHELL_ROWS) {
+        sp.ok = -1;
+        return;
+    }
+    auto put = [&](int slot, int i) {
+        deo::ShellRow& R = S.row[slot];
+        const bool band = i >= d.ilo && i <= d.ihi;
+        const int e = band ? 0 : (i < d.ilo ? i - 1 : (d.ilo - 1) + (i - d.ihi - 1));
+        R.p0 = band ? i + d.band_p0_off : H.p0[e];
+        R.nk = band ? d.band_nk : H.nk[e];
+        double w[DEO_MAX_NW];
+        for (int k = 0; k < DEO_MAX_NW; ++k)
+            w[k] = k >= R.nk ? 0.0 : (band ? d.wband[k] : H.W[(size_t)k * d.nexp + e]);
+        pack_values(w, R.w, DEO_MAX_NW, dtype);
+        sp.maxw = std::max(sp.maxw, R.nk);
+    };
+    for (int r = 0; r < S.nlo; ++r) put(r, r + 1);
+    for (int r = 0; r < S.nhi; ++r) put(S.nlo + r, len - S.nhi + 1 + r);
+}
+
+// The fixed-point kernel's weights: the shared band w[0..2H] as integers on
+// one exponent f (w[k] = W[k] * 2^f exactly).  Accepted only if (a) every
+// integer image fits 62 bits and the 2H+1 products with NT-tap sums (each
+// below NT * 2^(53+S)) cannot overflow a signed 128-bit accumulator, and (b)
+// ratio = NT * sum|w| / min|w| <= 256, which bounds the alignment error of the
+// kernel by ratio * 2^(1-S) <= 2 ulp of sum|c_k u_k|.
+static bool fx_weights(const double* w, int H, int nt, long long* W, int& f) {
+    const int S = nt == 3 ? 8 : 9;
+    long long M[DEO_MAX_NW];
+    int fk[DEO_MAX_NW];
+    int fmin = INT_MAX, fmax = INT_MIN;
+    double sum = 0.0, wmin = INFINITY;
+    for (int k = 0; k < 2 * H + 1; ++k) {
+        if (std::fpclassify(w[k]) != FP_NORMAL) return false;
+        int ex = 0;
+        const double fr = std::frexp(std::fabs(w[k]), &ex);  // |w| = fr * 2^ex, fr in [0.5, 1)
+        M[k] = (long long)std::ldexp(fr, 53);                  // exact 53-bit integer
+        fk[k] = ex - 53;
+        fmin = std::min(fmin, fk[k]);
+        fmax = std::max(fmax, fk[k]);
+        sum += std::fabs(w[k]);
+        wmin = std::min(wmin, std::fabs(w[k]));
+    }
+    const int bits = 53 + (fmax - fmin);
+    int lg = 0;
+    while ((1 << lg) < (2 * H + 1) * nt) ++lg;
+    if (bits > 62 || bits + 53 + S + lg > 127) return false;
+    if (nt * sum / wmin > 256.0) return false;
+    for (int k = 0; k < 2 * H + 1; ++k) W[k] = (w[k] < 0 ? -1 : 1) * (M[k] << (fk[k] - fmin));
+    f = fmin;
+    return true;
 }
 
 extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms,
@@ -837,6 +922,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             HostTab H;
             deo_status s = compile_table(A, mode, !T.has_field, v == 0 ? 1.0 : -1.0, H, rlo, rhi);
             if (s != DEO_OK) return s;
+            if (v == 0) shell_rows(H, A.len, dtype, t, P->shell);
             if ((s = upload_tab(*P, H, dtype, T.tab[v])) != DEO_OK) return s;
         }
         for (int p = 0; p < A.len + 2; ++p)
@@ -851,7 +937,20 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         for (int k = 0; k < DEO_MAX_BC; ++k) { T.al[k] = q.a_l[k]; T.ar[k] = q.a_r[k]; }
         T.bl = q.b_l;
         T.br = q.b_r;
+        if (t < 3) {
+            deo::ShellTerm& S = P->shell.t[t];
+            S.bc_kind = T.bc_kind;
+            S.periodic_nd = T.periodic_nd;
+            S.ml = T.ml;
+            S.mr = T.mr;
+            pack_values(T.al, S.al, DEO_MAX_BCW, dtype);
+            pack_values(T.ar, S.ar, DEO_MAX_BCW, dtype);
+            pack_values(&T.bl, &S.bl, 1, dtype);
+            pack_values(&T.br, &S.br, 1, dtype);
+            P->shell.maxw = std::max(P->shell.maxw, std::max(S.ml, S.mr));
+        }
     }
+    P->shell.ok = P->shell.ok >= 0 && nterms <= 3 ? 1 : 0;
     // fast path for 2-D/3-D plans whose terms all have constant interior rows
     {
         deo::UniPlan& U = P->uni;
@@ -899,6 +998,11 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
                 }
                 for (int k = 0; k < 2 * H + 1; ++k) U.ens_w[k] = U.t[0].w[k];  // weight at offset k - H
             }
+            // fixed-point evaluation: the same shared band, as exact integers on one exponent
+            U.fx = U.lap && dtype == DEO_F64 && H <= 3 && (nterms == 2 || nterms == 3);
+            for (int t = 0; t < nterms && U.fx; ++t)
+                U.fx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
+            if (U.fx) U.fx = fx_weights(U.t[0].w, H, nterms, U.fx_w, U.fx_f);
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
             U.enabled = 0;
@@ -906,6 +1010,11 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
     }
     CUDA_TRY(cudaMalloc(&P->d_plan, sizeof(PlanDev)), "cudaMalloc(plan)");
     CUDA_TRY(cudaMemcpy(P->d_plan, &P->dev, sizeof(PlanDev), cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
+    if (P->shell.ok && P->uni.enabled && P->uni.lap) {
+        CUDA_TRY(cudaMalloc(&P->d_shell, sizeof(deo::ShellPlan)), "cudaMalloc(shell rows)");
+        CUDA_TRY(cudaMemcpy(P->d_shell, &P->shell, sizeof(deo::ShellPlan), cudaMemcpyHostToDevice),
+                 "cudaMemcpy(shell rows)");
+    }
     *out = P.release();
     return DEO_OK;
 }
@@ -926,15 +1035,40 @@ static deo_status check_ptrs(const deo_plan* p, const void* a, const void* b) {
     return DEO_OK;
 }
 
+static void mark(const deo_plan* p, int k, void* stream) {
+    if (p->timing) cudaEventRecord(p->ev[k], static_cast<cudaStream_t>(stream));
+}
+
 static int launch_forward(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
+    mark(p, 0, stream);
     if (p->uni.enabled && p->fast_path) {
         if (p->uni.lap && p->use_tma) {
-            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream);
-            if (e != (int)cudaErrorNotSupported) return e;
+            const char* k = "";
+            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream, &k);
+            if (e != (int)cudaErrorNotSupported) {
+                if (e) return e;
+                mark(p, 1, stream);
+                p->last_kernel = k;
+                p->last_kernel2 = "k_shell";
+                p->ev_launches = 2;
+                const int e2 = deo_k_apply_shell(&p->uni, p->d_shell, p->shell.maxw, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+                mark(p, 2, stream);
+                return e2;
+            }
         }
-        return deo_k_apply_uniform(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+        p->last_kernel = p->uni.lap ? "k_lap" : "k_uni3";
+        p->last_kernel2 = "";
+        p->ev_launches = 1;
+        const int e = deo_k_apply_uniform(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+        mark(p, 1, stream);
+        return e;
     }
-    return deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
+    p->last_kernel = "k_apply";
+    p->last_kernel2 = "";
+    p->ev_launches = 1;
+    const int e = deo_k_apply(&p->dev, u, du, overwrite, 0, stream);
+    mark(p, 1, stream);
+    return e;
 }
 
 extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
@@ -942,7 +1076,15 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
     switch (option) {
         case DEO_OPT_FAST_PATH: p->fast_path = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_TMA: p->use_tma = value ? 1 : 0; return DEO_OK;
-        case DEO_OPT_EXACT_SUMS: p->exact_sums = (value == 2) ? 2 : (value ? 1 : 0); return DEO_OK;
+        case DEO_OPT_EXACT_SUMS:
+            if (value < 0 || value > 3) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..3", value);
+            p->exact_sums = value;
+            return DEO_OK;
+        case DEO_OPT_LAUNCH_TIMING:
+            if (value && !p->ev[0])
+                for (cudaEvent_t& e : p->ev) CUDA_TRY(cudaEventCreate(&e), "cudaEventCreate");
+            p->timing = value ? 1 : 0;
+            return DEO_OK;
     }
     return fail(DEO_ERR_BAD_ARG, "unknown plan option %d", option);
 }
@@ -952,9 +1094,25 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
     switch (option) {
         case DEO_OPT_FAST_PATH: return p->fast_path && p->uni.enabled;
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
-        case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && p->uni.ens;
+        case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
+        case DEO_OPT_LAUNCH_TIMING: return p->timing;
     }
     return -1;
+}
+
+extern "C" const char* deo_plan_kernels(const deo_plan* p, int which) {
+    if (!p) return "";
+    return which == 0 ? p->last_kernel.load() : (which == 1 ? p->last_kernel2.load() : "");
+}
+
+extern "C" deo_status deo_plan_launch_times(const deo_plan* p, float* ms, int* n) {
+    if (!p || !ms || !n) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (!p->timing || !p->ev_launches) return fail(DEO_ERR_BAD_ARG, "launch timing is off or nothing was applied");
+    const int k = p->ev_launches;
+    CUDA_TRY(cudaEventSynchronize(p->ev[k]), "cudaEventSynchronize");
+    for (int j = 0; j < k; ++j) CUDA_TRY(cudaEventElapsedTime(&ms[j], p->ev[j], p->ev[j + 1]), "cudaEventElapsedTime");
+    *n = k;
+    return DEO_OK;
 }
 
 extern "C" deo_status deo_device_status(unsigned int* status) {

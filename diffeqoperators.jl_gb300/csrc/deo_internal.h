@@ -41,6 +41,15 @@ struct FastDiv {
     uint32_t shr;
 };
 
+// Granlund-Montgomery constants for n / d with n < 2^31: l = ceil(log2 d),
+// mul = floor(2^32 (2^l - d) / d) + 1, q = (umulhi(n, mul) + n) >> l.
+inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 32 && (1ULL << l) < d) ++l;
+    const unsigned long long m = ((1ULL << 32) * ((1ULL << l) - d)) / d + 1;
+    return FastDiv{(uint32_t)m, l};
+}
+
 struct TermDev {
     int64_t stride;      // elements between neighbours along the axis
     int len;             // points along the axis
@@ -102,6 +111,36 @@ struct UniPlan {
     int pad2_;
     double ens_c0[8];             // merged centre weight for each mask of axes
     double ens_w[DEO_MAX_NW];     // band weight at offset k - H (index k)
+    // Fixed-point evaluation (Float64, one shared band of nonzero normal
+    // weights whose integer images fit the 128-bit accumulator): band weight
+    // at offset k - H = fx_w[k] * 2^fx_f exactly.
+    int fx;
+    int fx_f;
+    long long fx_w[DEO_MAX_NW];
+};
+
+// Boundary rows of the terms of a Laplacian-type plan (the rows outside each
+// term's interior range [flo, fhi]) with their weights and ghost maps; the
+// plan keeps a device copy that the boundary-shell kernel stages into shared
+// memory.  Weights (w, al, ar, bl, br) are the plan dtype's values: doubles,
+// or for Float32 plans floats packed from the start of each double array
+// (bl and br: a float in the first half of the double).
+#define DEO_SHELL_ROWS 8  // per end
+struct ShellRow {
+    int p0, nk;
+    double w[DEO_MAX_NW];
+};
+struct ShellTerm {
+    int nlo, nhi;  // rows 1..nlo and len-nhi+1..len
+    int len, bc_kind, periodic_nd, ml, mr, pad_;
+    double al[DEO_MAX_BCW], ar[DEO_MAX_BCW];
+    double bl, br;
+    ShellRow row[2 * DEO_SHELL_ROWS];  // the nlo low rows, then the nhi high rows
+};
+struct ShellPlan {
+    int ok;    // every term's boundary rows fit
+    int maxw;  // widest boundary row or ghost map over the terms
+    ShellTerm t[3];
 };
 
 // Work item of the batched persistent kernel: `count` points starting at
@@ -144,10 +183,19 @@ extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
-// TMA-fed fast path (deo_tma.cu); returns cudaErrorNotSupported when the
-// array does not meet the tensor-map alignment rules (caller falls back).
+// TMA-fed fast path (deo_tma.cu): the interior box of a Laplacian-type plan;
+// returns cudaErrorNotSupported when the array does not meet the tensor-map
+// alignment rules (caller falls back).  use_ens: 0 the reference's tap order,
+// 1 the best exact-sum kernel that applies, 2 exact sums v1, 3 exact sums v2.
+// *kernel receives the name of the kernel launched.
 extern "C" int deo_k_apply_tma(const deo::UniPlan* up, const deo::PlanDev* d_plan, int dtype, const void* u,
-                               void* du, int overwrite, int use_ens, void* stream);
+                               void* du, int overwrite, int use_ens, void* stream, const char** kernel);
+// The boundary shell around that interior box (boundary rows in the reference's
+// order); sp is the device copy of the plan's ShellPlan (maxw its widest row
+// or ghost map), or null to evaluate the boundary rows from the row tables.
+extern "C" int deo_k_apply_shell(const deo::UniPlan* up, const deo::ShellPlan* sp, int maxw,
+                                 const deo::PlanDev* d_plan, int dtype, const void* u, void* du, int overwrite,
+                                 void* stream);
 extern "C" int deo_k_read_status(unsigned int* status);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
                                  unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);

@@ -7,7 +7,10 @@
 // shared-memory ring of P slots with cp.async.bulk.tensor, each slot guarded by
 // an mbarrier; the ring keeps P - (2H+1) planes in flight ahead of the plane
 // being evaluated.  Planes outside the array arrive zero-filled (TMA OOB fill),
-// so loads need no bounds checks.  Every mbarrier wait is bounded: on timeout
+// so loads need no bounds checks.  A slot is refilled only after a barrier
+// that follows every thread's last read of it (its values are in registers by
+// then), so the copy needs no cross-proxy fence: nothing written by the
+// threads is read by the copy.  Every mbarrier wait is bounded: on timeout
 // the CTA records bit 0 of g_deo_status, waits (bounded) for its own copies
 // still in flight and returns.
 //
@@ -60,7 +63,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(m))
         : "memory");
 }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // Sum of N doubles, exact up to bits below 2^-59 of the largest, rounded
@@ -189,7 +191,6 @@ __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtenso
             const int pre = min(C::P, npl);
             for (int j = 0; j < pre; ++j) {
                 const int s = (base + j) & (C::P - 1);
-                fence_proxy_async();
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                 tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
             }
@@ -271,7 +272,6 @@ __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtenso
                 const int jn = (jc - HZ) + C::P;
                 if (jn < npl) {
                     const int s = (base + jn) & (C::P - 1);
-                    fence_proxy_async();
                     mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                     tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
                     issued = jn + 1;
@@ -389,7 +389,6 @@ __global__ void __launch_bounds__(256) k_lap_ens2(const __grid_constant__ CUtens
             const int pre = min(C::P, npl);
             for (int j = 0; j < pre; ++j) {
                 const int s = (base + j) & (C::P - 1);
-                fence_proxy_async();
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                 tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
             }
@@ -481,7 +480,6 @@ __global__ void __launch_bounds__(256) k_lap_ens2(const __grid_constant__ CUtens
                 const int jn = (jc - HZ) + C::P;
                 if (jn < npl) {
                     const int s = (base + jn) & (C::P - 1);
-                    fence_proxy_async();
                     mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                     tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
                     issued = jn + 1;
@@ -501,54 +499,619 @@ __global__ void __launch_bounds__(256) k_lap_ens2(const __grid_constant__ CUtens
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-point kernel (Float64): an interior point with no FP64 instruction.
+// Each value is decomposed once, when its plane lands, into (e, m) with
+// value = m * 2^(e - 1075 - S) and m = +-mantissa << S (S = 8 for three axes,
+// 9 for two, so that the NT taps of one offset add in int64 without
+// overflow).  For a point, the 1 + 2H*NT taps are aligned to their largest
+// exponent E by arithmetic shifts (bits below 2^(E - 1075 - S) are dropped,
+// rounding toward -inf), the NT taps of each offset are added in int64, each
+// offset's sum is multiplied by its weight's exact integer image fx_w (common
+// exponent fx_f) into a 128-bit accumulator, and the total is rounded once to
+// nearest even.  The dropped bits cost at most sum|w| * 2^(E - 1075 - S),
+// less than ratio * 2^(1 - S) ulp of sum|c_k u_k| with ratio = NT*sum|w| /
+// min|w|; the host enables the kernel only for ratio <= 256 and for weights
+// whose products cannot overflow the accumulator.  Inf/NaN inputs and results
+// that would be subnormal or overflow take the reference's tap order from
+// global memory.
+// The raw ring only receives planes (P slots); the decomposed ring (DP >= 2H+2
+// slots) holds the planes a point reads, so one barrier per plane orders the
+// decomposition before its use, and a slot is rewritten only after every
+// thread has left the points that read it.
+// ---------------------------------------------------------------------------
+template <int H>
+struct FxCfg {
+    using R = TmaCfg<double, H>;
+    static constexpr int P = 4;                                              // raw landing slots
+    static constexpr int DP = (2 * H + 2) <= 4 ? 4 : ((2 * H + 2) <= 8 ? 8 : 16);  // power of two >= 2H+2
+    static constexpr int DSLOT_M = R::PLANE * 8;                             // int64 mantissas
+    static constexpr int DSLOT = ((DSLOT_M + R::PLANE * 2 + 127) / 128) * 128;  // + int16 exponents
+    static constexpr int SMEM = P * R::SLOT + DP * DSLOT;
+};
+
+template <int S>
+__device__ __forceinline__ void decompose_fx(double v, long long& m, short& e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int ex = (int)((b >> 52) & 0x7ffULL);
+    const unsigned long long fr = b & 0xFFFFFFFFFFFFFULL;
+    const long long mag = (long long)((ex ? (fr | (1ULL << 52)) : fr) << S);
+    m = ((long long)b < 0) ? -mag : mag;
+    e = (short)(ex == 0x7ff ? 4095 : (ex ? ex : 1));  // 4095 marks Inf/NaN: forces the fallback
+}
+
+// The signed 128-bit integer (hi, lo) rounded to the nearest double, ties to
+// even, where a magnitude with lz leading zeros gets the biased exponent
+// ebase - lz.  ok = false when the result would be subnormal or overflow.
+__device__ __forceinline__ double fx_round(long long hi_s, unsigned long long lo, int ebase, bool& ok) {
+    unsigned long long hi = (unsigned long long)hi_s;
+    const bool neg = hi_s < 0;
+    if (neg) {
+        lo = 0ULL - lo;
+        hi = ~hi + (lo == 0ULL ? 1ULL : 0ULL);
+    }
+    if ((hi | lo) == 0ULL) {
+        ok = true;
+        return 0.0;
+    }
+    int lz;
+    if (hi) {
+        lz = __clzll((long long)hi);
+        if (lz) {
+            hi = (hi << lz) | (lo >> (64 - lz));
+            lo <<= lz;
+        }
+    } else {
+        lz = 64 + __clzll((long long)lo);
+        hi = lo << (lz - 64);
+        lo = 0ULL;
+    }
+    unsigned long long mant = hi >> 11;
+    const unsigned long long rb = hi & 0x7FFULL;
+    if (rb > 0x400ULL || (rb == 0x400ULL && (lo != 0ULL || (mant & 1ULL)))) ++mant;
+    int be = ebase - lz;
+    if (mant >> 53) {
+        mant >>= 1;
+        ++be;
+    }
+    if (be <= 0 || be >= 2047) {
+        ok = false;
+        return 0.0;
+    }
+    ok = true;
+    return __longlong_as_double(
+        (long long)(((unsigned long long)neg << 63) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
+}
+
+template <int H, int NT>
+__global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensorMap tmap,
+                                                const __grid_constant__ UniPlan U, const LapGrid g,
+                                                const double* __restrict__ u, double* __restrict__ du,
+                                                int overwrite) {
+    using C = TmaCfg<double, H>;
+    using F = FxCfg<H>;
+    constexpr int S = NT == 3 ? 8 : 9;
+    constexpr int HZ = NT == 3 ? H : 0;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar[F::P];
+    unsigned char* dsm = smem + F::P * C::SLOT;
+    const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
+    const int64_t sxy = (int64_t)nx * ny;
+    const int cc = (ty + H) * C::BX + tx + C::HR;
+    // result exponent: A * 2^(E - 1075 - S + fx_f) with |A| = N * 2^-lz, mantissa = N >> 75
+    const int ebase0 = 75 - S + U.fx_f;
+    if (tid == 0) {
+        for (int s = 0; s < F::P; ++s) mbar_init(&mbar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto raw = [&](int gj) -> const double* {
+        return reinterpret_cast<const double*>(smem + (gj & (F::P - 1)) * C::SLOT);
+    };
+    auto dm = [&](int gj) -> long long* {
+        return reinterpret_cast<long long*>(dsm + (gj & (F::DP - 1)) * F::DSLOT);
+    };
+    auto de = [&](int gj) -> short* {
+        return reinterpret_cast<short*>(dsm + (gj & (F::DP - 1)) * F::DSLOT + F::DSLOT_M);
+    };
+    int base = 0, issued = 0, waited = 0;
+    bool aborted = false;
+    for (int k = blockIdx.x; k < g.units && !aborted; k += gridDim.x) {
+        const int unit = (int)(((long long)k * g.perm) % g.units);
+        const int txi = unit % g.tiles_x;
+        const int rest = unit / g.tiles_x;
+        const int tyi = rest % g.tiles_y;
+        const int ci = rest / g.tiles_y;
+        const int x0 = txi * C::TX, y0 = tyi * C::TY;
+        const int x = x0 + tx, y = y0 + ty;
+        const int z0 = ci * g.zc;
+        const int z1 = min(z0 + g.zc, nz);
+        const int npl = (z1 - z0) + 2 * HZ;
+        const bool live = x < nx && y < ny && x + 1 >= U.t[0].flo && x + 1 <= U.t[0].fhi &&
+                          y + 1 >= U.t[1].flo && y + 1 <= U.t[1].fhi;
+        const int64_t col = (int64_t)y * nx + x;
+        if (tid == 0) {
+            const int pre = min(F::P, npl);
+            for (int j = 0; j < pre; ++j) {
+                const int s = (base + j) & (F::P - 1);
+                mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
+            }
+            issued = pre;
+        }
+        waited = 0;
+        for (int p = 0; p < npl; ++p) {
+            const int gj = base + p;
+            bool timeout = false;
+            {
+                const uint32_t par = (uint32_t)((gj / F::P) & 1);
+                uint32_t it = 0;
+                while (!mbar_try_wait(&mbar[gj & (F::P - 1)], par)) {
+                    if (++it > (1u << 22)) {
+                        timeout = true;
+                        break;
+                    }
+                }
+            }
+            if (!timeout) {
+                waited = p + 1;
+                const double* rp = raw(gj);
+                long long* mp = dm(gj);
+                short* ep = de(gj);
+                for (int q = tid; q < C::PLANE; q += C::TX * C::TY) decompose_fx<S>(rp[q], mp[q], ep[q]);
+            }
+            if (__syncthreads_or(timeout)) {
+                aborted = true;
+                break;
+            }
+            // every thread has decomposed plane p: its raw slot takes plane p + P
+            if (tid == 0 && p + F::P < npl) {
+                const int s = gj & (F::P - 1);
+                mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + p + F::P);
+                issued = p + F::P + 1;
+            }
+            if (p < 2 * HZ) continue;
+            const int z = z0 + p - 2 * HZ;  // the point whose last plane is p
+            const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
+            if (!(live && bz)) continue;
+            const int jg = gj - HZ;  // its centre plane
+            const long long* mc = dm(jg);
+            const short* ec = de(jg);
+            long long mt[2 * H][NT];  // [side * H + k - 1][axis]
+            int et[2 * H][NT];
+            const long long m0 = mc[cc];
+            const int e0 = ec[cc];
+#pragma unroll
+            for (int kk = 1; kk <= H; ++kk) {
+                mt[kk - 1][0] = mc[cc - kk];
+                et[kk - 1][0] = ec[cc - kk];
+                mt[H + kk - 1][0] = mc[cc + kk];
+                et[H + kk - 1][0] = ec[cc + kk];
+                mt[kk - 1][1] = mc[cc - kk * C::BX];
+                et[kk - 1][1] = ec[cc - kk * C::BX];
+                mt[H + kk - 1][1] = mc[cc + kk * C::BX];
+                et[H + kk - 1][1] = ec[cc + kk * C::BX];
+                if constexpr (NT == 3) {
+                    mt[kk - 1][2] = dm(jg - kk)[cc];
+                    et[kk - 1][2] = de(jg - kk)[cc];
+                    mt[H + kk - 1][2] = dm(jg + kk)[cc];
+                    et[H + kk - 1][2] = de(jg + kk)[cc];
+                }
+            }
+            int E = e0;
+#pragma unroll
+            for (int j = 0; j < 2 * H; ++j)
+#pragma unroll
+                for (int a = 0; a < NT; ++a) E = max(E, et[j][a]);
+            bool ok = E < 2047;
+            double total = 0.0;
+            if (ok) {
+                __int128 A = (__int128)((long long)NT * (m0 >> min(E - e0, 63))) * U.fx_w[H];
+#pragma unroll
+                for (int kk = 1; kk <= H; ++kk) {
+                    long long sm = 0, sp = 0;
+#pragma unroll
+                    for (int a = 0; a < NT; ++a) {
+                        sm += mt[kk - 1][a] >> min(E - et[kk - 1][a], 63);
+                        sp += mt[H + kk - 1][a] >> min(E - et[H + kk - 1][a], 63);
+                    }
+                    A += (__int128)sm * U.fx_w[H - kk];
+                    A += (__int128)sp * U.fx_w[H + kk];
+                }
+                total = fx_round((long long)(A >> 64), (unsigned long long)A, ebase0 + E, ok);
+            }
+            const int64_t idx = (int64_t)z * sxy + col;
+            if (!ok) {
+                // Inf/NaN or an extreme exponent: the reference's per-term tap order, from global memory
+                const int64_t st[3] = {1, (int64_t)nx, sxy};
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    double acc = 0.0;
+#pragma unroll
+                    for (int kk = 0; kk < 2 * H + 1; ++kk) acc = fma(U.t[t].w[kk], u[idx + (kk - H) * st[t]], acc);
+                    total = (t == 0) ? acc : total + acc;
+                }
+                total = zero_fix(total);
+            }
+            du[idx] = overwrite ? total : total + du[idx];
+        }
+        if (!aborted) base += npl;
+    }
+    if (aborted && tid == 0) {
+        atomicOr(&g_deo_status, 1u);
+        // wait (bounded) for this CTA's copies still in flight before its shared memory is released
+        for (int j = waited; j < issued; ++j) {
+            const int gj = base + j;
+            const uint32_t par = (uint32_t)((gj / F::P) & 1);
+            for (uint32_t it = 0; it < (1u << 22); ++it)
+                if (mbar_try_wait(&mbar[gj & (F::P - 1)], par)) break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reference-order kernel with a register queue (Float32 and Float64).
+// CTA = 32 x 8 threads over a 32 x 32 tile; each thread owns RY = 4
+// consecutive rows of one column.  Planes stream through a TMA ring as in
+// k_lap_tma.  Each thread keeps its rows' values at z-H..z+H in registers
+// (one shared-memory load per row and plane), reads the y-neighbours beyond
+// its own rows (2H loads) and the x-neighbours (2H per row) from the centre
+// plane, and evaluates each term's taps in the reference's order, bit for bit
+// the generic evaluator.  One barrier per plane releases the centre plane's
+// slot, which then takes the plane P further on.
+// ---------------------------------------------------------------------------
+template <typename T, int H>
+struct QCfg {
+    static constexpr int TX = 32, TYT = 8, RY = 4, TY = TYT * RY;  // threads in x, threads in y, rows per thread
+    static constexpr int ES = (int)sizeof(T);
+    static constexpr int HR = ((H * ES + 15) / 16) * 16 / ES;       // x halo rounded up to 16 bytes
+    static constexpr int BX = TX + 2 * HR, BY = TY + 2 * H;
+    static constexpr int PLANE = BX * BY;
+    static constexpr int PLANE_BYTES = PLANE * ES;
+    static constexpr int SLOT = ((PLANE_BYTES + 127) / 128) * 128;
+    static constexpr int P = 8;  // ring slots (>= H + 2)
+    static constexpr int SMEM = P * SLOT;
+};
+
+template <typename T, int H, int NT>
+__global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorMap tmap,
+                                               const __grid_constant__ UniPlan U, const LapGrid g,
+                                               T* __restrict__ du, int overwrite) {
+    using C = QCfg<T, H>;
+    constexpr int HZ = NT == 3 ? H : 0;
+    constexpr int RY = C::RY;
+    constexpr int K = 2 * H + 1;
+    static_assert(C::P >= H + 2, "ring too short");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t mbar[C::P];
+    const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
+    const int64_t sxy = (int64_t)nx * ny;
+    const int c0 = (ty * RY + H) * C::BX + tx + C::HR;  // the first own row's point inside a slot
+    T w[NT][K];
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+#pragma unroll
+        for (int k = 0; k < K; ++k) w[t][k] = uni_w<T>(U.t[t], k);
+    if (tid == 0) {
+        for (int s = 0; s < C::P; ++s) mbar_init(&mbar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto slot = [&](int gj) -> const T* {
+        return reinterpret_cast<const T*>(smem + (gj & (C::P - 1)) * C::SLOT);
+    };
+    int base = 0, issued = 0, waited = 0;
+    bool aborted = false;
+    for (int kk = blockIdx.x; kk < g.units && !aborted; kk += gridDim.x) {
+        const int unit = (int)(((long long)kk * g.perm) % g.units);
+        const int txi = unit % g.tiles_x;
+        const int rest = unit / g.tiles_x;
+        const int tyi = rest % g.tiles_y;
+        const int ci = rest / g.tiles_y;
+        const int x0 = txi * C::TX, y0 = tyi * C::TY;
+        const int x = x0 + tx, yr = y0 + ty * RY;
+        const int z0 = ci * g.zc;
+        const int z1 = min(z0 + g.zc, nz);
+        const int npl = (z1 - z0) + 2 * HZ;
+        const bool bx = x < nx && x + 1 >= U.t[0].flo && x + 1 <= U.t[0].fhi;
+        if (tid == 0) {
+            const int pre = min(C::P, npl);
+            for (int j = 0; j < pre; ++j) {
+                const int s = (base + j) & (C::P - 1);
+                mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
+            }
+            issued = pre;
+        }
+        waited = 0;
+        T q[RY][2 * HZ + 1];  // own rows at z - HZ .. z + HZ
+        for (int p = 0; p < npl; ++p) {
+            const int gj = base + p;
+            bool timeout = false;
+            {
+                const uint32_t par = (uint32_t)((gj / C::P) & 1);
+                uint32_t it = 0;
+                while (!mbar_try_wait(&mbar[gj & (C::P - 1)], par)) {
+                    if (++it > (1u << 22)) {
+                        timeout = true;
+                        break;
+                    }
+                }
+            }
+            if (!timeout) {
+                waited = p + 1;
+                const T* pn = slot(gj);
+#pragma unroll
+                for (int j = 0; j < RY; ++j) {
+#pragma unroll
+                    for (int o = 0; o < 2 * HZ; ++o) q[j][o] = q[j][o + 1];
+                    q[j][2 * HZ] = pn[c0 + j * C::BX];
+                }
+                const int z = z0 + p - 2 * HZ;  // the point whose last plane is p
+                const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
+                if (p >= 2 * HZ && bx && bz) {
+                    const T* pc = slot(gj - HZ);  // its centre plane
+                    T col[RY + 2 * H];            // this column at rows yr - H .. yr + RY - 1 + H
+#pragma unroll
+                    for (int m = 0; m < H; ++m) {
+                        col[m] = pc[c0 + (m - H) * C::BX];
+                        col[RY + H + m] = pc[c0 + (RY + m) * C::BX];
+                    }
+#pragma unroll
+                    for (int j = 0; j < RY; ++j) col[H + j] = q[j][HZ];
+#pragma unroll
+                    for (int j = 0; j < RY; ++j) {
+                        const int y = yr + j;
+                        if (y < ny && y + 1 >= U.t[1].flo && y + 1 <= U.t[1].fhi) {
+                            const int cc = c0 + j * C::BX;
+                            T ax = T(0), ay = T(0);
+#pragma unroll
+                            for (int k = 0; k < K; ++k) ax = fma(w[0][k], k == H ? col[H + j] : pc[cc + k - H], ax);
+#pragma unroll
+                            for (int k = 0; k < K; ++k) ay = fma(w[1][k], col[j + k], ay);
+                            T tot = ax + ay;
+                            if constexpr (NT == 3) {
+                                T az = T(0);
+#pragma unroll
+                                for (int k = 0; k < K; ++k) az = fma(w[2][k], q[j][k], az);
+                                tot = tot + az;
+                            }
+                            tot = zero_fix(tot);
+                            const int64_t idx = (int64_t)z * sxy + (int64_t)y * nx + x;
+                            du[idx] = overwrite ? tot : tot + du[idx];
+                        }
+                    }
+                }
+            }
+            if (__syncthreads_or(timeout)) {
+                aborted = true;
+                break;
+            }
+            // every thread is done with plane p - HZ: its slot takes plane p - HZ + P
+            if (tid == 0 && p >= HZ && p - HZ + C::P < npl) {
+                const int jn = p - HZ + C::P;
+                const int s = (base + jn) & (C::P - 1);
+                mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
+                issued = jn + 1;
+            }
+        }
+        if (!aborted) base += npl;
+    }
+    if (aborted && tid == 0) {
+        atomicOr(&g_deo_status, 1u);
+        // wait (bounded) for this CTA's copies still in flight before its shared memory is released
+        for (int j = waited; j < issued; ++j) {
+            const int gj = base + j;
+            const uint32_t par = (uint32_t)((gj / C::P) & 1);
+            for (uint32_t it = 0; it < (1u << 22); ++it)
+                if (mbar_try_wait(&mbar[gj & (C::P - 1)], par)) break;
+        }
+    }
+}
+
 // The boundary shell of a Laplacian-type plan: every point with a non-band
 // row along some axis (it reads a ghost or uses a boundary stencil).  The
 // tiled kernels compute the interior box [flo, fhi]^NT; this kernel computes
-// the rest with the generic row-table evaluator (the reference's order).
-// Index space: z outside the box (full planes), then z inside & y outside
-// (full rows), then z, y inside & x outside.
+// the rest in the reference's order (the generic evaluator's arithmetic, tap
+// for tap): along an axis where the point's row is an interior row, the
+// band's taps; along the others, the boundary row's taps with the ghost
+// values of the boundary condition.  With ROWS the boundary rows, weights and
+// ghost maps are staged once per CTA from the plan's ShellPlan into shared
+// memory and every load of a point is independent of the others; without it,
+// they come from the plan's row tables (the generic evaluator itself).
+// Index space, ordered so that the 32 points of a warp share their boundary
+// row: z outside the box (full planes, x fastest), then z inside & y outside
+// (full rows, x fastest), then z, y inside & x outside (y fastest).  The grid
+// strides over it.
 struct ShellBox {
     int lo[3], hi[3];      // interior box, 0-based inclusive (empty if lo > hi)
     int64_t n[3];
     int64_t cz, cy, cx;    // points in each part
+    int small;             // cz + cy + cx < 2^31: index arithmetic by the FastDiv constants below
+    FastDiv d_nxny, d_nx, d_nyonx, d_niy, d_nxo;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_shell(const __grid_constant__ ShellBox B, const PlanDev* __restrict__ P,
-                                               const T* __restrict__ u, T* __restrict__ du, int overwrite) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Coordinates of shell point t (see the index-space order above).
+__device__ __forceinline__ void shell_coords(const ShellBox& B, int64_t t, int64_t& x, int64_t& y, int64_t& z) {
     const int64_t nx = B.n[0], ny = B.n[1];
-    int64_t x, y, z;
+    const int64_t nyo = ny - (B.hi[1] - B.lo[1] + 1);
+    const int64_t nxo = nx - (B.hi[0] - B.lo[0] + 1);
+    const int64_t niy = B.hi[1] - B.lo[1] + 1;
     if (t < B.cz) {
-        const int64_t nzo = B.n[2] - (B.hi[2] - B.lo[2] + 1);  // planes outside
-        const int64_t pl = t / (nx * ny), r = t - pl * nx * ny;
-        const int64_t below = B.lo[2];
-        z = pl < below ? pl : pl - below + B.hi[2] + 1;
-        (void)nzo;
-        y = r / nx;
+        int64_t pl, r;
+        if (B.small) {
+            pl = fast_div((uint32_t)t, B.d_nxny);
+            r = t - pl * nx * ny;
+            y = fast_div((uint32_t)r, B.d_nx);
+        } else {
+            pl = t / (nx * ny);
+            r = t - pl * nx * ny;
+            y = r / nx;
+        }
         x = r - y * nx;
+        z = pl < B.lo[2] ? pl : pl - B.lo[2] + B.hi[2] + 1;
     } else if (t < B.cz + B.cy) {
         const int64_t q = t - B.cz;
-        const int64_t nyo = ny - (B.hi[1] - B.lo[1] + 1);
-        const int64_t pl = q / (nyo * nx), r = q - pl * nyo * nx;
+        int64_t pl, r, row;
+        if (B.small) {
+            pl = fast_div((uint32_t)q, B.d_nyonx);
+            r = q - pl * nyo * nx;
+            row = fast_div((uint32_t)r, B.d_nx);
+        } else {
+            pl = q / (nyo * nx);
+            r = q - pl * nyo * nx;
+            row = r / nx;
+        }
         z = B.lo[2] + pl;
-        const int64_t row = r / nx;
         x = r - row * nx;
         y = row < B.lo[1] ? row : row - B.lo[1] + B.hi[1] + 1;
-    } else if (t < B.cz + B.cy + B.cx) {
-        const int64_t q = t - B.cz - B.cy;
-        const int64_t nxo = nx - (B.hi[0] - B.lo[0] + 1);
-        const int64_t line = q / nxo, c = q - line * nxo;
-        const int64_t niy = B.hi[1] - B.lo[1] + 1;
-        z = B.lo[2] + line / niy;
-        y = B.lo[1] + line % niy;
-        x = c < B.lo[0] ? c : c - B.lo[0] + B.hi[0] + 1;
     } else {
-        return;
+        const int64_t q = t - B.cz - B.cy;
+        int64_t line, zz;
+        if (B.small) {
+            line = fast_div((uint32_t)q, B.d_niy);  // (z, x column) pairs, y fastest
+            zz = fast_div((uint32_t)line, B.d_nxo);
+        } else {
+            line = q / niy;
+            zz = line / nxo;
+        }
+        y = B.lo[1] + (q - line * niy);
+        z = B.lo[2] + zz;
+        const int64_t c = line - zz * nxo;
+        x = c < B.lo[0] ? c : c - B.lo[0] + B.hi[0] + 1;
     }
-    const int64_t idx = (z * ny + y) * nx + x;
-    const T r = eval_point<T, false>(*P, u, idx);
-    du[idx] = overwrite ? r : r + du[idx];
+}
+
+// Element k of a packed weight array (doubles, or floats packed from the start).
+template <typename T>
+__device__ __forceinline__ T sw(const double* a, int k);
+template <>
+__device__ __forceinline__ double sw<double>(const double* a, int k) {
+    return a[k];
+}
+template <>
+__device__ __forceinline__ float sw<float>(const double* a, int k) {
+    return reinterpret_cast<const float*>(a)[k];
+}
+
+// Ghost values, as ghost_left / ghost_right (same arithmetic), W >= ml, mr.
+template <typename T, int W>
+__device__ __forceinline__ T shell_ghost(const ShellTerm& S, const T* __restrict__ line, int64_t s, bool left) {
+    if (S.bc_kind == 1)
+        return (S.periodic_nd == left) ? __ldg(line) : __ldg(line + (int64_t)(S.len - 1) * s);
+    const int m = left ? S.ml : S.mr;
+    const int64_t o = left ? 0 : (int64_t)(S.len - S.mr);
+    const double* a = left ? S.al : S.ar;
+    T v[W];
+#pragma unroll
+    for (int j = 0; j < W; ++j) v[j] = j < m ? __ldg(line + (o + j) * s) : T(0);
+    T d = T(0);
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+        if (j < m) d = (j == 0) ? sw<T>(a, 0) * v[0] : fma(sw<T>(a, j), v[j], d);
+    return d + sw<T>(left ? &S.bl : &S.br, 0);
+}
+
+// Boundary row i (1-based) of a term on the line starting at `line`, as
+// eval_term (same taps, same order); W >= the row's taps.
+template <typename T, int W>
+__device__ __forceinline__ T shell_row(const ShellTerm& S, const T* __restrict__ line, int64_t s, int i) {
+    const int r = i <= S.nlo ? i - 1 : S.nlo + (i - (S.len - S.nhi + 1));
+    const ShellRow& R = S.row[r];
+    const int L2 = S.len + 2;
+    const int p0 = R.p0, nk = R.nk;
+    const T gl = p0 == 1 ? shell_ghost<T, W>(S, line, s, true) : T(0);
+    const T gr = p0 + nk - 1 == L2 ? shell_ghost<T, W>(S, line, s, false) : T(0);
+    T x[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        const int p = p0 + k;
+        x[k] = (k >= nk || p == 1 || p == L2) ? T(0) : __ldg(line + (int64_t)(p - 2) * s);
+    }
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+        if (k < nk) {
+            const int p = p0 + k;
+            acc = fma(sw<T>(R.w, k), p == 1 ? gl : (p == L2 ? gr : x[k]), acc);
+        }
+    }
+    return acc;
+}
+
+// Band taps of axis a at idx (interior row along a), as eval_term's band path.
+template <typename T, int H>
+__device__ __forceinline__ T shell_band(const UniTerm& ut, const T* __restrict__ u, int64_t idx, int64_t s) {
+    T r = T(0);
+#pragma unroll
+    for (int k = 0; k < 2 * H + 1; ++k) r = fma(uni_w<T>(ut, k), __ldg(u + idx + (k - H) * s), r);
+    return r;
+}
+
+template <typename T, int H, int NT, int W>
+__global__ void __launch_bounds__(256) k_shell(const __grid_constant__ ShellBox B, const __grid_constant__ UniPlan U,
+                                               const ShellPlan* __restrict__ SPg, const T* __restrict__ u,
+                                               T* __restrict__ du, int overwrite) {
+    static_assert(sizeof(ShellTerm) % 8 == 0, "ShellTerm copied in 8-byte words");
+    __shared__ __align__(16) ShellTerm S[NT];
+    {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(SPg->t);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(S);
+        for (int q = threadIdx.x; q < (int)(NT * sizeof(ShellTerm) / 8); q += blockDim.x) dst[q] = __ldg(src + q);
+        __syncthreads();
+    }
+    const int64_t nx = B.n[0], ny = B.n[1];
+    const int64_t total = B.cz + B.cy + B.cx;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t x, y, z;
+        shell_coords(B, t, x, y, z);
+        const int64_t idx = (z * ny + y) * nx + x;
+        const int64_t crd[3] = {x, y, z};
+        const int64_t st[3] = {1, nx, nx * ny};
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a < NT; ++a) {
+            const int i = (int)crd[a] + 1;
+            const T r = (i >= U.t[a].flo && i <= U.t[a].fhi)
+                            ? shell_band<T, H>(U.t[a], u, idx, st[a])
+                            : shell_row<T, W>(S[a], u + idx - crd[a] * st[a], st[a], i);
+            acc = (a == 0) ? r : acc + r;
+        }
+        const T tot = zero_fix(acc);
+        du[idx] = overwrite ? tot : tot + du[idx];
+    }
+}
+
+// The same shell with the boundary rows from the plan's row tables (plans
+// whose boundary rows do not fit a ShellPlan).
+template <typename T, int H, int NT>
+__global__ void __launch_bounds__(256) k_shell_generic(const __grid_constant__ ShellBox B,
+                                                       const __grid_constant__ UniPlan U,
+                                                       const PlanDev* __restrict__ P, const T* __restrict__ u,
+                                                       T* __restrict__ du, int overwrite) {
+    const int64_t nx = B.n[0], ny = B.n[1];
+    const int64_t total = B.cz + B.cy + B.cx;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t x, y, z;
+        shell_coords(B, t, x, y, z);
+        const int64_t idx = (z * ny + y) * nx + x;
+        const int64_t crd[3] = {x, y, z};
+        const int64_t st[3] = {1, nx, nx * ny};
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a < NT; ++a) {
+            const int i = (int)crd[a] + 1;
+            const T r = (i >= U.t[a].flo && i <= U.t[a].fhi) ? shell_band<T, H>(U.t[a], u, idx, st[a])
+                                                             : eval_term<T>(P->t[a], u, idx, i);
+            acc = (a == 0) ? r : acc + r;
+        }
+        const T tot = zero_fix(acc);
+        du[idx] = overwrite ? tot : tot + du[idx];
+    }
 }
 
 }  // namespace deo
@@ -671,6 +1234,43 @@ static int launch_ens2(const UniPlan* up, const PlanDev* dp, const void* u, void
     return (int)cudaGetLastError();
 }
 
+template <typename T, int H, int NT>
+static int launch_q(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+    using C = QCfg<T, H>;
+    CUtensorMap map;
+    if (!make_map(map, u, C::ES, up->n[0], up->n[1], up->n[2], C::BX, C::BY)) return (int)cudaErrorNotSupported;
+    static int64_t G = 0;
+    if (!G) {
+        const int e = occupancy_grid(k_lap_q<T, H, NT>, C::TX * C::TYT, C::SMEM, G);
+        if (e) return e;
+    }
+    const LapGrid g = make_grid(up, C::TX, C::TY, H, NT, G);
+    const int grid = (int)std::min<int64_t>(G, g.units);
+    k_lap_q<T, H, NT><<<grid, dim3(C::TX, C::TYT), C::SMEM, st>>>(map, *up, g, (T*)du, ow);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+static int launch_q_h(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+    const int H = up->radius;
+    if (up->nterms == 3) {
+        switch (H) {
+            case 1: return launch_q<T, 1, 3>(up, u, du, ow, st);
+            case 2: return launch_q<T, 2, 3>(up, u, du, ow, st);
+            case 3: return launch_q<T, 3, 3>(up, u, du, ow, st);
+            case 4: return launch_q<T, 4, 3>(up, u, du, ow, st);
+        }
+    } else if (up->nterms == 2) {
+        switch (H) {
+            case 1: return launch_q<T, 1, 2>(up, u, du, ow, st);
+            case 2: return launch_q<T, 2, 2>(up, u, du, ow, st);
+            case 3: return launch_q<T, 3, 2>(up, u, du, ow, st);
+            case 4: return launch_q<T, 4, 2>(up, u, du, ow, st);
+        }
+    }
+    return (int)cudaErrorNotSupported;
+}
+
 template <typename T, bool ENS>
 static int launch_tma_h(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st) {
     const int H = up->radius;
@@ -692,9 +1292,35 @@ static int launch_tma_h(const UniPlan* up, const PlanDev* dp, const void* u, voi
     return (int)cudaErrorNotSupported;
 }
 
-template <typename T>
-static int launch_shell(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st) {
-    ShellBox B;
+template <int H, int NT>
+static int launch_fx(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+    using C = TmaCfg<double, H>;
+    using F = FxCfg<H>;
+    CUtensorMap map;
+    if (!make_map(map, u, 8, up->n[0], up->n[1], up->n[2], C::BX, C::BY)) return (int)cudaErrorNotSupported;
+    static int64_t G = 0;
+    if (!G) {
+        const int e = occupancy_grid(k_lap_fx<H, NT>, C::TX * C::TY, F::SMEM, G);
+        if (e) return e;
+    }
+    const LapGrid g = make_grid(up, C::TX, C::TY, H, NT, G);
+    const int grid = (int)std::min<int64_t>(G, g.units);
+    k_lap_fx<H, NT><<<grid, dim3(C::TX, C::TY), F::SMEM, st>>>(map, *up, g, (const double*)u, (double*)du, ow);
+    return (int)cudaGetLastError();
+}
+
+template <typename K>
+static int64_t shell_grid(K kernel, int64_t total) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0);
+    if (per_sm < 1) per_sm = 1;
+    return std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)deo_k_num_sms() * per_sm));
+}
+
+template <typename T, int H, int NT>
+static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, const void* u, void* du,
+                          int ow, cudaStream_t st) {
+    ShellBox B{};
     for (int k = 0; k < 3; ++k) {
         B.n[k] = up->n[k];
         if (k < up->nterms) {
@@ -716,40 +1342,103 @@ static int launch_shell(const UniPlan* up, const PlanDev* dp, const void* u, voi
     B.cx = iz * iy * (nx - ix);
     const int64_t total = B.cz + B.cy + B.cx;
     if (total == 0) return 0;
-    const int64_t blocks = (total + 255) / 256;
-    k_shell<T><<<(unsigned)blocks, 256, 0, st>>>(B, dp, (const T*)u, (T*)du, ow);
+    B.small = total < (1LL << 31) && nx * ny < (1LL << 31);
+    if (B.small) {
+        auto fd = [](int64_t d) { return make_fastdiv((uint32_t)std::max<int64_t>(d, 1)); };
+        B.d_nxny = fd(nx * ny);
+        B.d_nx = fd(nx);
+        B.d_nyonx = fd((ny - iy) * nx);
+        B.d_niy = fd(iy);
+        B.d_nxo = fd(nx - ix);
+    }
+    if (sp && maxw <= 8) {
+        static int64_t g = 0;
+        if (!g) g = shell_grid(k_shell<T, H, NT, 8>, 1LL << 40);
+        k_shell<T, H, NT, 8><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, sp, (const T*)u,
+                                                                                       (T*)du, ow);
+    } else if (sp) {
+        static int64_t g = 0;
+        if (!g) g = shell_grid(k_shell<T, H, NT, 16>, 1LL << 40);
+        k_shell<T, H, NT, 16><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, sp, (const T*)u,
+                                                                                        (T*)du, ow);
+    } else {
+        static int64_t g = 0;
+        if (!g) g = shell_grid(k_shell_generic<T, H, NT>, 1LL << 40);
+        k_shell_generic<T, H, NT><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, dp, (const T*)u,
+                                                                                          (T*)du, ow);
+    }
     return (int)cudaGetLastError();
 }
 
-static int launch_tma_any(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du, int overwrite,
-                          int use_ens, cudaStream_t st);
-
-extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du,
-                               int overwrite, int use_ens, void* stream) {
-    if (!up->lap) return (int)cudaErrorNotSupported;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int e = launch_tma_any(up, dp, dtype, u, du, overwrite, use_ens, st);
-    if (e) return e;
-    return dtype == 0 ? launch_shell<double>(up, dp, u, du, overwrite, st)
-                      : launch_shell<float>(up, dp, u, du, overwrite, st);
+template <typename T>
+static int launch_shell(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, const void* u, void* du,
+                        int ow, cudaStream_t st) {
+    const int H = up->radius;
+    if (up->nterms == 3) {
+        switch (H) {
+            case 1: return launch_shell_t<T, 1, 3>(up, sp, maxw, dp, u, du, ow, st);
+            case 2: return launch_shell_t<T, 2, 3>(up, sp, maxw, dp, u, du, ow, st);
+            case 3: return launch_shell_t<T, 3, 3>(up, sp, maxw, dp, u, du, ow, st);
+            case 4: return launch_shell_t<T, 4, 3>(up, sp, maxw, dp, u, du, ow, st);
+        }
+    } else if (up->nterms == 2) {
+        switch (H) {
+            case 1: return launch_shell_t<T, 1, 2>(up, sp, maxw, dp, u, du, ow, st);
+            case 2: return launch_shell_t<T, 2, 2>(up, sp, maxw, dp, u, du, ow, st);
+            case 3: return launch_shell_t<T, 3, 2>(up, sp, maxw, dp, u, du, ow, st);
+            case 4: return launch_shell_t<T, 4, 2>(up, sp, maxw, dp, u, du, ow, st);
+        }
+    }
+    return (int)cudaErrorNotSupported;
 }
 
-static int launch_tma_any(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du, int overwrite,
-                          int use_ens, cudaStream_t st) {
-    if (dtype == 0 && use_ens && up->ens && use_ens != 2) {
-        int e = (int)cudaErrorNotSupported;
-        if (up->nterms == 3 && up->radius == 1) e = launch_ens2<1, 3>(up, dp, u, du, overwrite, st);
-        if (up->nterms == 3 && up->radius == 2) e = launch_ens2<2, 3>(up, dp, u, du, overwrite, st);
-        if (up->nterms == 3 && up->radius == 3) e = launch_ens2<3, 3>(up, dp, u, du, overwrite, st);
-        if (up->nterms == 2 && up->radius == 1) e = launch_ens2<1, 2>(up, dp, u, du, overwrite, st);
-        if (up->nterms == 2 && up->radius == 2) e = launch_ens2<2, 2>(up, dp, u, du, overwrite, st);
-        if (up->nterms == 2 && up->radius == 3) e = launch_ens2<3, 2>(up, dp, u, du, overwrite, st);
-        if (e != (int)cudaErrorNotSupported) return e;
+#define DEO_TRY_KERNEL(call, name)                            \
+    do {                                                      \
+        const int e_ = (call);                                \
+        if (e_ != (int)cudaErrorNotSupported) {               \
+            if (!e_) *kernel = (name);                        \
+            return e_;                                        \
+        }                                                     \
+    } while (0)
+
+extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du,
+                               int overwrite, int use_ens, void* stream, const char** kernel) {
+    static const char* none = "";
+    if (!kernel) kernel = &none;
+    if (!up->lap || up->nterms < 2 || up->nterms > 3) return (int)cudaErrorNotSupported;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int H = up->radius, NT = up->nterms;
+    if (dtype == 0 && use_ens == 1 && up->fx) {
+        if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 3>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 3>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 3>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 2>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 2>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 2>(up, u, du, overwrite, st)), "k_lap_fx");
     }
-    if (dtype == 0)
-        return (use_ens && up->ens) ? launch_tma_h<double, true>(up, dp, u, du, overwrite, st)
-                                    : launch_tma_h<double, false>(up, dp, u, du, overwrite, st);
-    return launch_tma_h<float, false>(up, dp, u, du, overwrite, st);
+    if (dtype == 0 && (use_ens == 1 || use_ens == 3) && up->ens) {
+        if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_ens2<1, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+        if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_ens2<2, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+        if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_ens2<3, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+        if (NT == 2 && H == 1) DEO_TRY_KERNEL((launch_ens2<1, 2>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+        if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_ens2<2, 2>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+        if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_ens2<3, 2>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
+    }
+    if (dtype == 0) {
+        if (use_ens && up->ens)
+            DEO_TRY_KERNEL((launch_tma_h<double, true>(up, dp, u, du, overwrite, st)), "k_lap_tma(exact sums v1)");
+        DEO_TRY_KERNEL((launch_q_h<double>(up, u, du, overwrite, st)), "k_lap_q");
+    } else {
+        DEO_TRY_KERNEL((launch_q_h<float>(up, u, du, overwrite, st)), "k_lap_q");
+    }
+    return (int)cudaErrorNotSupported;
+}
+
+extern "C" int deo_k_apply_shell(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, int dtype,
+                                 const void* u, void* du, int overwrite, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return dtype == 0 ? launch_shell<double>(up, sp, maxw, dp, u, du, overwrite, st)
+                      : launch_shell<float>(up, sp, maxw, dp, u, du, overwrite, st);
 }
 
 extern "C" int deo_k_read_status(unsigned int* status) {

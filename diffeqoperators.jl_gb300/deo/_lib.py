@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "OK", 1: "BAD_SHAPE", 2: "BAD_ARG", 3: "UNSUPPORTED", 4: "CUD
 DEO_F64, DEO_F32 = 0, 1
 DEO_BC_AFFINE, DEO_BC_PERIODIC = 0, 1
 DEO_PATH_AUTO, DEO_PATH_PADDED, DEO_PATH_GENERIC = 0, 1, 2
-DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS = 1, 2, 3
+DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS, DEO_OPT_LAUNCH_TIMING = 1, 2, 3, 4
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)
@@ -111,6 +111,8 @@ def lib():
     proto("deo_plan_table_bytes", C.c_size_t, _vp)
     proto("deo_plan_set_option", st, _vp, C.c_int, C.c_int)
     proto("deo_plan_get_option", C.c_int, _vp, C.c_int)
+    proto("deo_plan_kernels", C.c_char_p, _vp, C.c_int)
+    proto("deo_plan_launch_times", C.c_int, _vp, C.POINTER(C.c_float), C.POINTER(C.c_int))
     proto("deo_device_status", st, C.POINTER(C.c_uint))
     proto("deo_apply", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_apply_host", st, _vp, _vp, _vp, _vp)
@@ -147,7 +149,7 @@ EXPORTED = [
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
     "deo_operator_destroy", "deo_operator_array", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
-    "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
+    "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune",
 ]

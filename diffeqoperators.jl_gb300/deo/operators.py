@@ -630,6 +630,20 @@ class Plan:
     def uses_exact_sums(self) -> bool:
         return self.get_option(L.DEO_OPT_EXACT_SUMS)
 
+    @property
+    def kernels(self) -> tuple:
+        """Names of the kernels the last forward apply launched."""
+        lib = L.lib()
+        return tuple(k.decode() for k in (lib.deo_plan_kernels(self._h, 0), lib.deo_plan_kernels(self._h, 1)) if k)
+
+    def launch_times(self) -> list:
+        """Device ms of each launch of the last forward apply (needs
+        set_option(DEO_OPT_LAUNCH_TIMING, 1) before that apply)."""
+        ms = (C.c_float * 2)()
+        n = C.c_int()
+        check(L.lib().deo_plan_launch_times(self._h, ms, C.byref(n)))
+        return [float(ms[i]) for i in range(n.value)]
+
     def _check(self, u, du):
         if tuple(u.shape) != self.shape or tuple(du.shape) != self.shape:
             raise DeoShapeError(1, f"plan is for size {self.shape}; got {tuple(u.shape)} -> {tuple(du.shape)}")

@@ -174,20 +174,35 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *   DEO_OPT_TMA: Laplacian-type plans (term t a centred band on axis t) stream
  *     planes with TMA into a shared-memory ring; 0 uses the register-queue kernel.
  *   DEO_OPT_EXACT_SUMS: Float64 Laplacian-type plans whose terms share one
- *     band sum the equal-weight neighbours (one per axis at each offset)
- *     exactly in integer arithmetic and round once (2H+1 FP64 instructions per
- *     point instead of NT*(2H+1)+NT-1; result within a few ulp of
- *     sum|c_k u_k| of the reference's order).  0 keeps the reference's
- *     per-term tap order, bit-identical to the generic kernel.  Value 2 selects
- *     the earlier exact-sum kernel that decomposes values at every use (for
- *     comparison). 
+ *     band evaluate interior points in integer arithmetic and round once
+ *     (result within a few ulp of sum|c_k u_k| of the reference's order):
+ *       1 the best variant that applies (default): the fixed-point kernel
+ *         (no FP64 instruction per point) when the band's weights allow it,
+ *         else variant 3;
+ *       2 exact sums of the equal-weight neighbours, decomposing values at
+ *         every use (kept for comparison);
+ *       3 the same sums from values decomposed once per plane, one int64 ->
+ *         double conversion and one FMA per offset;
+ *       0 the reference's per-term tap order, bit-identical to the generic
+ *         kernel.
+ *   DEO_OPT_LAUNCH_TIMING: 1 records CUDA events around every kernel launch
+ *     of each forward apply (read with deo_plan_launch_times); default 0.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
 #define DEO_OPT_EXACT_SUMS 3
+#define DEO_OPT_LAUNCH_TIMING 4
 deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);
+/* Name of the kernel the last forward apply launched first (which = 0) and
+ * second (which = 1; "" if it launched one), e.g. "k_lap_fx" and "k_shell".
+ * Static strings; "" before the first apply.  No reference counterpart. */
+const char* deo_plan_kernels(const deo_plan* plan, int which);
+/* Device time in ms of each launch of the last forward apply (DEO_OPT_LAUNCH_TIMING
+ * must be on); ms needs room for 2 entries, *n receives the count.  Waits for
+ * that apply to finish.  No reference counterpart. */
+deo_status deo_plan_launch_times(const deo_plan* plan, float* ms, int* n);
 /* Device-side error flags raised since the last call (bit 0: a bounded wait
  * in a kernel gave up; the kernel returned without finishing).  Synchronises.
  * Returns DEO_ERR_TIMEOUT if any flag was set. */

@@ -117,8 +117,8 @@ def test_fast_path_bitwise_equals_generic(cuda, case):
     tol = 4 * np.spacing(O.abs_scale(oterms, u))
     outs = {}
     # (fast path, TMA ring, exact neighbour sums)
-    for name, opts in {"tma-ens": (1, 1, 1), "tma-ens-v1": (1, 1, 2), "tma-fma": (1, 1, 0), "queue": (1, 0, 0),
-                       "generic": (0, 0, 0)}.items():
+    for name, opts in {"tma-ens": (1, 1, 1), "tma-ens-v2": (1, 1, 3), "tma-ens-v1": (1, 1, 2), "tma-fma": (1, 1, 0),
+                       "queue": (1, 0, 0), "generic": (0, 0, 0)}.items():
         p.set_option(deo.DEO_OPT_FAST_PATH, opts[0])
         p.set_option(deo.DEO_OPT_TMA, opts[1])
         p.set_option(deo.DEO_OPT_EXACT_SUMS, opts[2])
@@ -263,11 +263,13 @@ def test_full_size_laplacian_against_oracle(cuda, dtype):
     ud = deo.julia_array((n, n, n), tdt)
     ud.copy_(torch.from_numpy(u).to(tdt))
     report = {}
-    modes = {"exact-sums": 1, "exact-sums-v1": 2, "reference-order": 0} if dtype == "f64" else {"default": 1}
+    modes = ({"exact-sums": 1, "exact-sums-v2": 3, "exact-sums-v1": 2, "reference-order": 0} if dtype == "f64"
+             else {"default": 1})
     for name, ens in modes.items():
         plan.set_option(deo.DEO_OPT_EXACT_SUMS, ens)
         du = deo.julia_array((n, n, n), tdt)
         plan.apply(ud, du)
+        report.setdefault("kernels", {})[name] = list(plan.kernels)
         got = du.to(torch.float64).cpu().numpy()
         ulps = np.abs(got - ref) / np.spacing(scale)
         report[name] = {"max_ulp_of_scale": float(ulps.max()), "mean_ulp_of_scale": float(ulps.mean()),
@@ -276,9 +278,112 @@ def test_full_size_laplacian_against_oracle(cuda, dtype):
             assert ulps.max() <= 4.0, (name, report[name])
         else:
             assert report[name]["max_rel_to_scale"] < 64 * 2.0 ** -24
+    if dtype == "f64":
+        assert report["kernels"]["exact-sums"] == ["k_lap_fx", "k_shell"]
+        assert report["kernels"]["exact-sums-v2"] == ["k_lap_ens2", "k_shell"]
     plan.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
     assert deo.device_status() == 0
     out = os.path.join(os.path.dirname(os.path.dirname(__file__)), "gpurun_out")
     if os.path.isdir(out):
         with open(os.path.join(out, f"parity_256_{dtype}.json"), "w") as f:
             json.dump(report, f)
+
+
+# ---- fixed-point interior kernel: bit-exact against its integer model ---------------
+LAP_CASES = [ND[0], ND[1],
+             dict(shape=(64, 50), terms=[T("centered", 2, 4, axis=k, h=1 / 65,
+                                           bc=("robin", (1.0, 0.5, 0.0), (1.0, 0.5, 0.0), 1)) for k in (1, 2)],
+                  seed=8)]
+
+
+def _wide_range(shape, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal(shape) * np.exp2(rng.integers(-40, 41, size=shape).astype(np.float64))
+    u[rng.random(shape) < 0.05] = 0.0
+    return np.asfortranarray(u)
+
+
+@pytest.mark.parametrize("field", ["normal", "wide", "special"])
+@pytest.mark.parametrize("case", LAP_CASES, ids=["3d-a4-robin", "3d-a2-dirichlet0", "2d-a4-robin"])
+def test_fixed_point_kernel_against_integer_model(cuda, case, field):
+    """Interior points: bit for bit the integer model (tests/fx_model.py) and
+    within 2 ulp of sum|c_k u_k| of the exact rational value; shell points and
+    Inf/NaN fallbacks: bit for bit the reference's order."""
+    import itertools
+    from fractions import Fraction
+    import fx_model as FX
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    nt = len(shape)
+    if field != "normal":
+        u = _wide_range(shape, 11)
+    if field == "special":
+        u[(3,) * nt] = np.inf
+        u[(shape[0] // 2,) + (4,) * (nt - 1)] = np.nan
+    p = deo.Plan(A.terms(), shape, 0)
+    ud = to_device(u)
+    got_t, gen_t = deo.julia_array(shape), deo.julia_array(shape)
+    p.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
+    p.apply(ud, got_t)
+    assert p.kernels == ("k_lap_fx", "k_shell")
+    p.set_option(deo.DEO_OPT_FAST_PATH, 0)
+    p.apply(ud, gen_t)
+    assert p.kernels == ("k_apply",)
+    got, gen = to_host(got_t), to_host(gen_t)
+    Lo = oterms[0][0]
+    w = Lo.tables()[0][0, 0, :]
+    H = len(w) // 2
+    lo = max(Lo.bpc, H)
+    inner = [range(lo, n - lo) for n in shape]
+    interior = np.zeros(shape, bool)
+    interior[tuple(slice(lo, n - lo) for n in shape)] = True
+    # shell: the reference's order, bit for bit (the generic row-table kernel)
+    assert np.array_equal(got[~interior], gen[~interior], equal_nan=True)
+    worst = 0.0
+    fallbacks = 0
+    for idx in itertools.product(*inner):
+        m = FX.fx_point(u, idx, w, H, nt)
+        if m is None:
+            fallbacks += 1
+            assert np.array_equal(got[idx], gen[idx], equal_nan=True), idx
+            continue
+        assert got[idx] == m and np.signbit(got[idx]) == np.signbit(m), (idx, got[idx], m)
+        if field != "special":
+            val, scale = FX.exact_point(u, idx, w, H, nt)
+            if scale:
+                err = abs(Fraction(float(got[idx])) - val)
+                worst = max(worst, float(err / Fraction(float(np.spacing(float(scale))))))
+    assert worst <= 2.0, worst
+    assert (fallbacks > 0) == (field == "special")
+    assert deo.device_status() == 0
+
+
+def test_fixed_point_kernel_not_used_for_wide_weight_ratios(cuda):
+    """A 6th-order Laplacian (outer weight 1/90 of the centre's scale) fails the
+    kernel's error-bound rule and runs the per-offset exact-sum kernel."""
+    case = dict(shape=(24, 20, 18), terms=[T("centered", 2, 6, axis=k, h=0.05, bc=("dirichlet0",))
+                                           for k in (1, 2, 3)], seed=9)
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    p = deo.Plan(A.terms(), shape, 0)
+    out = deo.julia_array(shape)
+    p.apply(to_device(u), out)
+    assert p.kernels == ("k_lap_ens2", "k_shell")
+    tol = 4 * np.spacing(O.abs_scale(oterms, u))
+    assert (np.abs(to_host(out) - O.apply(oterms, u)) <= tol).all()
+
+
+def test_launch_timing(cuda):
+    A, oterms, u = build(ND[0])
+    shape = tuple(ND[0]["shape"])
+    p = deo.Plan(A.terms(), shape, 0)
+    p.set_option(deo.DEO_OPT_LAUNCH_TIMING, 1)
+    out = deo.julia_array(shape)
+    p.apply(to_device(u), out)
+    ms = p.launch_times()
+    assert len(ms) == 2 and all(t > 0 for t in ms)
+    p.set_option(deo.DEO_OPT_FAST_PATH, 0)
+    p.apply(to_device(u), out)
+    assert p.kernels == ("k_apply",) and len(p.launch_times()) == 1
+    with pytest.raises(deo.DeoArgError):
+        p.set_option(deo.DEO_OPT_EXACT_SUMS, 7)
