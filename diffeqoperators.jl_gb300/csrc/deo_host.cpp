@@ -719,6 +719,11 @@ extern "C" int deo_fastdiv_probe(uint32_t n, uint32_t d) {  // host check of the
     const uint32_t t = (uint32_t)(((unsigned long long)n * f.mul) >> 32);
     return (int)((t + n) >> f.shr);
 }
+// Unit counters of the dynamically scheduled interior kernels, used in
+// rotation: applies of one plan in flight at the same time on different
+// streams each need their own (up to kSchedSlots of them).
+constexpr unsigned int kSchedSlots = 1024;
+
 struct deo_plan {
     PlanDev dev{};
     deo::UniPlan uni{};
@@ -727,8 +732,15 @@ struct deo_plan {
     int use_tma = 1;     // DEO_OPT_TMA
     int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
     int timing = 0;      // DEO_OPT_LAUNCH_TIMING
+    int concurrent = 0;  // DEO_OPT_CONCURRENT_SHELL
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     deo::ShellPlan* d_shell = nullptr;  // device copy of `shell` when shell.ok
+    // concurrent shell: a side stream, fork/join events and the interior kernel's unit counter
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    unsigned int* d_sched = nullptr;  // kSchedSlots unit counters, one per apply in rotation
+    mutable std::atomic<unsigned int> sched_slot{0};
+    mutable std::mutex apply_mu;  // one fork/join sequence at a time per plan
     std::vector<void*> allocs;
     size_t table_bytes = 0;
     void* stage_u = nullptr;
@@ -743,6 +755,10 @@ struct deo_plan {
         for (void* p : allocs) cudaFree(p);
         if (d_plan) cudaFree(d_plan);
         if (d_shell) cudaFree(d_shell);
+        if (d_sched) cudaFree(d_sched);
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (side) cudaStreamDestroy(side);
         if (stage_u) cudaFree(stage_u);
         if (stage_du) cudaFree(stage_du);
         for (cudaEvent_t e : ev)
@@ -829,6 +845,12 @@ static void shell_rows(const HostTab& H, int len, int dtype, int t, deo::ShellPl
     };
     for (int r = 0; r < S.nlo; ++r) put(r, r + 1);
     for (int r = 0; r < S.nhi; ++r) put(S.nlo + r, len - S.nhi + 1 + r);
+    // the points of the line each end's rows read (ghost maps added with the BC)
+    S.wlo = S.whi = 0;
+    for (int r = 0; r < S.nlo; ++r) S.wlo = std::max(S.wlo, S.row[r].p0 + S.row[r].nk - 2);
+    for (int r = 0; r < S.nhi; ++r) S.whi = std::max(S.whi, len + 2 - S.row[S.nlo + r].p0);
+    S.wlo = std::min(S.wlo, len);
+    S.whi = std::min(S.whi, len);
 }
 
 // The fixed-point kernel's weights: the shared band w[0..2H] as integers on
@@ -948,6 +970,13 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             pack_values(&T.bl, &S.bl, 1, dtype);
             pack_values(&T.br, &S.br, 1, dtype);
             P->shell.maxw = std::max(P->shell.maxw, std::max(S.ml, S.mr));
+            if (S.bc_kind == 1) {  // periodic: the ghost is an end point, of this end (N-D) or the other (1-D)
+                S.wlo = std::max(S.wlo, S.periodic_nd ? 1 : S.len);
+                S.whi = std::max(S.whi, S.periodic_nd ? 1 : S.len);
+            } else {
+                S.wlo = std::max(S.wlo, S.ml);
+                S.whi = std::max(S.whi, S.mr);
+            }
         }
     }
     P->shell.ok = P->shell.ok >= 0 && nterms <= 3 ? 1 : 0;
@@ -1014,6 +1043,10 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         CUDA_TRY(cudaMalloc(&P->d_shell, sizeof(deo::ShellPlan)), "cudaMalloc(shell rows)");
         CUDA_TRY(cudaMemcpy(P->d_shell, &P->shell, sizeof(deo::ShellPlan), cudaMemcpyHostToDevice),
                  "cudaMemcpy(shell rows)");
+        CUDA_TRY(cudaMalloc(&P->d_sched, kSchedSlots * sizeof(unsigned int)), "cudaMalloc(unit counters)");
+        CUDA_TRY(cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking), "cudaStreamCreate");
+        CUDA_TRY(cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        CUDA_TRY(cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming), "cudaEventCreate");
     }
     *out = P.release();
     return DEO_OK;
@@ -1039,19 +1072,49 @@ static void mark(const deo_plan* p, int k, void* stream) {
     if (p->timing) cudaEventRecord(p->ev[k], static_cast<cudaStream_t>(stream));
 }
 
+// Interior kernel on the caller's stream; the boundary shell either after it
+// on the same stream (default), or (DEO_OPT_CONCURRENT_SHELL) on the plan's
+// side stream at the same time, joined back before the apply completes.  The
+// interior kernels claim their units from the plan's device counter (zeroed
+// on the stream before each launch), so they balance dynamically.
 static int launch_forward(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     mark(p, 0, stream);
     if (p->uni.enabled && p->fast_path) {
         if (p->uni.lap && p->use_tma) {
+            const bool conc = p->concurrent && p->side && p->d_shell;
+            std::unique_lock<std::mutex> lk(p->apply_mu, std::defer_lock);
+            if (conc) {
+                lk.lock();
+                const cudaError_t e = cudaEventRecord(p->ev_fork, st);
+                if (e != cudaSuccess) return (int)e;
+            }
             const char* k = "";
-            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream, &k);
+            // a counter of its own for this launch (applies of one plan may run on several streams at once)
+            unsigned int* sched = p->d_sched ? p->d_sched + (p->sched_slot.fetch_add(1) % kSchedSlots) : nullptr;
+            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream,
+                                          &k, sched);
             if (e != (int)cudaErrorNotSupported) {
                 if (e) return e;
                 mark(p, 1, stream);
                 p->last_kernel = k;
-                p->last_kernel2 = "k_shell";
                 p->ev_launches = 2;
-                const int e2 = deo_k_apply_shell(&p->uni, p->d_shell, p->shell.maxw, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
+                const char* k2 = "";
+                int e2;
+                if (conc) {
+                    cudaError_t c = cudaStreamWaitEvent(p->side, p->ev_fork, 0);
+                    if (c != cudaSuccess) return (int)c;
+                    e2 = deo_k_apply_shell(&p->uni, &p->shell, p->d_shell, DEO_SHELL_CONCURRENT, p->d_plan,
+                                           p->dev.dtype, u, du, overwrite, p->side, &k2);
+                    if (e2) return e2;
+                    c = cudaEventRecord(p->ev_join, p->side);
+                    if (c == cudaSuccess) c = cudaStreamWaitEvent(st, p->ev_join, 0);
+                    if (c != cudaSuccess) return (int)c;
+                } else {
+                    e2 = deo_k_apply_shell(&p->uni, p->d_shell ? &p->shell : nullptr, p->d_shell, DEO_SHELL_ALONE,
+                                           p->d_plan, p->dev.dtype, u, du, overwrite, stream, &k2);
+                }
+                p->last_kernel2 = k2;
                 mark(p, 2, stream);
                 return e2;
             }
@@ -1080,6 +1143,7 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
             if (value < 0 || value > 3) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..3", value);
             p->exact_sums = value;
             return DEO_OK;
+        case DEO_OPT_CONCURRENT_SHELL: p->concurrent = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_LAUNCH_TIMING:
             if (value && !p->ev[0])
                 for (cudaEvent_t& e : p->ev) CUDA_TRY(cudaEventCreate(&e), "cudaEventCreate");
@@ -1096,6 +1160,7 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
         case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
+        case DEO_OPT_CONCURRENT_SHELL: return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap;
     }
     return -1;
 }
@@ -1117,8 +1182,11 @@ extern "C" deo_status deo_plan_launch_times(const deo_plan* p, float* ms, int* n
 
 extern "C" deo_status deo_device_status(unsigned int* status) {
     if (!status) return fail(DEO_ERR_BAD_ARG, "null argument");
-    const int e = deo_k_read_status(status);
+    int e = deo_k_read_status(status);
+    unsigned int s2 = 0;
+    if (!e) e = deo_k_read_shell_status(&s2);
     if (e) return cuda_fail((cudaError_t)e, "deo_device_status");
+    *status |= s2;
     return *status ? fail(DEO_ERR_TIMEOUT, "a bounded device wait gave up (status 0x%x)", *status) : DEO_OK;
 }
 

@@ -132,7 +132,9 @@ struct ShellRow {
 };
 struct ShellTerm {
     int nlo, nhi;  // rows 1..nlo and len-nhi+1..len
-    int len, bc_kind, periodic_nd, ml, mr, pad_;
+    int len, bc_kind, periodic_nd, ml, mr;
+    int wlo, whi;  // points of the line the low / high rows read (with the ghost): [0, wlo), [len-whi, len)
+    int pad_;
     double al[DEO_MAX_BCW], ar[DEO_MAX_BCW];
     double bl, br;
     ShellRow row[2 * DEO_SHELL_ROWS];  // the nlo low rows, then the nhi high rows
@@ -187,15 +189,30 @@ extern "C" int deo_k_num_sms(void);
 // returns cudaErrorNotSupported when the array does not meet the tensor-map
 // alignment rules (caller falls back).  use_ens: 0 the reference's tap order,
 // 1 the best exact-sum kernel that applies, 2 exact sums v1, 3 exact sums v2.
-// *kernel receives the name of the kernel launched.
+// *kernel receives the name of the kernel launched.  sched: null, or a device
+// counter the persistent CTAs claim their units from (zeroed here on the
+// stream before the launch), so that they balance around other work sharing
+// the SMs (the concurrent shell).
 extern "C" int deo_k_apply_tma(const deo::UniPlan* up, const deo::PlanDev* d_plan, int dtype, const void* u,
-                               void* du, int overwrite, int use_ens, void* stream, const char** kernel);
+                               void* du, int overwrite, int use_ens, void* stream, const char** kernel,
+                               unsigned int* sched);
 // The boundary shell around that interior box (boundary rows in the reference's
-// order); sp is the device copy of the plan's ShellPlan (maxw its widest row
-// or ghost map), or null to evaluate the boundary rows from the row tables.
-extern "C" int deo_k_apply_shell(const deo::UniPlan* up, const deo::ShellPlan* sp, int maxw,
-                                 const deo::PlanDev* d_plan, int dtype, const void* u, void* du, int overwrite,
-                                 void* stream);
+// order); sp / sp_dev are the host and device copies of the plan's ShellPlan,
+// or null to evaluate the boundary rows from the row tables.  mode: run alone
+// after the interior kernel (the faster kernel for the dtype) or concurrently
+// with it on another stream (a small grid that fits beside it).  *kernel
+// receives the name of the kernel that runs (it may fall back to another).
+#define DEO_SHELL_ALONE 0
+#define DEO_SHELL_CONCURRENT 1
+extern "C" int deo_k_apply_shell(const deo::UniPlan* up, const deo::ShellPlan* sp, const deo::ShellPlan* sp_dev,
+                                 int mode, const deo::PlanDev* d_plan, int dtype, const void* u, void* du,
+                                 int overwrite, void* stream, const char** kernel);
 extern "C" int deo_k_read_status(unsigned int* status);
+// Encodes a CUtensorMap (written to map, 128 bytes) of a 3-D array nx x ny x nz
+// of es-byte elements for box loads of bx x by x bz; cudaErrorNotSupported if
+// the tensor-map alignment rules are not met.
+extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
+                                 int bz);
+extern "C" int deo_k_read_shell_status(unsigned int* status);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
                                  unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);

@@ -25,7 +25,7 @@
 //     value are dropped) and rounded once.  This takes 2H + 1 FP64
 //     instructions per point instead of NT*(2H+1) + NT - 1, which is what
 //     bounds a Float64 stencil on this part (1.68 DFMA/clk/SM).
-// Points on boundary rows use the generic evaluator for the affected terms.
+// Points on boundary rows (the boundary shell) are left to deo_shell.cu.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -35,35 +35,11 @@
 #include <mutex>
 
 #include "deo_eval.cuh"
+#include "deo_ptx.cuh"
 
 namespace deo {
 
 __device__ unsigned int g_deo_status;  // bit 0: a bounded mbarrier wait gave up
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t* m, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* m, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* m, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(m)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* m, int x, int y, int z) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(m))
-        : "memory");
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // Sum of N doubles, exact up to bits below 2^-59 of the largest, rounded
 // once to nearest.  ok = false for Inf/NaN inputs or a result that is
@@ -144,7 +120,18 @@ struct LapGrid {
     int units;
     int perm;  // coprime with units: unit k of the round-robin is (k * perm) % units,
                // so one CTA's units are spread over tile columns and z chunks
+    unsigned int* sched;  // null: static round-robin; else a zeroed device counter the CTAs claim units from
 };
+
+// The next unit of a CTA: with g.sched claimed from the counter (dynamic, so
+// CTAs that share their SM with other work take fewer units), else k_static.
+// Every thread of the CTA calls it (it contains a barrier).
+__device__ __forceinline__ int claim_unit(const LapGrid& g, int& s_next, int k_static) {
+    if (!g.sched) return k_static;
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_next = (int)atomicAdd(g.sched, 1u);
+    __syncthreads();
+    return s_next;
+}
 
 template <typename T, int H, int NT, bool ENS>
 __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtensorMap tmap,
@@ -617,7 +604,9 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
     };
     int base = 0, issued = 0, waited = 0;
     bool aborted = false;
-    for (int k = blockIdx.x; k < g.units && !aborted; k += gridDim.x) {
+    __shared__ int s_next;
+    for (int k = claim_unit(g, s_next, blockIdx.x); k < g.units && !aborted;
+         k = claim_unit(g, s_next, k + gridDim.x)) {
         const int unit = (int)(((long long)k * g.perm) % g.units);
         const int txi = unit % g.tiles_x;
         const int rest = unit / g.tiles_x;
@@ -753,20 +742,21 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
 
 // ---------------------------------------------------------------------------
 // Reference-order kernel with a register queue (Float32 and Float64).
-// CTA = 32 x 8 threads over a 32 x 32 tile; each thread owns RY = 4
+// CTA = 32 x 8 threads over a 32 x (8 RY) tile; each thread owns RY
 // consecutive rows of one column.  Planes stream through a TMA ring as in
-// k_lap_tma.  Each thread keeps its rows' values at z-H..z+H in registers
-// (one shared-memory load per row and plane), reads the y-neighbours beyond
-// its own rows (2H loads) and the x-neighbours (2H per row) from the centre
-// plane, and evaluates each term's taps in the reference's order, bit for bit
-// the generic evaluator.  One barrier per plane releases the centre plane's
-// slot, which then takes the plane P further on.
+// k_lap_tma.  Each thread keeps its rows' values at z-H..z+H in registers (one
+// shared-memory load per row and plane; the plane loop is unrolled by 2H+1 so
+// the queue rotates by register naming, without moves), reads the
+// y-neighbours beyond its own rows (2H loads) and the x-neighbours (2H per
+// row) from the centre plane, and evaluates each term's taps in the
+// reference's order, bit for bit the generic evaluator.  One barrier per plane
+// releases the centre plane's slot, which then takes the plane P further on.
 // ---------------------------------------------------------------------------
 template <typename T, int H>
 struct QCfg {
-    static constexpr int TX = 32, TYT = 8, RY = 4, TY = TYT * RY;  // threads in x, threads in y, rows per thread
     static constexpr int ES = (int)sizeof(T);
-    static constexpr int HR = ((H * ES + 15) / 16) * 16 / ES;       // x halo rounded up to 16 bytes
+    static constexpr int TX = 32, TYT = 8, RY = ES == 4 ? 8 : 4, TY = TYT * RY;
+    static constexpr int HR = ((H * ES + 15) / 16) * 16 / ES;  // x halo rounded up to 16 bytes
     static constexpr int BX = TX + 2 * HR, BY = TY + 2 * H;
     static constexpr int PLANE = BX * BY;
     static constexpr int PLANE_BYTES = PLANE * ES;
@@ -775,12 +765,23 @@ struct QCfg {
     static constexpr int SMEM = P * SLOT;
 };
 
-template <typename T, int H, int NT>
+// -0 -> +0 (see zero_fix); for Float32 one add of +0, which is exact otherwise.
+template <typename T>
+__device__ __forceinline__ T zero_fix_q(T x) {
+    return zero_fix(x);
+}
+template <>
+__device__ __forceinline__ float zero_fix_q<float>(float x) {
+    return __fadd_rn(x, 0.0f);
+}
+
+template <typename T, int H, int NT, bool OW>
 __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorMap tmap,
                                                const __grid_constant__ UniPlan U, const LapGrid g,
-                                               T* __restrict__ du, int overwrite) {
+                                               T* __restrict__ du) {
     using C = QCfg<T, H>;
     constexpr int HZ = NT == 3 ? H : 0;
+    constexpr int NQ = 2 * HZ + 1;  // queue length = unroll factor of the plane loop
     constexpr int RY = C::RY;
     constexpr int K = 2 * H + 1;
     static_assert(C::P >= H + 2, "ring too short");
@@ -805,7 +806,9 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
     };
     int base = 0, issued = 0, waited = 0;
     bool aborted = false;
-    for (int kk = blockIdx.x; kk < g.units && !aborted; kk += gridDim.x) {
+    __shared__ int s_next;
+    for (int kk = claim_unit(g, s_next, blockIdx.x); kk < g.units && !aborted;
+         kk = claim_unit(g, s_next, kk + gridDim.x)) {
         const int unit = (int)(((long long)kk * g.perm) % g.units);
         const int txi = unit % g.tiles_x;
         const int rest = unit / g.tiles_x;
@@ -817,6 +820,11 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
         const int z1 = min(z0 + g.zc, nz);
         const int npl = (z1 - z0) + 2 * HZ;
         const bool bx = x < nx && x + 1 >= U.t[0].flo && x + 1 <= U.t[0].fhi;
+        unsigned vmask = 0;  // own rows that are interior rows along y
+#pragma unroll
+        for (int j = 0; j < RY; ++j)
+            if (bx && yr + j < ny && yr + j + 1 >= U.t[1].flo && yr + j + 1 <= U.t[1].fhi) vmask |= 1u << j;
+        T* dcol = du + (int64_t)yr * nx + x;
         if (tid == 0) {
             const int pre = min(C::P, npl);
             for (int j = 0; j < pre; ++j) {
@@ -827,76 +835,79 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
             issued = pre;
         }
         waited = 0;
-        T q[RY][2 * HZ + 1];  // own rows at z - HZ .. z + HZ
-        for (int p = 0; p < npl; ++p) {
-            const int gj = base + p;
-            bool timeout = false;
-            {
-                const uint32_t par = (uint32_t)((gj / C::P) & 1);
-                uint32_t it = 0;
-                while (!mbar_try_wait(&mbar[gj & (C::P - 1)], par)) {
-                    if (++it > (1u << 22)) {
-                        timeout = true;
-                        break;
-                    }
-                }
-            }
-            if (!timeout) {
-                waited = p + 1;
-                const T* pn = slot(gj);
+        T q[RY][NQ];  // own rows; plane p lands in q[.][p % NQ]
+        for (int p0 = 0; p0 < npl && !aborted; p0 += NQ) {
 #pragma unroll
-                for (int j = 0; j < RY; ++j) {
-#pragma unroll
-                    for (int o = 0; o < 2 * HZ; ++o) q[j][o] = q[j][o + 1];
-                    q[j][2 * HZ] = pn[c0 + j * C::BX];
-                }
-                const int z = z0 + p - 2 * HZ;  // the point whose last plane is p
-                const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
-                if (p >= 2 * HZ && bx && bz) {
-                    const T* pc = slot(gj - HZ);  // its centre plane
-                    T col[RY + 2 * H];            // this column at rows yr - H .. yr + RY - 1 + H
-#pragma unroll
-                    for (int m = 0; m < H; ++m) {
-                        col[m] = pc[c0 + (m - H) * C::BX];
-                        col[RY + H + m] = pc[c0 + (RY + m) * C::BX];
-                    }
-#pragma unroll
-                    for (int j = 0; j < RY; ++j) col[H + j] = q[j][HZ];
-#pragma unroll
-                    for (int j = 0; j < RY; ++j) {
-                        const int y = yr + j;
-                        if (y < ny && y + 1 >= U.t[1].flo && y + 1 <= U.t[1].fhi) {
-                            const int cc = c0 + j * C::BX;
-                            T ax = T(0), ay = T(0);
-#pragma unroll
-                            for (int k = 0; k < K; ++k) ax = fma(w[0][k], k == H ? col[H + j] : pc[cc + k - H], ax);
-#pragma unroll
-                            for (int k = 0; k < K; ++k) ay = fma(w[1][k], col[j + k], ay);
-                            T tot = ax + ay;
-                            if constexpr (NT == 3) {
-                                T az = T(0);
-#pragma unroll
-                                for (int k = 0; k < K; ++k) az = fma(w[2][k], q[j][k], az);
-                                tot = tot + az;
-                            }
-                            tot = zero_fix(tot);
-                            const int64_t idx = (int64_t)z * sxy + (int64_t)y * nx + x;
-                            du[idx] = overwrite ? tot : tot + du[idx];
+            for (int ph = 0; ph < NQ; ++ph) {
+                const int p = p0 + ph;
+                if (p >= npl) break;
+                const int gj = base + p;
+                bool timeout = false;
+                {
+                    const uint32_t par = (uint32_t)((gj / C::P) & 1);
+                    uint32_t it = 0;
+                    while (!mbar_try_wait(&mbar[gj & (C::P - 1)], par)) {
+                        if (++it > (1u << 22)) {
+                            timeout = true;
+                            break;
                         }
                     }
                 }
-            }
-            if (__syncthreads_or(timeout)) {
-                aborted = true;
-                break;
-            }
-            // every thread is done with plane p - HZ: its slot takes plane p - HZ + P
-            if (tid == 0 && p >= HZ && p - HZ + C::P < npl) {
-                const int jn = p - HZ + C::P;
-                const int s = (base + jn) & (C::P - 1);
-                mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
-                tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
-                issued = jn + 1;
+                if (!timeout) {
+                    waited = p + 1;
+                    const T* pn = slot(gj);
+#pragma unroll
+                    for (int j = 0; j < RY; ++j) q[j][ph] = pn[c0 + j * C::BX];
+                    const int z = z0 + p - 2 * HZ;  // the point whose last plane is p
+                    const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
+                    if (p >= 2 * HZ && vmask && bz) {
+                        const T* pc = slot(gj - HZ);  // its centre plane
+                        T col[RY + 2 * H];            // this column at rows yr - H .. yr + RY - 1 + H
+#pragma unroll
+                        for (int m = 0; m < H; ++m) {
+                            col[m] = pc[c0 + (m - H) * C::BX];
+                            col[RY + H + m] = pc[c0 + (RY + m) * C::BX];
+                        }
+#pragma unroll
+                        for (int j = 0; j < RY; ++j) col[H + j] = q[j][(ph + 1 + HZ) % NQ];
+                        T* dz = dcol + (int64_t)z * sxy;
+#pragma unroll
+                        for (int j = 0; j < RY; ++j) {
+                            if (vmask & (1u << j)) {
+                                const int cc = c0 + j * C::BX;
+                                T ax = T(0), ay = T(0);
+#pragma unroll
+                                for (int k = 0; k < K; ++k)
+                                    ax = fma(w[0][k], k == H ? col[H + j] : pc[cc + k - H], ax);
+#pragma unroll
+                                for (int k = 0; k < K; ++k) ay = fma(w[1][k], col[j + k], ay);
+                                T tot = ax + ay;
+                                if constexpr (NT == 3) {
+                                    T az = T(0);
+#pragma unroll
+                                    for (int k = 0; k < K; ++k) az = fma(w[2][k], q[j][(ph + 1 + k) % NQ], az);
+                                    tot = tot + az;
+                                }
+                                tot = zero_fix_q(tot);
+                                T* d = dz + (int64_t)j * nx;
+                                if constexpr (OW) *d = tot;
+                                else *d = tot + *d;
+                            }
+                        }
+                    }
+                }
+                if (__syncthreads_or(timeout)) {
+                    aborted = true;
+                    break;
+                }
+                // every thread is done with plane p - HZ: its slot takes plane p - HZ + P
+                if (tid == 0 && p >= HZ && p - HZ + C::P < npl) {
+                    const int jn = p - HZ + C::P;
+                    const int s = (base + jn) & (C::P - 1);
+                    mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
+                    tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + jn);
+                    issued = jn + 1;
+                }
             }
         }
         if (!aborted) base += npl;
@@ -910,207 +921,6 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
             for (uint32_t it = 0; it < (1u << 22); ++it)
                 if (mbar_try_wait(&mbar[gj & (C::P - 1)], par)) break;
         }
-    }
-}
-
-// The boundary shell of a Laplacian-type plan: every point with a non-band
-// row along some axis (it reads a ghost or uses a boundary stencil).  The
-// tiled kernels compute the interior box [flo, fhi]^NT; this kernel computes
-// the rest in the reference's order (the generic evaluator's arithmetic, tap
-// for tap): along an axis where the point's row is an interior row, the
-// band's taps; along the others, the boundary row's taps with the ghost
-// values of the boundary condition.  With ROWS the boundary rows, weights and
-// ghost maps are staged once per CTA from the plan's ShellPlan into shared
-// memory and every load of a point is independent of the others; without it,
-// they come from the plan's row tables (the generic evaluator itself).
-// Index space, ordered so that the 32 points of a warp share their boundary
-// row: z outside the box (full planes, x fastest), then z inside & y outside
-// (full rows, x fastest), then z, y inside & x outside (y fastest).  The grid
-// strides over it.
-struct ShellBox {
-    int lo[3], hi[3];      // interior box, 0-based inclusive (empty if lo > hi)
-    int64_t n[3];
-    int64_t cz, cy, cx;    // points in each part
-    int small;             // cz + cy + cx < 2^31: index arithmetic by the FastDiv constants below
-    FastDiv d_nxny, d_nx, d_nyonx, d_niy, d_nxo;
-};
-
-// Coordinates of shell point t (see the index-space order above).
-__device__ __forceinline__ void shell_coords(const ShellBox& B, int64_t t, int64_t& x, int64_t& y, int64_t& z) {
-    const int64_t nx = B.n[0], ny = B.n[1];
-    const int64_t nyo = ny - (B.hi[1] - B.lo[1] + 1);
-    const int64_t nxo = nx - (B.hi[0] - B.lo[0] + 1);
-    const int64_t niy = B.hi[1] - B.lo[1] + 1;
-    if (t < B.cz) {
-        int64_t pl, r;
-        if (B.small) {
-            pl = fast_div((uint32_t)t, B.d_nxny);
-            r = t - pl * nx * ny;
-            y = fast_div((uint32_t)r, B.d_nx);
-        } else {
-            pl = t / (nx * ny);
-            r = t - pl * nx * ny;
-            y = r / nx;
-        }
-        x = r - y * nx;
-        z = pl < B.lo[2] ? pl : pl - B.lo[2] + B.hi[2] + 1;
-    } else if (t < B.cz + B.cy) {
-        const int64_t q = t - B.cz;
-        int64_t pl, r, row;
-        if (B.small) {
-            pl = fast_div((uint32_t)q, B.d_nyonx);
-            r = q - pl * nyo * nx;
-            row = fast_div((uint32_t)r, B.d_nx);
-        } else {
-            pl = q / (nyo * nx);
-            r = q - pl * nyo * nx;
-            row = r / nx;
-        }
-        z = B.lo[2] + pl;
-        x = r - row * nx;
-        y = row < B.lo[1] ? row : row - B.lo[1] + B.hi[1] + 1;
-    } else {
-        const int64_t q = t - B.cz - B.cy;
-        int64_t line, zz;
-        if (B.small) {
-            line = fast_div((uint32_t)q, B.d_niy);  // (z, x column) pairs, y fastest
-            zz = fast_div((uint32_t)line, B.d_nxo);
-        } else {
-            line = q / niy;
-            zz = line / nxo;
-        }
-        y = B.lo[1] + (q - line * niy);
-        z = B.lo[2] + zz;
-        const int64_t c = line - zz * nxo;
-        x = c < B.lo[0] ? c : c - B.lo[0] + B.hi[0] + 1;
-    }
-}
-
-// Element k of a packed weight array (doubles, or floats packed from the start).
-template <typename T>
-__device__ __forceinline__ T sw(const double* a, int k);
-template <>
-__device__ __forceinline__ double sw<double>(const double* a, int k) {
-    return a[k];
-}
-template <>
-__device__ __forceinline__ float sw<float>(const double* a, int k) {
-    return reinterpret_cast<const float*>(a)[k];
-}
-
-// Ghost values, as ghost_left / ghost_right (same arithmetic), W >= ml, mr.
-template <typename T, int W>
-__device__ __forceinline__ T shell_ghost(const ShellTerm& S, const T* __restrict__ line, int64_t s, bool left) {
-    if (S.bc_kind == 1)
-        return (S.periodic_nd == left) ? __ldg(line) : __ldg(line + (int64_t)(S.len - 1) * s);
-    const int m = left ? S.ml : S.mr;
-    const int64_t o = left ? 0 : (int64_t)(S.len - S.mr);
-    const double* a = left ? S.al : S.ar;
-    T v[W];
-#pragma unroll
-    for (int j = 0; j < W; ++j) v[j] = j < m ? __ldg(line + (o + j) * s) : T(0);
-    T d = T(0);
-#pragma unroll
-    for (int j = 0; j < W; ++j)
-        if (j < m) d = (j == 0) ? sw<T>(a, 0) * v[0] : fma(sw<T>(a, j), v[j], d);
-    return d + sw<T>(left ? &S.bl : &S.br, 0);
-}
-
-// Boundary row i (1-based) of a term on the line starting at `line`, as
-// eval_term (same taps, same order); W >= the row's taps.
-template <typename T, int W>
-__device__ __forceinline__ T shell_row(const ShellTerm& S, const T* __restrict__ line, int64_t s, int i) {
-    const int r = i <= S.nlo ? i - 1 : S.nlo + (i - (S.len - S.nhi + 1));
-    const ShellRow& R = S.row[r];
-    const int L2 = S.len + 2;
-    const int p0 = R.p0, nk = R.nk;
-    const T gl = p0 == 1 ? shell_ghost<T, W>(S, line, s, true) : T(0);
-    const T gr = p0 + nk - 1 == L2 ? shell_ghost<T, W>(S, line, s, false) : T(0);
-    T x[W];
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-        const int p = p0 + k;
-        x[k] = (k >= nk || p == 1 || p == L2) ? T(0) : __ldg(line + (int64_t)(p - 2) * s);
-    }
-    T acc = T(0);
-#pragma unroll
-    for (int k = 0; k < W; ++k) {
-        if (k < nk) {
-            const int p = p0 + k;
-            acc = fma(sw<T>(R.w, k), p == 1 ? gl : (p == L2 ? gr : x[k]), acc);
-        }
-    }
-    return acc;
-}
-
-// Band taps of axis a at idx (interior row along a), as eval_term's band path.
-template <typename T, int H>
-__device__ __forceinline__ T shell_band(const UniTerm& ut, const T* __restrict__ u, int64_t idx, int64_t s) {
-    T r = T(0);
-#pragma unroll
-    for (int k = 0; k < 2 * H + 1; ++k) r = fma(uni_w<T>(ut, k), __ldg(u + idx + (k - H) * s), r);
-    return r;
-}
-
-template <typename T, int H, int NT, int W>
-__global__ void __launch_bounds__(256) k_shell(const __grid_constant__ ShellBox B, const __grid_constant__ UniPlan U,
-                                               const ShellPlan* __restrict__ SPg, const T* __restrict__ u,
-                                               T* __restrict__ du, int overwrite) {
-    static_assert(sizeof(ShellTerm) % 8 == 0, "ShellTerm copied in 8-byte words");
-    __shared__ __align__(16) ShellTerm S[NT];
-    {
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(SPg->t);
-        unsigned long long* dst = reinterpret_cast<unsigned long long*>(S);
-        for (int q = threadIdx.x; q < (int)(NT * sizeof(ShellTerm) / 8); q += blockDim.x) dst[q] = __ldg(src + q);
-        __syncthreads();
-    }
-    const int64_t nx = B.n[0], ny = B.n[1];
-    const int64_t total = B.cz + B.cy + B.cx;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t x, y, z;
-        shell_coords(B, t, x, y, z);
-        const int64_t idx = (z * ny + y) * nx + x;
-        const int64_t crd[3] = {x, y, z};
-        const int64_t st[3] = {1, nx, nx * ny};
-        T acc = T(0);
-#pragma unroll
-        for (int a = 0; a < NT; ++a) {
-            const int i = (int)crd[a] + 1;
-            const T r = (i >= U.t[a].flo && i <= U.t[a].fhi)
-                            ? shell_band<T, H>(U.t[a], u, idx, st[a])
-                            : shell_row<T, W>(S[a], u + idx - crd[a] * st[a], st[a], i);
-            acc = (a == 0) ? r : acc + r;
-        }
-        const T tot = zero_fix(acc);
-        du[idx] = overwrite ? tot : tot + du[idx];
-    }
-}
-
-// The same shell with the boundary rows from the plan's row tables (plans
-// whose boundary rows do not fit a ShellPlan).
-template <typename T, int H, int NT>
-__global__ void __launch_bounds__(256) k_shell_generic(const __grid_constant__ ShellBox B,
-                                                       const __grid_constant__ UniPlan U,
-                                                       const PlanDev* __restrict__ P, const T* __restrict__ u,
-                                                       T* __restrict__ du, int overwrite) {
-    const int64_t nx = B.n[0], ny = B.n[1];
-    const int64_t total = B.cz + B.cy + B.cx;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-        int64_t x, y, z;
-        shell_coords(B, t, x, y, z);
-        const int64_t idx = (z * ny + y) * nx + x;
-        const int64_t crd[3] = {x, y, z};
-        const int64_t st[3] = {1, nx, nx * ny};
-        T acc = T(0);
-#pragma unroll
-        for (int a = 0; a < NT; ++a) {
-            const int i = (int)crd[a] + 1;
-            const T r = (i >= U.t[a].flo && i <= U.t[a].fhi) ? shell_band<T, H>(U.t[a], u, idx, st[a])
-                                                             : eval_term<T>(P->t[a], u, idx, i);
-            acc = (a == 0) ? r : acc + r;
-        }
-        const T tot = zero_fix(acc);
-        du[idx] = overwrite ? tot : tot + du[idx];
     }
 }
 
@@ -1132,17 +942,30 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-static bool make_map(CUtensorMap& map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by) {
-    if (((uintptr_t)u & 15) || ((nx * es) & 15) || nx > (1 << 30) || ny > (1 << 30) || nz > (1 << 30)) return false;
+static bool make_map3(CUtensorMap& map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
+                      int bz) {
+    if (((uintptr_t)u & 15) || ((nx * es) & 15) || ((bx * es) & 15) || nx > (1 << 30) || ny > (1 << 30) ||
+        nz > (1 << 30) || bx < 1 || bx > 256 || by < 1 || by > 256 || bz < 1 || bz > 256)
+        return false;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     if (!enc) return false;
     const cuuint64_t gdim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
     const cuuint64_t gstride[2] = {(cuuint64_t)(nx * es), (cuuint64_t)(nx * ny * es)};
-    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(&map, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(u),
                gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static bool make_map(CUtensorMap& map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by) {
+    return make_map3(map, u, es, nx, ny, nz, bx, by, 1);
+}
+
+extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
+                                 int bz) {
+    return make_map3(*reinterpret_cast<CUtensorMap*>(map), u, es, nx, ny, nz, bx, by, bz) ? 0
+                                                                                          : (int)cudaErrorNotSupported;
 }
 
 // Units and z chunk for a persistent grid of G CTAs (see LapGrid).
@@ -1170,6 +993,7 @@ static LapGrid make_grid(const UniPlan* up, int tx, int ty, int H, int nt, int64
     }
     g.chunks = (int)((nz + g.zc - 1) / g.zc);
     g.units = (int)(tiles * g.chunks);
+    g.sched = nullptr;
     g.perm = 1;
     for (int cand : {7919, 6007, 4099, 2053, 1031, 521, 263, 131, 67, 37, 17}) {
         int a = cand, b = g.units;
@@ -1235,37 +1059,47 @@ static int launch_ens2(const UniPlan* up, const PlanDev* dp, const void* u, void
 }
 
 template <typename T, int H, int NT>
-static int launch_q(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+static int launch_q(const UniPlan* up, unsigned int* sched, const void* u, void* du, int ow, cudaStream_t st) {
     using C = QCfg<T, H>;
     CUtensorMap map;
     if (!make_map(map, u, C::ES, up->n[0], up->n[1], up->n[2], C::BX, C::BY)) return (int)cudaErrorNotSupported;
     static int64_t G = 0;
     if (!G) {
-        const int e = occupancy_grid(k_lap_q<T, H, NT>, C::TX * C::TYT, C::SMEM, G);
+        int e = occupancy_grid(k_lap_q<T, H, NT, true>, C::TX * C::TYT, C::SMEM, G);
+        if (!e) e = occupancy_grid(k_lap_q<T, H, NT, false>, C::TX * C::TYT, C::SMEM, G);
         if (e) return e;
     }
     const LapGrid g = make_grid(up, C::TX, C::TY, H, NT, G);
+    LapGrid g2 = g;
+    g2.sched = sched;
+    if (sched) {
+        const cudaError_t e = cudaMemsetAsync(sched, 0, sizeof(unsigned int), st);
+        if (e != cudaSuccess) return (int)e;
+    }
     const int grid = (int)std::min<int64_t>(G, g.units);
-    k_lap_q<T, H, NT><<<grid, dim3(C::TX, C::TYT), C::SMEM, st>>>(map, *up, g, (T*)du, ow);
+    if (ow)
+        k_lap_q<T, H, NT, true><<<grid, dim3(C::TX, C::TYT), C::SMEM, st>>>(map, *up, g2, (T*)du);
+    else
+        k_lap_q<T, H, NT, false><<<grid, dim3(C::TX, C::TYT), C::SMEM, st>>>(map, *up, g2, (T*)du);
     return (int)cudaGetLastError();
 }
 
 template <typename T>
-static int launch_q_h(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+static int launch_q_h(const UniPlan* up, unsigned int* sched, const void* u, void* du, int ow, cudaStream_t st) {
     const int H = up->radius;
     if (up->nterms == 3) {
         switch (H) {
-            case 1: return launch_q<T, 1, 3>(up, u, du, ow, st);
-            case 2: return launch_q<T, 2, 3>(up, u, du, ow, st);
-            case 3: return launch_q<T, 3, 3>(up, u, du, ow, st);
-            case 4: return launch_q<T, 4, 3>(up, u, du, ow, st);
+            case 1: return launch_q<T, 1, 3>(up, sched, u, du, ow, st);
+            case 2: return launch_q<T, 2, 3>(up, sched, u, du, ow, st);
+            case 3: return launch_q<T, 3, 3>(up, sched, u, du, ow, st);
+            case 4: return launch_q<T, 4, 3>(up, sched, u, du, ow, st);
         }
     } else if (up->nterms == 2) {
         switch (H) {
-            case 1: return launch_q<T, 1, 2>(up, u, du, ow, st);
-            case 2: return launch_q<T, 2, 2>(up, u, du, ow, st);
-            case 3: return launch_q<T, 3, 2>(up, u, du, ow, st);
-            case 4: return launch_q<T, 4, 2>(up, u, du, ow, st);
+            case 1: return launch_q<T, 1, 2>(up, sched, u, du, ow, st);
+            case 2: return launch_q<T, 2, 2>(up, sched, u, du, ow, st);
+            case 3: return launch_q<T, 3, 2>(up, sched, u, du, ow, st);
+            case 4: return launch_q<T, 4, 2>(up, sched, u, du, ow, st);
         }
     }
     return (int)cudaErrorNotSupported;
@@ -1293,7 +1127,7 @@ static int launch_tma_h(const UniPlan* up, const PlanDev* dp, const void* u, voi
 }
 
 template <int H, int NT>
-static int launch_fx(const UniPlan* up, const void* u, void* du, int ow, cudaStream_t st) {
+static int launch_fx(const UniPlan* up, unsigned int* sched, const void* u, void* du, int ow, cudaStream_t st) {
     using C = TmaCfg<double, H>;
     using F = FxCfg<H>;
     CUtensorMap map;
@@ -1304,92 +1138,15 @@ static int launch_fx(const UniPlan* up, const void* u, void* du, int ow, cudaStr
         if (e) return e;
     }
     const LapGrid g = make_grid(up, C::TX, C::TY, H, NT, G);
+    LapGrid g2 = g;
+    g2.sched = sched;
+    if (sched) {
+        const cudaError_t e = cudaMemsetAsync(sched, 0, sizeof(unsigned int), st);
+        if (e != cudaSuccess) return (int)e;
+    }
     const int grid = (int)std::min<int64_t>(G, g.units);
-    k_lap_fx<H, NT><<<grid, dim3(C::TX, C::TY), F::SMEM, st>>>(map, *up, g, (const double*)u, (double*)du, ow);
+    k_lap_fx<H, NT><<<grid, dim3(C::TX, C::TY), F::SMEM, st>>>(map, *up, g2, (const double*)u, (double*)du, ow);
     return (int)cudaGetLastError();
-}
-
-template <typename K>
-static int64_t shell_grid(K kernel, int64_t total) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0);
-    if (per_sm < 1) per_sm = 1;
-    return std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)deo_k_num_sms() * per_sm));
-}
-
-template <typename T, int H, int NT>
-static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, const void* u, void* du,
-                          int ow, cudaStream_t st) {
-    ShellBox B{};
-    for (int k = 0; k < 3; ++k) {
-        B.n[k] = up->n[k];
-        if (k < up->nterms) {
-            B.lo[k] = up->t[k].flo - 1;
-            B.hi[k] = up->t[k].fhi - 1;
-        } else {
-            B.lo[k] = 0;
-            B.hi[k] = (int)up->n[k] - 1;
-        }
-        if (B.lo[k] > B.hi[k]) {  // no interior along k: everything is shell
-            B.lo[k] = (int)up->n[k];
-            B.hi[k] = (int)up->n[k] - 1;
-        }
-    }
-    const int64_t ix = B.hi[0] - B.lo[0] + 1, iy = B.hi[1] - B.lo[1] + 1, iz = B.hi[2] - B.lo[2] + 1;
-    const int64_t nx = B.n[0], ny = B.n[1], nz = B.n[2];
-    B.cz = (nz - iz) * nx * ny;
-    B.cy = iz * (ny - iy) * nx;
-    B.cx = iz * iy * (nx - ix);
-    const int64_t total = B.cz + B.cy + B.cx;
-    if (total == 0) return 0;
-    B.small = total < (1LL << 31) && nx * ny < (1LL << 31);
-    if (B.small) {
-        auto fd = [](int64_t d) { return make_fastdiv((uint32_t)std::max<int64_t>(d, 1)); };
-        B.d_nxny = fd(nx * ny);
-        B.d_nx = fd(nx);
-        B.d_nyonx = fd((ny - iy) * nx);
-        B.d_niy = fd(iy);
-        B.d_nxo = fd(nx - ix);
-    }
-    if (sp && maxw <= 8) {
-        static int64_t g = 0;
-        if (!g) g = shell_grid(k_shell<T, H, NT, 8>, 1LL << 40);
-        k_shell<T, H, NT, 8><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, sp, (const T*)u,
-                                                                                       (T*)du, ow);
-    } else if (sp) {
-        static int64_t g = 0;
-        if (!g) g = shell_grid(k_shell<T, H, NT, 16>, 1LL << 40);
-        k_shell<T, H, NT, 16><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, sp, (const T*)u,
-                                                                                        (T*)du, ow);
-    } else {
-        static int64_t g = 0;
-        if (!g) g = shell_grid(k_shell_generic<T, H, NT>, 1LL << 40);
-        k_shell_generic<T, H, NT><<<(unsigned)std::min(g, (total + 255) / 256), 256, 0, st>>>(B, *up, dp, (const T*)u,
-                                                                                          (T*)du, ow);
-    }
-    return (int)cudaGetLastError();
-}
-
-template <typename T>
-static int launch_shell(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, const void* u, void* du,
-                        int ow, cudaStream_t st) {
-    const int H = up->radius;
-    if (up->nterms == 3) {
-        switch (H) {
-            case 1: return launch_shell_t<T, 1, 3>(up, sp, maxw, dp, u, du, ow, st);
-            case 2: return launch_shell_t<T, 2, 3>(up, sp, maxw, dp, u, du, ow, st);
-            case 3: return launch_shell_t<T, 3, 3>(up, sp, maxw, dp, u, du, ow, st);
-            case 4: return launch_shell_t<T, 4, 3>(up, sp, maxw, dp, u, du, ow, st);
-        }
-    } else if (up->nterms == 2) {
-        switch (H) {
-            case 1: return launch_shell_t<T, 1, 2>(up, sp, maxw, dp, u, du, ow, st);
-            case 2: return launch_shell_t<T, 2, 2>(up, sp, maxw, dp, u, du, ow, st);
-            case 3: return launch_shell_t<T, 3, 2>(up, sp, maxw, dp, u, du, ow, st);
-            case 4: return launch_shell_t<T, 4, 2>(up, sp, maxw, dp, u, du, ow, st);
-        }
-    }
-    return (int)cudaErrorNotSupported;
 }
 
 #define DEO_TRY_KERNEL(call, name)                            \
@@ -1402,19 +1159,19 @@ static int launch_shell(const UniPlan* up, const ShellPlan* sp, int maxw, const 
     } while (0)
 
 extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du,
-                               int overwrite, int use_ens, void* stream, const char** kernel) {
+                               int overwrite, int use_ens, void* stream, const char** kernel, unsigned int* sched) {
     static const char* none = "";
     if (!kernel) kernel = &none;
     if (!up->lap || up->nterms < 2 || up->nterms > 3) return (int)cudaErrorNotSupported;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int H = up->radius, NT = up->nterms;
     if (dtype == 0 && use_ens == 1 && up->fx) {
-        if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 3>(up, u, du, overwrite, st)), "k_lap_fx");
-        if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 3>(up, u, du, overwrite, st)), "k_lap_fx");
-        if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 3>(up, u, du, overwrite, st)), "k_lap_fx");
-        if (NT == 2 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 2>(up, u, du, overwrite, st)), "k_lap_fx");
-        if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 2>(up, u, du, overwrite, st)), "k_lap_fx");
-        if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 2>(up, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
+        if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
     }
     if (dtype == 0 && (use_ens == 1 || use_ens == 3) && up->ens) {
         if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_ens2<1, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
@@ -1427,19 +1184,13 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
     if (dtype == 0) {
         if (use_ens && up->ens)
             DEO_TRY_KERNEL((launch_tma_h<double, true>(up, dp, u, du, overwrite, st)), "k_lap_tma(exact sums v1)");
-        DEO_TRY_KERNEL((launch_q_h<double>(up, u, du, overwrite, st)), "k_lap_q");
+        DEO_TRY_KERNEL((launch_q_h<double>(up, sched, u, du, overwrite, st)), "k_lap_q");
     } else {
-        DEO_TRY_KERNEL((launch_q_h<float>(up, u, du, overwrite, st)), "k_lap_q");
+        DEO_TRY_KERNEL((launch_q_h<float>(up, sched, u, du, overwrite, st)), "k_lap_q");
     }
     return (int)cudaErrorNotSupported;
 }
 
-extern "C" int deo_k_apply_shell(const UniPlan* up, const ShellPlan* sp, int maxw, const PlanDev* dp, int dtype,
-                                 const void* u, void* du, int overwrite, void* stream) {
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return dtype == 0 ? launch_shell<double>(up, sp, maxw, dp, u, du, overwrite, st)
-                      : launch_shell<float>(up, sp, maxw, dp, u, du, overwrite, st);
-}
 
 extern "C" int deo_k_read_status(unsigned int* status) {
     unsigned int v = 0, zero = 0;

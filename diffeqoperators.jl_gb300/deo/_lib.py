@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "OK", 1: "BAD_SHAPE", 2: "BAD_ARG", 3: "UNSUPPORTED", 4: "CUD
 DEO_F64, DEO_F32 = 0, 1
 DEO_BC_AFFINE, DEO_BC_PERIODIC = 0, 1
 DEO_PATH_AUTO, DEO_PATH_PADDED, DEO_PATH_GENERIC = 0, 1, 2
-DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS, DEO_OPT_LAUNCH_TIMING = 1, 2, 3, 4
+DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS, DEO_OPT_LAUNCH_TIMING, DEO_OPT_CONCURRENT_SHELL = 1, 2, 3, 4, 5
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)

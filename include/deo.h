@@ -167,7 +167,7 @@ deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int
 void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
-/* Plan options (defaults 1):
+/* Plan options (defaults 1 unless stated):
  *   DEO_OPT_FAST_PATH: 2-D/3-D plans whose terms all have constant interior
  *     rows use tiled kernels for interior points; 0 forces the generic
  *     row-table kernel.
@@ -187,11 +187,17 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *         kernel.
  *   DEO_OPT_LAUNCH_TIMING: 1 records CUDA events around every kernel launch
  *     of each forward apply (read with deo_plan_launch_times); default 0.
+ *   DEO_OPT_CONCURRENT_SHELL: 1 evaluates the boundary shell of a
+ *     Laplacian-type plan on the TMA path on a plan-owned side stream at the
+ *     same time as the interior (forked from and joined back into the
+ *     caller's stream, so the apply stays stream-ordered); default 0, the
+ *     shell after the interior on the caller's stream.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
 #define DEO_OPT_EXACT_SUMS 3
 #define DEO_OPT_LAUNCH_TIMING 4
+#define DEO_OPT_CONCURRENT_SHELL 5
 deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);
@@ -200,8 +206,10 @@ int deo_plan_get_option(const deo_plan* plan, int option);
  * Static strings; "" before the first apply.  No reference counterpart. */
 const char* deo_plan_kernels(const deo_plan* plan, int which);
 /* Device time in ms of each launch of the last forward apply (DEO_OPT_LAUNCH_TIMING
- * must be on); ms needs room for 2 entries, *n receives the count.  Waits for
- * that apply to finish.  No reference counterpart. */
+ * must be on); ms needs room for 2 entries, *n receives the count.  With a
+ * concurrent shell, ms[0] is the interior kernel and ms[1] the time the apply
+ * then still waits for the shell.  Waits for that apply to finish.  No
+ * reference counterpart. */
 deo_status deo_plan_launch_times(const deo_plan* plan, float* ms, int* n);
 /* Device-side error flags raised since the last call (bit 0: a bounded wait
  * in a kernel gave up; the kernel returned without finishing).  Synchronises.
@@ -212,7 +220,9 @@ deo_status deo_device_status(unsigned int* status);
  * the reference's `mul!(x, L, M; overwrite=false)`, convolutions.jl:17-22).
  * Replaces LinearAlgebra.mul!(out, A::GhostDerivativeOperator, u)
  * (ghost_derivative_operator.jl:15-24) and `(A*Q)*u` (ghost_derivative_operator.jl:26-37,
- * composite_operators.jl:64-65).  u and du must not overlap. */
+ * composite_operators.jl:64-65).  u and du must not overlap.  A plan may be applied
+ * from several host threads and streams at once (up to 1024 applies of one plan in
+ * flight at the same time). */
 deo_status deo_apply(const deo_plan* plan, const void* u, void* du, int overwrite, void* stream);
 
 /* Same, reading u from host memory and writing du to host memory (copies
