@@ -504,6 +504,12 @@ def run_batch(args):
     t_b = _event_time(batched, max(3, args.steps // 50), 2)
     t_1 = _event_time(one_by_one, max(2, args.steps // 200), 1)
     t_n = _event_time(one_by_one_native, max(2, args.steps // 100), 1)
+    # the plain per-instance apply: the generic row-table kernel, one launch per instance
+    for p in plans:
+        p.set_option(deo.DEO_OPT_FAST_PATH, 0)
+    t_p = _event_time(one_by_one_native, max(2, args.steps // 100), 1)
+    for p in plans:
+        p.set_option(deo.DEO_OPT_FAST_PATH, 1)
     # results agree bit for bit
     torch.cuda.synchronize()
     same = max(float(((a - b).abs().max() / b.abs().max().clamp_min(1e-300))) for a, b in zip(fw, ones))
@@ -512,6 +518,8 @@ def run_batch(args):
     return {"metric": "solves/s (4096 batched forward+adjoint applies)", "workload": "batched_4096_mixed_f64",
             "value": len(inst) / t_b, "unit": "solves/s", "dtype": "f64", "total_points": total,
             "ms_per_pass": t_b * 1e3,
+            "one_launch_per_instance_plain_ms": t_p * 1e3,
+            "speedup_vs_one_launch_per_instance_plain": t_p / t_b,
             "one_launch_per_instance_native_ms": t_n * 1e3,
             "speedup_vs_one_launch_per_instance_native": t_n / t_b,
             "one_launch_per_instance_python_ms": t_1 * 1e3,

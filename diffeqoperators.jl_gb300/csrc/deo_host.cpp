@@ -732,7 +732,7 @@ struct deo_plan {
     int use_tma = 1;     // DEO_OPT_TMA
     int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
     int timing = 0;      // DEO_OPT_LAUNCH_TIMING
-    int concurrent = 0;  // DEO_OPT_CONCURRENT_SHELL
+    int concurrent = -1;  // DEO_OPT_CONCURRENT_SHELL; -1: by dtype (Float32 on, Float64 off)
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     deo::ShellPlan* d_shell = nullptr;  // device copy of `shell` when shell.ok
     // concurrent shell: a side stream, fork/join events and the interior kernel's unit counter
@@ -1082,7 +1082,7 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
     mark(p, 0, stream);
     if (p->uni.enabled && p->fast_path) {
         if (p->uni.lap && p->use_tma) {
-            const bool conc = p->concurrent && p->side && p->d_shell;
+            const bool conc = (p->concurrent < 0 ? p->dev.dtype == DEO_F32 : p->concurrent != 0) && p->side && p->d_shell;
             std::unique_lock<std::mutex> lk(p->apply_mu, std::defer_lock);
             if (conc) {
                 lk.lock();
@@ -1160,7 +1160,9 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
         case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
-        case DEO_OPT_CONCURRENT_SHELL: return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap;
+        case DEO_OPT_CONCURRENT_SHELL:
+            return (p->concurrent < 0 ? p->dev.dtype == DEO_F32 : p->concurrent != 0) && p->side && p->d_shell &&
+                   p->uni.enabled && p->uni.lap;
     }
     return -1;
 }

@@ -29,7 +29,8 @@ __device__ __forceinline__ float sw<float>(const double* a, int k) {
 }
 
 // Ghost value of one end of a line with its m taps unrolled (M = m): the
-// arithmetic of ghost_left / ghost_right.
+// arithmetic of ghost_left / ghost_right.  The dispatchers below take MAXW, the
+// widest ghost map / row they must handle (8 or 16), to keep registers low.
 template <typename T, int M>
 __device__ __forceinline__ T ghost_m(const double* a, const double* b, const T* __restrict__ p, int64_t s) {
     T d = sw<T>(a, 0) * ldv(p);
@@ -38,7 +39,7 @@ __device__ __forceinline__ T ghost_m(const double* a, const double* b, const T* 
     return d + sw<T>(b, 0);
 }
 
-template <typename T>
+template <typename T, int MAXW = 16>
 __device__ __forceinline__ T shell_ghost(const ShellTerm& S, const T* __restrict__ line, int64_t s, bool left) {
     if (S.bc_kind == 1) return (S.periodic_nd == left) ? ldv(line) : ldv(line + (int64_t)(S.len - 1) * s);
     const int m = left ? S.ml : S.mr;
@@ -55,14 +56,14 @@ __device__ __forceinline__ T shell_ghost(const ShellTerm& S, const T* __restrict
         case 6: return ghost_m<T, 6>(a, b, p, s);
         case 7: return ghost_m<T, 7>(a, b, p, s);
         case 8: return ghost_m<T, 8>(a, b, p, s);
-        case 9: return ghost_m<T, 9>(a, b, p, s);
-        case 10: return ghost_m<T, 10>(a, b, p, s);
-        case 11: return ghost_m<T, 11>(a, b, p, s);
-        case 12: return ghost_m<T, 12>(a, b, p, s);
-        case 13: return ghost_m<T, 13>(a, b, p, s);
-        case 14: return ghost_m<T, 14>(a, b, p, s);
-        case 15: return ghost_m<T, 15>(a, b, p, s);
-        case 16: return ghost_m<T, 16>(a, b, p, s);
+        case 9: if constexpr (9 <= MAXW) return ghost_m<T, 9>(a, b, p, s); break;
+        case 10: if constexpr (10 <= MAXW) return ghost_m<T, 10>(a, b, p, s); break;
+        case 11: if constexpr (11 <= MAXW) return ghost_m<T, 11>(a, b, p, s); break;
+        case 12: if constexpr (12 <= MAXW) return ghost_m<T, 12>(a, b, p, s); break;
+        case 13: if constexpr (13 <= MAXW) return ghost_m<T, 13>(a, b, p, s); break;
+        case 14: if constexpr (14 <= MAXW) return ghost_m<T, 14>(a, b, p, s); break;
+        case 15: if constexpr (15 <= MAXW) return ghost_m<T, 15>(a, b, p, s); break;
+        case 16: if constexpr (16 <= MAXW) return ghost_m<T, 16>(a, b, p, s); break;
     }
     return T(0);
 }
@@ -85,7 +86,7 @@ __device__ __forceinline__ T row_nk(const double* w, int p0, const T* __restrict
     return acc;
 }
 
-template <typename T>
+template <typename T, int MAXW = 16>
 __device__ __forceinline__ T row_eval(const ShellRow& R, const T* __restrict__ line, int64_t s, int L2, T gl, T gr) {
     switch (R.nk) {
         case 1: return row_nk<T, 1>(R.w, R.p0, line, s, L2, gl, gr);
@@ -96,28 +97,28 @@ __device__ __forceinline__ T row_eval(const ShellRow& R, const T* __restrict__ l
         case 6: return row_nk<T, 6>(R.w, R.p0, line, s, L2, gl, gr);
         case 7: return row_nk<T, 7>(R.w, R.p0, line, s, L2, gl, gr);
         case 8: return row_nk<T, 8>(R.w, R.p0, line, s, L2, gl, gr);
-        case 9: return row_nk<T, 9>(R.w, R.p0, line, s, L2, gl, gr);
-        case 10: return row_nk<T, 10>(R.w, R.p0, line, s, L2, gl, gr);
-        case 11: return row_nk<T, 11>(R.w, R.p0, line, s, L2, gl, gr);
-        case 12: return row_nk<T, 12>(R.w, R.p0, line, s, L2, gl, gr);
-        case 13: return row_nk<T, 13>(R.w, R.p0, line, s, L2, gl, gr);
-        case 14: return row_nk<T, 14>(R.w, R.p0, line, s, L2, gl, gr);
-        case 15: return row_nk<T, 15>(R.w, R.p0, line, s, L2, gl, gr);
-        case 16: return row_nk<T, 16>(R.w, R.p0, line, s, L2, gl, gr);
+        case 9: if constexpr (9 <= MAXW) return row_nk<T, 9>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 10: if constexpr (10 <= MAXW) return row_nk<T, 10>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 11: if constexpr (11 <= MAXW) return row_nk<T, 11>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 12: if constexpr (12 <= MAXW) return row_nk<T, 12>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 13: if constexpr (13 <= MAXW) return row_nk<T, 13>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 14: if constexpr (14 <= MAXW) return row_nk<T, 14>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 15: if constexpr (15 <= MAXW) return row_nk<T, 15>(R.w, R.p0, line, s, L2, gl, gr); break;
+        case 16: if constexpr (16 <= MAXW) return row_nk<T, 16>(R.w, R.p0, line, s, L2, gl, gr); break;
     }
     return T(0);
 }
 
 // Boundary row i (1-based) of a term on the line starting at `line`, with
 // its own ghosts (edges and corners of the shell).
-template <typename T>
+template <typename T, int MAXW = 16>
 __device__ __forceinline__ T shell_row(const ShellTerm& S, const T* __restrict__ line, int64_t s, int i) {
     const int r = i <= S.nlo ? i - 1 : S.nlo + (i - (S.len - S.nhi + 1));
     const ShellRow& R = S.row[r];
     const int L2 = S.len + 2;
-    const T gl = R.p0 == 1 ? shell_ghost<T>(S, line, s, true) : T(0);
-    const T gr = R.p0 + R.nk - 1 == L2 ? shell_ghost<T>(S, line, s, false) : T(0);
-    return row_eval<T>(R, line, s, L2, gl, gr);
+    const T gl = R.p0 == 1 ? shell_ghost<T, MAXW>(S, line, s, true) : T(0);
+    const T gr = R.p0 + R.nk - 1 == L2 ? shell_ghost<T, MAXW>(S, line, s, false) : T(0);
+    return row_eval<T, MAXW>(R, line, s, L2, gl, gr);
 }
 
 // Band taps of axis a at idx (interior row along a), as eval_term's band

@@ -234,7 +234,7 @@ struct ShellLines {
     int small;           // 2 * (l2 + l1 + l0) < 2^31
 };
 
-template <typename T, int NT, int A>
+template <typename T, int NT, int A, int MAXW>
 __device__ __forceinline__ void shell_line(const ShellTerm* S, const UniPlan& U, const T* __restrict__ u,
                                            T* __restrict__ du, int ow, int e, int64_t c0, int64_t c1, int64_t c2,
                                            int64_t nx, int64_t sxy) {
@@ -252,8 +252,8 @@ __device__ __forceinline__ void shell_line(const ShellTerm* S, const UniPlan& U,
         need_l |= R.p0 == 1;
         need_r |= R.p0 + R.nk - 1 == L2;
     }
-    const T gl = need_l ? shell_ghost<T>(SA, line, st[A], true) : T(0);
-    const T gr = need_r ? shell_ghost<T>(SA, line, st[A], false) : T(0);
+    const T gl = need_l ? shell_ghost<T, MAXW>(SA, line, st[A], true) : T(0);
+    const T gr = need_r ? shell_ghost<T, MAXW>(SA, line, st[A], false) : T(0);
 #pragma unroll 1
     for (int r = 0; r < nrows; ++r) {
         const ShellRow& R = SA.row[(e ? SA.nlo : 0) + r];
@@ -264,12 +264,12 @@ __device__ __forceinline__ void shell_line(const ShellTerm* S, const UniPlan& U,
         for (int b = 0; b < NT; ++b) {
             T v;
             if (b == A) {
-                v = row_eval<T>(R, line, st[A], L2, gl, gr);
+                v = row_eval<T, MAXW>(R, line, st[A], L2, gl, gr);
             } else {
                 const int ib = (int)c[b] + 1;
                 v = (ib >= U.t[b].flo && ib <= U.t[b].fhi)
                         ? shell_band<T>(U.t[b], U.radius, u, idx, st[b])
-                        : shell_row<T>(S[b], u + idx - c[b] * st[b], st[b], ib);
+                        : shell_row<T, MAXW>(S[b], u + idx - c[b] * st[b], st[b], ib);
             }
             acc = (b == 0) ? v : acc + v;
         }
@@ -278,7 +278,7 @@ __device__ __forceinline__ void shell_line(const ShellTerm* S, const UniPlan& U,
     }
 }
 
-template <typename T, int NT>
+template <typename T, int NT, int MAXW>
 __global__ void __launch_bounds__(256) k_shell_lines(const __grid_constant__ ShellBox B,
                                                      const __grid_constant__ ShellLines SL,
                                                      const __grid_constant__ UniPlan U,
@@ -302,18 +302,18 @@ __global__ void __launch_bounds__(256) k_shell_lines(const __grid_constant__ She
             const int e = q >= SL.l2;
             q -= e * SL.l2;
             const int64_t yy = SL.small ? (int64_t)fast_div((uint32_t)q, SL.d_nx) : q / nx;
-            if constexpr (NT == 3) shell_line<T, NT, 2>(S, U, u, du, ow, e, q - yy * nx, yy, 0, nx, sxy);
+            if constexpr (NT == 3) shell_line<T, NT, 2, MAXW>(S, U, u, du, ow, e, q - yy * nx, yy, 0, nx, sxy);
         } else if ((q -= 2 * SL.l2) < 2 * SL.l1) {
             const int e = q >= SL.l1;
             q -= e * SL.l1;
             const int64_t zi = SL.small ? (int64_t)fast_div((uint32_t)q, SL.d_nx) : q / nx;
-            shell_line<T, NT, 1>(S, U, u, du, ow, e, q - zi * nx, 0, B.lo[2] + zi, nx, sxy);
+            shell_line<T, NT, 1, MAXW>(S, U, u, du, ow, e, q - zi * nx, 0, B.lo[2] + zi, nx, sxy);
         } else {
             q -= 2 * SL.l1;
             const int e = q >= SL.l0;
             q -= e * SL.l0;
             const int64_t zi = SL.small ? (int64_t)fast_div((uint32_t)q, SL.d_iy) : q / iy;
-            shell_line<T, NT, 0>(S, U, u, du, ow, e, 0, B.lo[1] + (q - zi * iy), B.lo[2] + zi, nx, sxy);
+            shell_line<T, NT, 0, MAXW>(S, U, u, du, ow, e, 0, B.lo[1] + (q - zi * iy), B.lo[2] + zi, nx, sxy);
         }
     }
 }
@@ -483,7 +483,9 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         B.d_nxo = fd(nx - ix);
     }
     const bool have_lines = sp && sp_dev && B.lo[0] <= B.hi[0] && B.lo[1] <= B.hi[1] && B.lo[2] <= B.hi[2];
-    if (have_lines && (mode == DEO_SHELL_CONCURRENT || (mode == DEO_SHELL_ALONE && sizeof(T) == 8))) {
+    // Float64: the line kernel (FP64-bound; beside the interior kernel one CTA per SM is what fits);
+    // Float32: the face kernel (a shared-memory box per tile; fits beside the interior kernel)
+    if (have_lines && sizeof(T) == 8) {
         ShellLines SL{};
         const int64_t niz = NT == 3 ? iz : 1;
         SL.l2 = NT == 3 ? nx * ny : 0;
@@ -493,12 +495,16 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         SL.d_nx = make_fastdiv((uint32_t)std::max<int64_t>(nx, 1));
         SL.d_iy = make_fastdiv((uint32_t)std::max<int64_t>(iy, 1));
         const int64_t lines = 2 * (SL.l2 + SL.l1 + SL.l0);
-        static int64_t g = 0;
-        if (!g) g = shell_grid(k_shell_lines<T, NT>, 1LL << 40);
-        // beside the interior kernel: one CTA per SM (fits next to its CTAs); alone: a full grid
-        const int64_t grid = std::min<int64_t>(mode == DEO_SHELL_CONCURRENT ? deo_k_num_sms() : g, (lines + 255) / 256);
-        k_shell_lines<T, NT><<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(B, SL, *up, sp_dev, (const T*)u,
-                                                                                (T*)du, ow);
+        auto go = [&](auto kernel) {
+            static int64_t g = 0;
+            if (!g) g = shell_grid(kernel, 1LL << 40);
+            // beside the interior kernel: one CTA per SM (fits next to its CTAs); alone: a full grid
+            const int64_t grid =
+                std::min<int64_t>(mode == DEO_SHELL_CONCURRENT ? deo_k_num_sms() : g, (lines + 255) / 256);
+            kernel<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(B, SL, *up, sp_dev, (const T*)u, (T*)du, ow);
+        };
+        if (sp->maxw <= 8) go(k_shell_lines<T, NT, 8>);
+        else go(k_shell_lines<T, NT, 16>);
         *kernel = "k_shell_lines";
         return (int)cudaGetLastError();
     }

@@ -418,6 +418,6 @@ def test_shell_kernels_bitwise_equal_generic(cuda, case, dtype):
         a = base.clone()
         p.apply(ud, a, overwrite=False)
         assert torch.equal(a, ref_acc), (conc, p.kernels)
-    # rows of 16-byte multiples take the TMA path (interior + shell); others one register-queue kernel
-    assert ("k_shell_lines" in seen) == ((shape[0] * (8 if dtype == "f64" else 4)) % 16 == 0)
+    # rows of 16-byte multiples take the TMA path (interior + shell kernel); others one register-queue kernel
+    assert bool(seen & {"k_shell_lines", "k_face"}) == ((shape[0] * (8 if dtype == "f64" else 4)) % 16 == 0)
     assert deo.device_status() == 0
