@@ -199,6 +199,13 @@ __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ 
     return ADJ ? acc : zero_fix(acc);
 }
 
+// Out-of-line copy for a kernel that evaluates a few boundary points with
+// the generic evaluator (the shell fallback).
+template <typename T>
+__device__ __noinline__ T eval_term_cold(const TermDev& t, const T* __restrict__ u, int64_t idx, int i) {
+    return eval_term<T>(t, u, idx, i);
+}
+
 template <typename T>
 __device__ __forceinline__ T uni_w(const UniTerm& t, int k);
 template <>

@@ -121,6 +121,12 @@ __device__ __forceinline__ T shell_row(const ShellTerm& S, const T* __restrict__
     return row_eval<T, MAXW>(R, line, s, L2, gl, gr);
 }
 
+// Out of line, for the rarely taken rows (edges and corners of the shell).
+template <typename T, int MAXW = 16>
+__device__ __noinline__ T shell_row_cold(const ShellTerm& S, const T* __restrict__ line, int64_t s, int i) {
+    return shell_row<T, MAXW>(S, line, s, i);
+}
+
 // Band taps of axis a at idx (interior row along a), as eval_term's band
 // path; H = the band's radius (<= 4).
 template <typename T>

@@ -127,9 +127,9 @@ __device__ __forceinline__ T face_point(const ShellTerm* S, const UniPlan& U, co
             const int w0 = low ? 0 : SB.len - SB.whi;
             const int w1 = low ? SB.wlo : SB.len;
             if (w0 >= org[b] && w1 <= org[b] + bd[b])  // the row's points are in the box
-                v = shell_row<T>(SB, pc - c[b] * sb[b], sb[b], ib);
+                v = shell_row_cold<T>(SB, pc - c[b] * sb[b], sb[b], ib);
             else
-                v = shell_row<T>(SB, u + gidx - c[b] * gst[b], gst[b], ib);
+                v = shell_row_cold<T>(SB, u + gidx - c[b] * gst[b], gst[b], ib);
         }
         acc = (b == 0) ? v : acc + v;
     }
@@ -269,7 +269,7 @@ __device__ __forceinline__ void shell_line(const ShellTerm* S, const UniPlan& U,
                 const int ib = (int)c[b] + 1;
                 v = (ib >= U.t[b].flo && ib <= U.t[b].fhi)
                         ? shell_band<T>(U.t[b], U.radius, u, idx, st[b])
-                        : shell_row<T, MAXW>(S[b], u + idx - c[b] * st[b], st[b], ib);
+                        : shell_row_cold<T, MAXW>(S[b], u + idx - c[b] * st[b], st[b], ib);
             }
             acc = (b == 0) ? v : acc + v;
         }
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(256) k_shell_generic(const __grid_constant__ S
         for (int a = 0; a < NT; ++a) {
             const int i = (int)crd[a] + 1;
             const T r = (i >= U.t[a].flo && i <= U.t[a].fhi) ? shell_band<T>(U.t[a], U.radius, u, idx, st[a])
-                                                             : eval_term<T>(P->t[a], u, idx, i);
+                                                             : eval_term_cold<T>(P->t[a], u, idx, i);
             acc = (a == 0) ? r : acc + r;
         }
         const T tot = zero_fix(acc);
