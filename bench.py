@@ -466,7 +466,7 @@ def run_batch(args):
     import torch
 
     import deo
-    inst = batch_instances()
+    inst = batch_instances(scale=args.size_scale)
     plans, us, fw, bw, ones = [], [], [], [], []
     g = torch.Generator(device="cuda").manual_seed(SEED)
     total = 0
@@ -478,11 +478,17 @@ def run_batch(args):
         plans.append(p); us.append(u); fw.append(deo.julia_array(shape)); bw.append(deo.julia_array(shape))
         ones.append(deo.julia_array(shape))
         total += int(np.prod(shape))
-    bf = deo.Batch(list(zip(plans, us, fw)))
-    ba = deo.Batch(list(zip(plans, fw, bw)), adjoint=True)
-    cfg_f = bf.autotune(os.path.join(ROOT, "gpurun_out", "autotune.cache") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else None)
-    cfg_a = ba.autotune()
+    if args.batch_config:  # fixed tile / CTAs per SM (e.g. for profiling), no autotuning
+        tile, ctas = (int(v) for v in args.batch_config.split(","))
+        bf = deo.Batch(list(zip(plans, us, fw)), tile=tile, ctas_per_sm=ctas)
+        ba = deo.Batch(list(zip(plans, fw, bw)), adjoint=True, tile=tile, ctas_per_sm=ctas)
+        cfg_f, cfg_a = bf.config, ba.config
+    else:
+        bf = deo.Batch(list(zip(plans, us, fw)))
+        ba = deo.Batch(list(zip(plans, fw, bw)), adjoint=True)
+        cfg_f = bf.autotune(os.path.join(ROOT, "gpurun_out", "autotune.cache") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else None)
+        cfg_a = ba.autotune()
 
     def batched():
         bf.run(True)
@@ -607,6 +613,7 @@ def main():
     ap.add_argument("--size-scale", type=float, default=1.0)
     ap.add_argument("--kmax", type=int, default=1000)
     ap.add_argument("--serve-baseline", action="store_true")
+    ap.add_argument("--batch-config", default="", help="tile,ctas_per_sm for the batch workload (skips autotuning)")
     args = ap.parse_args()
     if args.workload in ("line1d", "nonuniform2d", "batch", "serve"):
         import torch

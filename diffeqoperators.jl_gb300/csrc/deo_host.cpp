@@ -732,7 +732,7 @@ struct deo_plan {
     int use_tma = 1;     // DEO_OPT_TMA
     int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
     int timing = 0;      // DEO_OPT_LAUNCH_TIMING
-    int concurrent = -1;  // DEO_OPT_CONCURRENT_SHELL; -1: by dtype (Float32 on, Float64 off)
+    int concurrent = 1;  // DEO_OPT_CONCURRENT_SHELL
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     deo::ShellPlan* d_shell = nullptr;  // device copy of `shell` when shell.ok
     // concurrent shell: a side stream, fork/join events and the interior kernel's unit counter
@@ -1072,52 +1072,59 @@ static void mark(const deo_plan* p, int k, void* stream) {
     if (p->timing) cudaEventRecord(p->ev[k], static_cast<cudaStream_t>(stream));
 }
 
-// Interior kernel on the caller's stream; the boundary shell either after it
-// on the same stream (default), or (DEO_OPT_CONCURRENT_SHELL) on the plan's
-// side stream at the same time, joined back before the apply completes.  The
-// interior kernels claim their units from the plan's device counter (zeroed
-// on the stream before each launch), so they balance dynamically.
+// Laplacian-type plans: interior kernel on the caller's stream and the
+// boundary shell either after it on the same stream, or (DEO_OPT_CONCURRENT_SHELL,
+// default) on the plan's side stream at the same time, forked from and joined
+// back into the caller's stream.  The interior kernels claim their units from
+// a device counter (zeroed on the stream before each launch), so they balance
+// around the shell's CTAs.  Launch timing with a concurrent shell: ms[0] =
+// fork to the end of the interior kernel, ms[1] = the wait for the shell after it.
 static int launch_forward(const deo_plan* p, const void* u, void* du, int overwrite, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     mark(p, 0, stream);
     if (p->uni.enabled && p->fast_path) {
-        if (p->uni.lap && p->use_tma) {
-            const bool conc = (p->concurrent < 0 ? p->dev.dtype == DEO_F32 : p->concurrent != 0) && p->side && p->d_shell;
-            std::unique_lock<std::mutex> lk(p->apply_mu, std::defer_lock);
-            if (conc) {
-                lk.lock();
-                const cudaError_t e = cudaEventRecord(p->ev_fork, st);
-                if (e != cudaSuccess) return (int)e;
-            }
+        if (p->uni.lap && p->use_tma && deo_k_tma_ok(&p->uni, p->dev.dtype, u)) {
+            // overlap only pays beside an interior kernel that leaves the FP64 pipe free: the fixed-point
+            // kernel (Float64) or any Float32 kernel; the FP64-bound interiors run the shell after them
+            const bool fx = p->dev.dtype == DEO_F64 && p->exact_sums == 1 && p->uni.fx && p->uni.radius <= 3;
+            const bool conc = p->concurrent && p->side && p->d_shell && (p->dev.dtype == DEO_F32 || fx);
             const char* k = "";
+            const char* k2 = "";
             // a counter of its own for this launch (applies of one plan may run on several streams at once)
             unsigned int* sched = p->d_sched ? p->d_sched + (p->sched_slot.fetch_add(1) % kSchedSlots) : nullptr;
-            const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums, stream,
-                                          &k, sched);
-            if (e != (int)cudaErrorNotSupported) {
+            if (conc) {
+                // the shell first, on the side stream, so that its CTAs hold a place on every SM; then the
+                // interior on the caller's stream; the caller's stream waits for the shell at the end
+                std::lock_guard<std::mutex> lk(p->apply_mu);
+                cudaError_t c = cudaEventRecord(p->ev_fork, st);
+                if (c == cudaSuccess) c = cudaStreamWaitEvent(p->side, p->ev_fork, 0);
+                if (c != cudaSuccess) return (int)c;
+                int e2 = deo_k_apply_shell(&p->uni, &p->shell, p->d_shell, DEO_SHELL_CONCURRENT, p->d_plan,
+                                           p->dev.dtype, u, du, overwrite, p->side, &k2);
+                if (e2) return e2;
+                c = cudaEventRecord(p->ev_join, p->side);
+                if (c != cudaSuccess) return (int)c;
+                const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
+                                              stream, &k, sched);
+                mark(p, 1, stream);
+                c = cudaStreamWaitEvent(st, p->ev_join, 0);
+                if (e) return e;  // (cudaErrorNotSupported cannot occur: the tensor-map rules were checked)
+                if (c != cudaSuccess) return (int)c;
+            } else {
+                const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
+                                              stream, &k, sched);
                 if (e) return e;
                 mark(p, 1, stream);
-                p->last_kernel = k;
-                p->ev_launches = 2;
-                const char* k2 = "";
-                int e2;
-                if (conc) {
-                    cudaError_t c = cudaStreamWaitEvent(p->side, p->ev_fork, 0);
-                    if (c != cudaSuccess) return (int)c;
-                    e2 = deo_k_apply_shell(&p->uni, &p->shell, p->d_shell, DEO_SHELL_CONCURRENT, p->d_plan,
-                                           p->dev.dtype, u, du, overwrite, p->side, &k2);
-                    if (e2) return e2;
-                    c = cudaEventRecord(p->ev_join, p->side);
-                    if (c == cudaSuccess) c = cudaStreamWaitEvent(st, p->ev_join, 0);
-                    if (c != cudaSuccess) return (int)c;
-                } else {
-                    e2 = deo_k_apply_shell(&p->uni, p->d_shell ? &p->shell : nullptr, p->d_shell, DEO_SHELL_ALONE,
-                                           p->d_plan, p->dev.dtype, u, du, overwrite, stream, &k2);
-                }
-                p->last_kernel2 = k2;
-                mark(p, 2, stream);
-                return e2;
+                const int e2 = deo_k_apply_shell(&p->uni, p->d_shell ? &p->shell : nullptr, p->d_shell,
+                                                 DEO_SHELL_ALONE, p->d_plan, p->dev.dtype, u, du, overwrite, stream,
+                                                 &k2);
+                if (e2) return e2;
             }
+            p->last_kernel = k;
+            p->last_kernel2 = k2;
+            p->ev_launches = 2;
+            mark(p, 2, stream);
+            return 0;
         }
         p->last_kernel = p->uni.lap ? "k_lap" : "k_uni3";
         p->last_kernel2 = "";
@@ -1161,8 +1168,8 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
         case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
         case DEO_OPT_CONCURRENT_SHELL:
-            return (p->concurrent < 0 ? p->dev.dtype == DEO_F32 : p->concurrent != 0) && p->side && p->d_shell &&
-                   p->uni.enabled && p->uni.lap;
+            return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap &&
+                   (p->dev.dtype == DEO_F32 || (p->exact_sums == 1 && p->uni.fx && p->uni.radius <= 3));
     }
     return -1;
 }

@@ -214,5 +214,7 @@ extern "C" int deo_k_read_status(unsigned int* status);
 extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
                                  int bz);
 extern "C" int deo_k_read_shell_status(unsigned int* status);
+// 1 if deo_k_apply_tma can run on u (tensor-map alignment rules).
+extern "C" int deo_k_tma_ok(const deo::UniPlan* up, int dtype, const void* u);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
                                  unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);

@@ -147,22 +147,6 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(16) ShellTerm S[NT];
     __shared__ __align__(8) uint64_t mbar;
-    const int blk = blockIdx.x;
-    const int A = blk < G.cta0[1] ? 2 : (blk < G.cta0[2] ? 1 : 0);
-    const int b1 = A == 0 ? 1 : 0, b2 = A == 2 ? 1 : 2;
-    const int local = blk - G.cta0[2 - A];
-    const int per_end = G.tiles1[A] * G.tiles2[A];
-    const int e = local / per_end;
-    const int rem = local - e * per_end;
-    const int tt2 = rem / G.tiles1[A], tt1 = rem - tt2 * G.tiles1[A];
-    const int c1 = G.r1[A] + tt1 * G.tw1[A], c2 = G.r2[A] + tt2 * G.tw2[A];
-    int org[3], bd[3];
-    org[A] = G.orgA[A][e];
-    org[b1] = c1 - G.halo[b1];
-    org[b2] = c2 - G.halo[b2];
-    bd[0] = G.box[A][0];
-    bd[1] = G.box[A][1];
-    bd[2] = G.box[A][2];
     if (threadIdx.x == 0) {
         mbar_init(&mbar, 1);
         fence_mbar_init();
@@ -173,50 +157,70 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
         for (int q = threadIdx.x; q < (int)(NT * sizeof(ShellTerm) / 8); q += blockDim.x) dst[q] = __ldg(src + q);
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&mbar, (uint32_t)G.box_bytes[A]);
-        tma_load_3d(smem, A == 0 ? &m0 : (A == 1 ? &m1 : &m2), &mbar, org[0], org[1], org[2]);
-    }
-    bool timeout = false;
-    {
-        uint32_t it = 0;
-        while (!mbar_try_wait(&mbar, 0)) {
-            if (++it > (1u << 22)) {
-                timeout = true;
-                break;
-            }
-        }
-    }
-    if (__syncthreads_or(timeout)) {
-        if (threadIdx.x == 0) {
-            atomicOr(&g_deo_shell_status, 1u);
-            for (uint32_t it = 0; it < (1u << 22); ++it)  // the copy may still be in flight
-                if (mbar_try_wait(&mbar, 0)) break;
-        }
-        return;
-    }
     const T* box = reinterpret_cast<const T*>(smem);
-    const int64_t sb[3] = {1, bd[0], (int64_t)bd[0] * bd[1]};
     const int64_t nx = G.n[0], sxy = (int64_t)G.n[0] * G.n[1];
     const int64_t gst[3] = {1, nx, sxy};
-    const ShellTerm& SA = S[A];
-    const int nrows = e ? SA.nhi : SA.nlo;
-    const int cA0 = e ? SA.len - SA.nhi : 0;
-    const int tw1 = G.tw1[A], tw2 = G.tw2[A];
-    const int npts = nrows * tw1 * tw2;
-    for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-        const int r = q / (tw1 * tw2);
-        const int q2 = q - r * tw1 * tw2;
-        const int p2 = q2 / tw1, p1 = q2 - p2 * tw1;
-        int c[3];
-        c[A] = cA0 + r;
-        c[b1] = c1 + p1;
-        c[b2] = c2 + p2;
-        if (c[b1] >= G.e1[A] || c[b2] >= G.e2[A]) continue;
-        const int64_t gidx = c[0] + c[1] * nx + (int64_t)c[2] * sxy;
-        const T* pc = box + (int64_t)(c[2] - org[2]) * sb[2] + (int64_t)(c[1] - org[1]) * sb[1] + (c[0] - org[0]);
-        const T tot = face_point<T, NT>(S, U, pc, c, org, bd, sb, u, gidx, gst);
-        du[gidx] = ow ? tot : tot + du[gidx];
+    // tiles blockIdx.x, + gridDim.x, ...: one box each; the mbarrier's phase flips per tile
+    uint32_t phase = 0;
+    for (int blk = blockIdx.x; blk < G.cta0[3]; blk += gridDim.x, phase ^= 1u) {
+        const int A = blk < G.cta0[1] ? 2 : (blk < G.cta0[2] ? 1 : 0);
+        const int b1 = A == 0 ? 1 : 0, b2 = A == 2 ? 1 : 2;
+        const int local = blk - G.cta0[2 - A];
+        const int per_end = G.tiles1[A] * G.tiles2[A];
+        const int e = local / per_end;
+        const int rem = local - e * per_end;
+        const int tt2 = rem / G.tiles1[A], tt1 = rem - tt2 * G.tiles1[A];
+        const int c1 = G.r1[A] + tt1 * G.tw1[A], c2 = G.r2[A] + tt2 * G.tw2[A];
+        int org[3], bd[3];
+        org[A] = G.orgA[A][e];
+        org[b1] = c1 - G.halo[b1];
+        org[b2] = c2 - G.halo[b2];
+        bd[0] = G.box[A][0];
+        bd[1] = G.box[A][1];
+        bd[2] = G.box[A][2];
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&mbar, (uint32_t)G.box_bytes[A]);
+            tma_load_3d(smem, A == 0 ? &m0 : (A == 1 ? &m1 : &m2), &mbar, org[0], org[1], org[2]);
+        }
+        bool timeout = false;
+        {
+            uint32_t it = 0;
+            while (!mbar_try_wait(&mbar, phase)) {
+                if (++it > (1u << 22)) {
+                    timeout = true;
+                    break;
+                }
+            }
+        }
+        if (__syncthreads_or(timeout)) {
+            if (threadIdx.x == 0) {
+                atomicOr(&g_deo_shell_status, 1u);
+                for (uint32_t it = 0; it < (1u << 22); ++it)  // the copy may still be in flight
+                    if (mbar_try_wait(&mbar, phase)) break;
+            }
+            return;
+        }
+        const int64_t sb[3] = {1, bd[0], (int64_t)bd[0] * bd[1]};
+        const ShellTerm& SA = S[A];
+        const int nrows = e ? SA.nhi : SA.nlo;
+        const int cA0 = e ? SA.len - SA.nhi : 0;
+        const int tw1 = G.tw1[A], tw2 = G.tw2[A];
+        const int npts = nrows * tw1 * tw2;
+        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
+            const int r = q / (tw1 * tw2);
+            const int q2 = q - r * tw1 * tw2;
+            const int p2 = q2 / tw1, p1 = q2 - p2 * tw1;
+            int c[3];
+            c[A] = cA0 + r;
+            c[b1] = c1 + p1;
+            c[b2] = c2 + p2;
+            if (c[b1] >= G.e1[A] || c[b2] >= G.e2[A]) continue;
+            const int64_t gidx = c[0] + c[1] * nx + (int64_t)c[2] * sxy;
+            const T* pc = box + (int64_t)(c[2] - org[2]) * sb[2] + (int64_t)(c[1] - org[1]) * sb[1] + (c[0] - org[0]);
+            const T tot = face_point<T, NT>(S, U, pc, c, org, bd, sb, u, gidx, gst);
+            du[gidx] = ow ? tot : tot + du[gidx];
+        }
+        __syncthreads();  // every thread is done with the box before the next copy overwrites it
     }
 }
 
@@ -360,9 +364,13 @@ static int64_t shell_grid(K kernel, int64_t total) {
 
 // Face grid and the three tensor maps; returns cudaErrorNotSupported when a
 // box would exceed the TMA / shared-memory limits (the caller falls back).
+// small: one persistent 128-thread CTA per SM over 32 x 8 tiles (16 x 8 on the
+// x faces), launched before the Float64 interior kernel so that it holds its
+// place on every SM beside the interior's CTAs; else 256 threads, one CTA per
+// 32 x 32 tile.
 template <typename T, int NT>
 static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* sp_dev, const void* u, void* du, int ow,
-                       cudaStream_t st) {
+                       cudaStream_t st, bool small) {
     const int ES = (int)sizeof(T);
     const int al = 16 / ES;  // TMA: x coordinates and x extents in multiples of 16 bytes
     FaceGrid G{};
@@ -393,8 +401,8 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
         };
         range(b1, G.r1[A], G.e1[A]);
         range(b2, G.r2[A], G.e2[A]);
-        G.tw1[A] = std::min(32, G.e1[A] - G.r1[A]);
-        G.tw2[A] = (b2 < NT) ? std::min(32, G.e2[A] - G.r2[A]) : 1;
+        G.tw1[A] = std::min(small && b1 == 1 ? 16 : 32, G.e1[A] - G.r1[A]);
+        G.tw2[A] = (b2 < NT) ? std::min(small ? 8 : 32, G.e2[A] - G.r2[A]) : 1;
         G.tiles1[A] = (G.e1[A] - G.r1[A] + G.tw1[A] - 1) / G.tw1[A];
         G.tiles2[A] = (G.e2[A] - G.r2[A] + G.tw2[A] - 1) / G.tw2[A];
         // box along A: the points both ends' rows read
@@ -438,12 +446,16 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
     if (NT < 3) maps[2] = maps[0];
     static size_t smem_set = 0;
     if (smem_max > smem_set) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k_face<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        cudaError_t e = cudaFuncSetAttribute(k_face<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        // the interior kernels run with the largest shared-memory carveout; asking for the same lets this
+        // kernel's CTAs share their SMs
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_face<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return (int)e;
         smem_set = smem_max;
     }
-    k_face<T, NT><<<(unsigned)cta, 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u,
+    k_face<T, NT><<<(unsigned)(small ? std::min(cta, deo_k_num_sms()) : cta), small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u,
                                                           (T*)du, ow);
     return (int)cudaGetLastError();
 }
@@ -483,9 +495,10 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         B.d_nxo = fd(nx - ix);
     }
     const bool have_lines = sp && sp_dev && B.lo[0] <= B.hi[0] && B.lo[1] <= B.hi[1] && B.lo[2] <= B.hi[2];
-    // Float64: the line kernel (FP64-bound; beside the interior kernel one CTA per SM is what fits);
-    // Float32: the face kernel (a shared-memory box per tile; fits beside the interior kernel)
-    if (have_lines && sizeof(T) == 8) {
+    // Float64 alone: the line kernel (FP64-bound, full grid).  Otherwise the face kernel: a shared-memory
+    // box per tile; beside a Float64 interior kernel in small CTAs that fit next to its CTAs, so that the
+    // shell's FP64 work overlaps the interior's integer work.
+    if (have_lines && sizeof(T) == 8 && mode == DEO_SHELL_ALONE) {
         ShellLines SL{};
         const int64_t niz = NT == 3 ? iz : 1;
         SL.l2 = NT == 3 ? nx * ny : 0;
@@ -509,7 +522,8 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         return (int)cudaGetLastError();
     }
     if (sp && sp_dev) {
-        const int e = face_launch<T, NT>(up, sp, sp_dev, u, du, ow, st);
+        // Float64 interiors are long: a small persistent shell beside them; Float32 interiors are short: a full grid
+        const int e = face_launch<T, NT>(up, sp, sp_dev, u, du, ow, st, mode == DEO_SHELL_CONCURRENT && sizeof(T) == 8);
         if (e != (int)cudaErrorNotSupported) {
             *kernel = "k_face";
             return e;

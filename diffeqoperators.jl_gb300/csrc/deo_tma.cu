@@ -962,6 +962,14 @@ static bool make_map(CUtensorMap& map, const void* u, int es, int64_t nx, int64_
     return make_map3(map, u, es, nx, ny, nz, bx, by, 1);
 }
 
+// 1 if the TMA path can run on u (the tensor-map rules: 16-byte aligned base,
+// rows of a 16-byte multiple, sizes below 2^30).
+extern "C" int deo_k_tma_ok(const UniPlan* up, int dtype, const void* u) {
+    const int64_t es = dtype == 0 ? 8 : 4;
+    return up->lap && !((uintptr_t)u & 15) && !((up->n[0] * es) & 15) && up->n[0] <= (1 << 30) &&
+           up->n[1] <= (1 << 30) && up->n[2] <= (1 << 30);
+}
+
 extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
                                  int bz) {
     return make_map3(*reinterpret_cast<CUtensorMap*>(map), u, es, nx, ny, nz, bx, by, bz) ? 0

@@ -190,9 +190,11 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *   DEO_OPT_CONCURRENT_SHELL: 1 evaluates the boundary shell of a
  *     Laplacian-type plan on the TMA path on a plan-owned side stream at the
  *     same time as the interior (forked from and joined back into the
- *     caller's stream, so the apply stays stream-ordered); 0 runs it after
- *     the interior on the caller's stream.  Default: 1 for Float32 plans (the
- *     shell's CTAs fit beside the interior kernel's), 0 for Float64.
+ *     caller's stream, so the apply stays stream-ordered; the shell's CTAs
+ *     are sized to fit beside the interior kernel's).  It applies to Float32
+ *     plans and to the fixed-point Float64 interior (whose FP64 pipe is free
+ *     for the shell); other Float64 interiors are FP64-bound and run the
+ *     shell after them.  0 runs the shell after the interior always.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
