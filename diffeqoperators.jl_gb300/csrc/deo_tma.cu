@@ -570,6 +570,26 @@ __device__ __forceinline__ double fx_round(long long hi_s, unsigned long long lo
         (long long)(((unsigned long long)neg << 63) | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFULL)));
 }
 
+// 128-bit accumulator (hi, lo) += a * b for signed 64-bit a, b: one 64 x 64
+// -> 128 product (mul.lo / mul.hi) and a carry-propagating add.
+// Arithmetic shift right by d >= 0; PTX clamps shift amounts above 64 to 64
+// (the result is then 0 or -1), so no clamp is needed.
+__device__ __forceinline__ long long sar64(long long m, int d) {
+    long long r;
+    asm("shr.s64 %0, %1, %2;" : "=l"(r) : "l"(m), "r"(d));
+    return r;
+}
+
+struct Acc128 {
+    unsigned long long lo;
+    long long hi;
+};
+__device__ __forceinline__ void mad128(Acc128& A, long long a, long long b) {
+    const unsigned long long plo = (unsigned long long)(a * b);
+    const long long phi = __mul64hi(a, b);
+    asm("add.cc.u64 %0, %0, %2;\n\taddc.s64 %1, %1, %3;" : "+l"(A.lo), "+l"(A.hi) : "l"(plo), "l"(phi));
+}
+
 template <int H, int NT>
 __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensorMap tmap,
                                                 const __grid_constant__ UniPlan U, const LapGrid g,
@@ -697,19 +717,20 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
             bool ok = E < 2047;
             double total = 0.0;
             if (ok) {
-                __int128 A = (__int128)((long long)NT * (m0 >> min(E - e0, 63))) * U.fx_w[H];
+                Acc128 A{0ULL, 0LL};
+                mad128(A, (long long)NT * sar64(m0, E - e0), U.fx_w[H]);
 #pragma unroll
                 for (int kk = 1; kk <= H; ++kk) {
                     long long sm = 0, sp = 0;
 #pragma unroll
                     for (int a = 0; a < NT; ++a) {
-                        sm += mt[kk - 1][a] >> min(E - et[kk - 1][a], 63);
-                        sp += mt[H + kk - 1][a] >> min(E - et[H + kk - 1][a], 63);
+                        sm += sar64(mt[kk - 1][a], E - et[kk - 1][a]);
+                        sp += sar64(mt[H + kk - 1][a], E - et[H + kk - 1][a]);
                     }
-                    A += (__int128)sm * U.fx_w[H - kk];
-                    A += (__int128)sp * U.fx_w[H + kk];
+                    mad128(A, sm, U.fx_w[H - kk]);
+                    mad128(A, sp, U.fx_w[H + kk]);
                 }
-                total = fx_round((long long)(A >> 64), (unsigned long long)A, ebase0 + E, ok);
+                total = fx_round(A.hi, A.lo, ebase0 + E, ok);
             }
             const int64_t idx = (int64_t)z * sxy + col;
             if (!ok) {
