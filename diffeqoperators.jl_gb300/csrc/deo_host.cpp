@@ -547,6 +547,30 @@ extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
     return DEO_OK;
 }
 
+// BandedMatrix(L): the reference's bandwidths (concretization.jl:123-128 centred,
+// :794-890 upwind) and the entries of Array(L) in band storage.
+extern "C" deo_status deo_operator_banded(const deo_operator* op, int* l, int* u, double* data) {
+    if (!op || !l || !u) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *l = op->wind ? op->stl - 2 : op->bstl - 3;
+    *u = op->wind ? op->stl : op->bstl - 1;
+    if (!data) return DEO_OK;
+    const long N = op->len, rows = *l + *u + 1;
+    std::vector<double> M((size_t)N * (N + 2));
+    deo_status s = deo_operator_array(op, M.data());
+    if (s != DEO_OK) return s;
+    std::fill(data, data + rows * (N + 2), 0.0);
+    for (long j = 1; j <= N + 2; ++j)
+        for (long i = 1; i <= N; ++i) {
+            const double v = M[(size_t)(j - 1) * N + (i - 1)];
+            const long b = *u + i - j;  // band row of entry (i, j)
+            if (b >= 0 && b < rows) data[(size_t)(j - 1) * rows + b] = v;
+            else if (v != 0.0)
+                return fail(DEO_ERR_BAD_SHAPE, "entry (%ld, %ld) of Array(L) lies outside the bands (%d, %d)", i, j,
+                            *l, *u);
+        }
+    return DEO_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Row-table compiler.  build_row() resolves, for output row i, which branch
 // of the reference's convolve_* loops runs and returns its window and

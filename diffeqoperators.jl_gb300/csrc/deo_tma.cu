@@ -782,7 +782,8 @@ struct QCfg {
     static constexpr int PLANE = BX * BY;
     static constexpr int PLANE_BYTES = PLANE * ES;
     static constexpr int SLOT = ((PLANE_BYTES + 127) / 128) * 128;
-    static constexpr int P = 8;  // ring slots (>= H + 2)
+    // ring slots (>= H + 2, a power of two): 4 for Float32 at H <= 2 (more CTAs per SM), else 8
+    static constexpr int P = (ES == 4 && H + 2 <= 4) ? 4 : 8;
     static constexpr int SMEM = P * SLOT;
 };
 

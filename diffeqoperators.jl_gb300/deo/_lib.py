@@ -100,6 +100,7 @@ def lib():
     proto("deo_operator_clone", st, _vp, C.POINTER(_vp))
     proto("deo_operator_destroy", None, _vp)
     proto("deo_operator_array", st, _vp, _dp)
+    proto("deo_operator_banded", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), _dp)
     proto("deo_robin_bc", st, _dp, _dp, _dp, C.c_int, C.c_int, C.POINTER(BCStruct))
     proto("deo_general_bc", st, _dp, C.c_int, _dp, C.c_int, _dp, C.c_int, C.c_int, C.POINTER(BCStruct))
     proto("deo_dirichlet_bc", st, C.c_double, C.c_double, C.POINTER(BCStruct))
@@ -147,7 +148,7 @@ EXPORTED = [
     "deo_last_error", "deo_abi_version", "deo_calculate_weights", "deo_centered_difference",
     "deo_upwind_difference", "deo_operator_from_tables", "deo_operator_describe",
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
-    "deo_operator_destroy", "deo_operator_array", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
+    "deo_operator_destroy", "deo_operator_array", "deo_operator_banded", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",

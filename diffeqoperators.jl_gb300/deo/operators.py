@@ -214,10 +214,15 @@ class DerivativeOperator:
         return M
 
     def banded(self):
-        """BandedMatrix(L) data: (matrix, (lower, upper)) with the reference's
-        bandwidths (bstl-3, bstl-1) for centred operators (concretization.jl:123-128)."""
-        bstl = self.boundary_stencil_length
-        return self.array(), (bstl - 3, bstl - 1)
+        """BandedMatrix(L) (concretization.jl:123-128 centred, :794-890 upwind):
+        (data, (lower, upper)) with the reference's bandwidths and data the
+        (lower+upper+1) x (len+2) band storage (entry (i, j) at row upper+i-j
+        of column j, 0-based here), BandedMatrices.jl's `bandeddata` layout."""
+        lo, up = C.c_int(), C.c_int()
+        check(L.lib().deo_operator_banded(self._h, C.byref(lo), C.byref(up), None))
+        data = np.zeros((lo.value + up.value + 1, self.len + 2), order="F")
+        check(L.lib().deo_operator_banded(self._h, C.byref(lo), C.byref(up), data.ctypes.data_as(_dp)))
+        return data, (lo.value, up.value)
 
 
 class DimensionMismatch(DeoShapeError):

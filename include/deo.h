@@ -109,6 +109,12 @@ deo_status deo_operator_clone(const deo_operator* op, deo_operator** out);
 void deo_operator_destroy(deo_operator* op);
 /* Array(L) (concretization.jl:8-52 centred, :556-671 upwind): len x (len+2), column-major. */
 deo_status deo_operator_array(const deo_operator* op, double* out);
+/* BandedMatrix(L) (concretization.jl:123-128 centred, :794-890 upwind): *l, *u receive the
+ * reference's bandwidths ((bstl-3, bstl-1) centred, (stl-2, stl) upwind); data (may be null)
+ * receives the (l+u+1) x (len+2) band storage, column-major, with entry (i, j) of Array(L)
+ * (1-based) at row u+i-j of column j -- BandedMatrices.jl's `bandeddata` layout.
+ * DEO_ERR_BAD_SHAPE if a nonzero of Array(L) lies outside those bands. */
+deo_status deo_operator_banded(const deo_operator* op, int* l, int* u, double* data);
 
 /* ------------------------------------------------------------------------
  * Boundary conditions: the affine ghost map of an AffineBC

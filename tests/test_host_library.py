@@ -145,3 +145,35 @@ def test_fast_division_constants():
         for n in ns:
             if 0 <= n < (1 << 31):
                 assert lib.deo_fastdiv_probe(n, d) == n // d, (n, d)
+
+
+def _from_band(data, lo, up, n):
+    M = np.zeros((n, n + 2))
+    for j in range(n + 2):
+        for b in range(lo + up + 1):
+            i = b - up + j
+            if 0 <= i < n:
+                M[i, j] = data[b, j]
+    return M
+
+
+@pytest.mark.parametrize("kind,d,a", [("c", d, a) for d in (1, 2, 3, 4) for a in (2, 4, 6)] +
+                         [("u", d, a) for d in (1, 2, 3) for a in (1, 2, 3)])
+@pytest.mark.parametrize("grid", ["uniform", "nonuniform"])
+def test_banded_matrix_export(kind, d, a, grid):
+    """BandedMatrix(L): the reference's bandwidths ((bstl-3, bstl-1) centred,
+    concretization.jl:126; (stl-2, stl) upwind, :802) and the entries of
+    Array(L) in band storage, bit for bit the oracle's Array(L)."""
+    n = 32
+    dx = 1.0 / 33 if grid == "uniform" else np.random.default_rng(d * 7 + a).uniform(0.5, 1.5, n + 1) / n
+    if kind == "c":
+        P, Q = deo.CenteredDifference(d, a, dx, n), O.centered(d, a, dx, n)
+        want = (P.boundary_stencil_length - 3, P.boundary_stencil_length - 1)
+    else:
+        c = np.random.default_rng(3).uniform(-1, 1, n)
+        P, Q = deo.UpwindDifference(d, a, dx, n, c), O.upwind(d, a, dx, n, c)
+        want = (P.stencil_length - 2, P.stencil_length)
+    data, (lo, up) = P.banded()
+    assert (lo, up) == want
+    assert data.shape == (lo + up + 1, n + 2)
+    _same(_from_band(data, lo, up, n), Q.array())
