@@ -769,6 +769,15 @@ struct deo_plan {
     size_t table_bytes = 0;
     void* stage_u = nullptr;
     void* stage_du = nullptr;
+    // pipelined host applies: two staging slots, copy-in / copy-out streams and their events
+    struct HostPipe {
+        void* u[2] = {nullptr, nullptr};
+        void* du[2] = {nullptr, nullptr};
+        cudaStream_t in = nullptr, out = nullptr;
+        cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_comp[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+        unsigned next = 0;
+    } pipe;
+    std::mutex pipe_mu;
     // kernels launched by the last forward apply (diagnostics; last writer wins)
     mutable std::atomic<const char*> last_kernel{""};
     mutable std::atomic<const char*> last_kernel2{""};
@@ -785,6 +794,14 @@ struct deo_plan {
         if (side) cudaStreamDestroy(side);
         if (stage_u) cudaFree(stage_u);
         if (stage_du) cudaFree(stage_du);
+        for (int k = 0; k < 2; ++k) {
+            if (pipe.u[k]) cudaFree(pipe.u[k]);
+            if (pipe.du[k]) cudaFree(pipe.du[k]);
+            for (cudaEvent_t e : {pipe.ev_in[k], pipe.ev_comp[k], pipe.ev_out[k]})
+                if (e) cudaEventDestroy(e);
+        }
+        if (pipe.in) cudaStreamDestroy(pipe.in);
+        if (pipe.out) cudaStreamDestroy(pipe.out);
         for (cudaEvent_t e : ev)
             if (e) cudaEventDestroy(e);
     }
@@ -1253,6 +1270,52 @@ extern "C" deo_status deo_apply_host(deo_plan* p, const void* uh, void* duh, voi
     if (e) return cuda_fail((cudaError_t)e, "deo_apply_host launch");
     CUDA_TRY(cudaMemcpyAsync(duh, p->stage_du, bytes, cudaMemcpyDeviceToHost, st), "D2H");
     CUDA_TRY(cudaStreamSynchronize(st), "synchronize");
+    return DEO_OK;
+}
+
+// Pipelined host applies: call i uses staging slot i % 2.  Its copy-in runs
+// on the plan's copy-in stream once apply i-2 has finished reading the slot;
+// the apply runs on the caller's stream once the copy-in has landed and copy-out
+// i-2 has drained the slot; the copy-out runs on the plan's copy-out stream.
+// So copy-in i+1, apply i and copy-out i-1 overlap (H2D and D2H run in both
+// directions at once).
+extern "C" deo_status deo_apply_host_async(deo_plan* p, const void* uh, void* duh, void* stream) {
+    deo_status s = check_ptrs(p, uh, duh);
+    if (s != DEO_OK) return s;
+    const size_t bytes = (size_t)p->dev.total * (p->dev.dtype == DEO_F64 ? 8 : 4);
+    std::lock_guard<std::mutex> lk(p->pipe_mu);
+    auto& P = p->pipe;
+    if (!P.in) {
+        for (int k = 0; k < 2; ++k) {
+            CUDA_TRY(cudaMalloc(&P.u[k], bytes), "cudaMalloc(staging)");
+            CUDA_TRY(cudaMalloc(&P.du[k], bytes), "cudaMalloc(staging)");
+            for (cudaEvent_t* e : {&P.ev_in[k], &P.ev_comp[k], &P.ev_out[k]})
+                CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
+        }
+        CUDA_TRY(cudaStreamCreateWithFlags(&P.out, cudaStreamNonBlocking), "cudaStreamCreate");
+        CUDA_TRY(cudaStreamCreateWithFlags(&P.in, cudaStreamNonBlocking), "cudaStreamCreate");
+    }
+    const int k = (int)(P.next++ & 1u);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaStreamWaitEvent(P.in, P.ev_comp[k], 0), "cudaStreamWaitEvent");
+    CUDA_TRY(cudaMemcpyAsync(P.u[k], uh, bytes, cudaMemcpyHostToDevice, P.in), "H2D");
+    CUDA_TRY(cudaEventRecord(P.ev_in[k], P.in), "cudaEventRecord");
+    CUDA_TRY(cudaStreamWaitEvent(st, P.ev_in[k], 0), "cudaStreamWaitEvent");
+    CUDA_TRY(cudaStreamWaitEvent(st, P.ev_out[k], 0), "cudaStreamWaitEvent");
+    const int e = launch_forward(p, P.u[k], P.du[k], 1, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_apply_host_async launch");
+    CUDA_TRY(cudaEventRecord(P.ev_comp[k], st), "cudaEventRecord");
+    CUDA_TRY(cudaStreamWaitEvent(P.out, P.ev_comp[k], 0), "cudaStreamWaitEvent");
+    CUDA_TRY(cudaMemcpyAsync(duh, P.du[k], bytes, cudaMemcpyDeviceToHost, P.out), "D2H");
+    CUDA_TRY(cudaEventRecord(P.ev_out[k], P.out), "cudaEventRecord");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_plan_host_sync(deo_plan* p) {
+    if (!p) return fail(DEO_ERR_BAD_ARG, "null plan");
+    std::lock_guard<std::mutex> lk(p->pipe_mu);
+    for (int k = 0; k < 2; ++k)
+        if (p->pipe.ev_out[k]) CUDA_TRY(cudaEventSynchronize(p->pipe.ev_out[k]), "cudaEventSynchronize");
     return DEO_OK;
 }
 

@@ -677,6 +677,19 @@ class Plan:
                                      stream if stream is not None else _stream_ptr()))
         return du
 
+    def apply_host_async(self, u, du, stream=None):
+        """Pipelined host apply (deo_apply_host_async): u, du are host buffers
+        (numpy Fortran arrays or pinned CPU tensors, in the plan's layout) that
+        must stay alive, and du unread, until host_sync()."""
+        up = u.ctypes.data if isinstance(u, np.ndarray) else u.data_ptr()
+        dp = du.ctypes.data if isinstance(du, np.ndarray) else du.data_ptr()
+        check(L.lib().deo_apply_host_async(self._h, C.c_void_p(up), C.c_void_p(dp),
+                                           stream if stream is not None else _stream_ptr()))
+        return du
+
+    def host_sync(self):
+        check(L.lib().deo_plan_host_sync(self._h))
+
     def concretize(self):
         n = int(np.prod(self.shape))
         Al = np.zeros((n, n), order="F")

@@ -237,6 +237,15 @@ deo_status deo_apply(const deo_plan* plan, const void* u, void* du, int overwrit
 /* Same, reading u from host memory and writing du to host memory (copies
  * through the plan's staging buffers on `stream`; synchronises before return). */
 deo_status deo_apply_host(deo_plan* plan, const void* u_host, void* du_host, void* stream);
+/* The same for a sequence of host arrays, pipelined and not synchronising: the
+ * copy of call i+1's input, call i's apply and the copy of call i-1's result
+ * overlap (two plan-owned staging slots, plan-owned copy streams; the apply
+ * itself runs on `stream`).  u_host and du_host (pinned memory for overlap)
+ * must stay valid, and du_host unread, until deo_plan_host_sync returns.
+ * No reference counterpart (the reference applies to host arrays only). */
+deo_status deo_apply_host_async(deo_plan* plan, const void* u_host, void* du_host, void* stream);
+/* Waits for every deo_apply_host_async of the plan issued so far. */
+deo_status deo_plan_host_sync(deo_plan* plan);
 
 /* Adjoint of the linear part: ubar = A_l^T dbar, where (A_l, A_b) = Array(L*Q)
  * (concretization.jl:914-918) of the map deo_apply computes.  No reference
