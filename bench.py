@@ -409,8 +409,9 @@ def run_nonuniform2d(args):
 
     import deo
     n = 2048
-    x = np.cumsum(np.r_[0.0, np.ones(n)]) / n
-    a = np.asfortranarray(np.cos(2 * np.pi * x[1:, None]) * np.sin(2 * np.pi * x[None, 1:]))
+    ops, (_, _, dx) = nonuniform2d_ops(n)
+    x = np.cumsum(dx)[:n]  # the grid's nodes
+    a = np.asfortranarray(np.cos(2 * np.pi * x[:, None]) * np.sin(2 * np.pi * x[None, :]))
     fdev = deo.julia_array((n, n)); fdev.copy_(torch.from_numpy(a))
     ops, _ = nonuniform2d_ops(n, fdev)
     rng = np.random.default_rng(SEED + 3)
