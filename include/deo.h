@@ -211,7 +211,7 @@ deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);
 /* Name of the kernel the last forward apply launched first (which = 0) and
- * second (which = 1; "" if it launched one), e.g. "k_lap_fx" and "k_shell".
+ * second (which = 1; "" if it launched one), e.g. "k_lap_fx" and "k_face".
  * Static strings; "" before the first apply.  No reference counterpart. */
 const char* deo_plan_kernels(const deo_plan* plan, int which);
 /* Device time in ms of each launch of the last forward apply (DEO_OPT_LAUNCH_TIMING
