@@ -895,22 +895,24 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
                         T* dz = dcol + (int64_t)z * sxy;
 #pragma unroll
                         for (int j = 0; j < RY; ++j) {
+                            // every row is evaluated (the tile in shared memory covers it: no branch
+                            // around the loads, so they schedule across rows); only interior rows are stored
+                            const int cc = c0 + j * C::BX;
+                            T ax = T(0), ay = T(0);
+#pragma unroll
+                            for (int k = 0; k < K; ++k)
+                                ax = fma(w[0][k], k == H ? col[H + j] : pc[cc + k - H], ax);
+#pragma unroll
+                            for (int k = 0; k < K; ++k) ay = fma(w[1][k], col[j + k], ay);
+                            T tot = ax + ay;
+                            if constexpr (NT == 3) {
+                                T az = T(0);
+#pragma unroll
+                                for (int k = 0; k < K; ++k) az = fma(w[2][k], q[j][(ph + 1 + k) % NQ], az);
+                                tot = tot + az;
+                            }
+                            tot = zero_fix_q(tot);
                             if (vmask & (1u << j)) {
-                                const int cc = c0 + j * C::BX;
-                                T ax = T(0), ay = T(0);
-#pragma unroll
-                                for (int k = 0; k < K; ++k)
-                                    ax = fma(w[0][k], k == H ? col[H + j] : pc[cc + k - H], ax);
-#pragma unroll
-                                for (int k = 0; k < K; ++k) ay = fma(w[1][k], col[j + k], ay);
-                                T tot = ax + ay;
-                                if constexpr (NT == 3) {
-                                    T az = T(0);
-#pragma unroll
-                                    for (int k = 0; k < K; ++k) az = fma(w[2][k], q[j][(ph + 1 + k) % NQ], az);
-                                    tot = tot + az;
-                                }
-                                tot = zero_fix_q(tot);
                                 T* d = dz + (int64_t)j * nx;
                                 if constexpr (OW) *d = tot;
                                 else *d = tot + *d;
