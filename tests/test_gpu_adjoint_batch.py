@@ -443,3 +443,22 @@ def test_pipelined_host_applies(cuda):
         d = deo.julia_array(shape)
         p.apply(ud, d)
         assert torch.equal(d.permute(*reversed(range(len(shape)))).contiguous().view(-1).cpu(), b)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_default_path_accumulate_equals_overwrite_plus_base(cuda, dtype):
+    """Default options (fixed-point interior for Float64, concurrent shell):
+    overwrite=false adds the same values the overwriting apply writes."""
+    import torch
+    A, oterms, u = build(ND[0], dtype=dtype)
+    shape = tuple(ND[0]["shape"])
+    p = deo.Plan(A.terms(), shape, 0 if dtype == "f64" else 1)
+    assert p.get_option(deo.DEO_OPT_CONCURRENT_SHELL)
+    ud = to_device(u, dtype)
+    base = to_device(np.asfortranarray(np.random.default_rng(8).standard_normal(shape)), dtype)
+    ow = deo.julia_array(shape, ud.dtype)
+    p.apply(ud, ow)
+    acc = base.clone()
+    p.apply(ud, acc, overwrite=False)
+    assert torch.equal(acc, base + ow)
+    assert deo.device_status() == 0
