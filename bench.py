@@ -542,6 +542,28 @@ def run_batch(args):
             "autotune_forward": cfg_f, "autotune_adjoint": cfg_a, "gpu_launches_per_pass": 2}
 
 
+def run_nld(args):
+    """nonlinear_diffusion!(du, 2, 1, 4, p, q, h, N) on N = 2^24 points (Float64):
+    six operator applications (orders 1-3 on q and 1-2 on p) and the products,
+    one fused kernel."""
+    import torch
+
+    import deo
+    N = 1 << 24
+    h = 1.0 / (N + 1)
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    x = torch.linspace(0, 1, N + 2, device="cuda", dtype=torch.float64)
+    q = torch.sin(6.283185307179586 * x) + 1e-3 * torch.randn(N + 2, generator=g, device="cuda", dtype=torch.float64)
+    p = 1.0 + 0.5 * torch.cos(6.283185307179586 * x)
+    du = torch.empty(N, device="cuda", dtype=torch.float64)
+    t = _event_time(lambda: deo.nonlinear_diffusion_(du, 2, 1, 4, p, q, h, N), args.steps, args.warmup)
+    hbm, _ = peaks()
+    byts = 3 * 8 * N
+    return {"metric": "grid-pts/s (nonlinear_diffusion!, n=2, m=1, a=4)", "workload": "nonlinear_diffusion_2^24_f64",
+            "value": N / t, "unit": "grid-pts/s", "dtype": "f64", "us_per_apply": t * 1e6,
+            "GBps": byts / t / 1e9, "frac_hbm": byts / t / 1e9 / hbm, "gpu_launches_per_apply": 1}
+
+
 def run_serve(args):
     import torch
 
@@ -614,7 +636,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lap3d",
-                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve"])
+                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=64)
@@ -623,11 +645,11 @@ def main():
     ap.add_argument("--serve-baseline", action="store_true")
     ap.add_argument("--batch-config", default="", help="tile,ctas_per_sm for the batch workload (skips autotuning)")
     args = ap.parse_args()
-    if args.workload in ("line1d", "nonuniform2d", "batch", "serve"):
+    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld"):
         import torch
         torch.cuda.set_device(0)
         fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "batch": run_batch,
-              "serve": run_serve}[args.workload]
+              "serve": run_serve, "nld": run_nld}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     if args.warmup < 3:

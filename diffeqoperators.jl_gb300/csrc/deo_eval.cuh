@@ -24,6 +24,7 @@ template <typename T>
 __device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ line) {
     const int64_t s = t.stride;
     if (t.bc_kind == 1) return t.periodic_nd ? line[0] : line[(int64_t)(t.len - 1) * s];
+    if (t.bc_kind == 2) return line[-s];  // padded input: the ghost is stored before the line
     T d = T(0);
     for (int j = 0; j < t.ml; ++j) d = (j == 0) ? T(t.al[0]) * line[0] : fma(T(t.al[j]), line[(int64_t)j * s], d);
     return d + T(t.bl);
@@ -33,6 +34,7 @@ template <typename T>
 __device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__ line) {
     const int64_t s = t.stride;
     if (t.bc_kind == 1) return t.periodic_nd ? line[(int64_t)(t.len - 1) * s] : line[0];
+    if (t.bc_kind == 2) return line[(int64_t)t.len * s];  // padded input: the ghost is stored after the line
     T d = T(0);
     const int64_t o = (int64_t)(t.len - t.mr);
     for (int j = 0; j < t.mr; ++j)

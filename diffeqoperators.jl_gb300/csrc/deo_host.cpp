@@ -1319,6 +1319,61 @@ extern "C" deo_status deo_plan_host_sync(deo_plan* p) {
     return DEO_OK;
 }
 
+// nonlinear_diffusion!: a plan over the order-1 .. (m+n) CenteredDifference
+// operators of the grid (term k-1 has order k), whose ghosts are read from the
+// padded inputs themselves (bc_kind 2), evaluated by the generic method.
+struct deo_nld {
+    deo_plan* plan = nullptr;
+    int n = 0, m = 0, len = 0;
+    ~deo_nld() { deo_plan_destroy(plan); }
+};
+
+extern "C" deo_status deo_nonlinear_diffusion_plan(int second_order, int first_order, int approx_order,
+                                                   const double* dx, int dx_len, int nknots, deo_dtype dtype,
+                                                   deo_nld** out) {
+    if (!out || !dx) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    if (approx_order <= 1) return fail(DEO_ERR_BAD_ARG, "approximation_order must be greater than 1.");
+    if (second_order < 1 || first_order < 0 || first_order + second_order > DEO_MAX_TERMS)
+        return fail(DEO_ERR_BAD_ARG, "differential orders must satisfy n >= 1, m >= 0, m + n <= %d", DEO_MAX_TERMS);
+    const int K = first_order + second_order;
+    std::vector<deo_operator*> ops(K, nullptr);
+    auto free_ops = [&] {
+        for (deo_operator* o : ops) deo_operator_destroy(o);
+    };
+    deo_bc bc;
+    deo_status s = deo_dirichlet_bc(0.0, 0.0, &bc);  // placeholder: the ghosts come from the padded inputs
+    std::vector<deo_term> terms(K);
+    for (int k = 1; k <= K && s == DEO_OK; ++k) {
+        s = deo_centered_difference(k, approx_order, dx, dx_len, nknots, &ops[k - 1]);
+        terms[k - 1] = deo_term{ops[k - 1], 1, &bc, nullptr, DEO_PATH_GENERIC};
+    }
+    auto N = std::make_unique<deo_nld>();
+    const int64_t size = nknots;
+    if (s == DEO_OK) s = deo_plan_create(1, &size, dtype, K, terms.data(), &N->plan);
+    free_ops();
+    if (s != DEO_OK) return s;
+    for (int k = 0; k < K; ++k) N->plan->dev.t[k].bc_kind = 2;
+    CUDA_TRY(cudaMemcpy(N->plan->d_plan, &N->plan->dev, sizeof(PlanDev), cudaMemcpyHostToDevice), "cudaMemcpy(plan)");
+    N->n = second_order;
+    N->m = first_order;
+    N->len = nknots;
+    *out = N.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_nonlinear_diffusion(const deo_nld* nl, const void* p, const void* q, void* du,
+                                              void* stream) {
+    if (!nl || !p || !q || !du) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (du == p || du == q) return fail(DEO_ERR_BAD_ARG, "du must not alias p or q");
+    const int e = deo_k_nonlinear_diffusion(nl->plan->d_plan, nl->len, nl->n, nl->m, nl->plan->dev.dtype, p, q, du,
+                                            stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_nonlinear_diffusion launch");
+    return DEO_OK;
+}
+
+extern "C" void deo_nonlinear_diffusion_destroy(deo_nld* nl) { delete nl; }
+
 extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double* Ab) {
     if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");
     const int64_t n = p->dev.total;

@@ -64,7 +64,7 @@ struct TermDev {
     const int* rlo;
     const int* rhi;
     // boundary condition (ghost map)
-    int bc_kind;         // 0 affine, 1 periodic
+    int bc_kind;         // 0 affine, 1 periodic, 2 padded input (ghosts stored around the line)
     int periodic_nd;     // N-D PeriodicBC pads with the edge planes (multi_dim_bc_operators.jl:221-228)
     int ml, mr;
     double al[DEO_MAX_BCW];
@@ -185,6 +185,10 @@ extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
+// nonlinear_diffusion! on padded vectors p, q (length len+2): term k-1 of the
+// plan is CenteredDifference of order k (padded-input ghosts).
+extern "C" int deo_k_nonlinear_diffusion(const deo::PlanDev* d_plan, int len, int n, int m, int dtype, const void* p,
+                                         const void* q, void* du, void* stream);
 // TMA-fed fast path (deo_tma.cu): the interior box of a Laplacian-type plan;
 // returns cudaErrorNotSupported when the array does not meet the tensor-map
 // alignment rules (caller falls back).  use_ens: 0 the reference's tap order,

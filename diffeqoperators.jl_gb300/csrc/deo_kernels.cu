@@ -354,6 +354,40 @@ extern "C" int deo_k_apply_uniform(const UniPlan* up, const PlanDev* dp, int dty
     return (int)cudaErrorInvalidValue;
 }
 
+// nonlinear_diffusion!{N}(du, n, m, approx, p, q, dx, len) on padded vectors
+// (derivative_operator.jl:34-66): with D_k the order-k centred operator (plan
+// term k-1) applied to a padded vector by the generic method,
+//   du = (D_m q) .* (D_n p)            (m > 0)   or   q[2:len+1] .* (D_n p)   (m == 0)
+//   du = du .+ binomial(n, l) * (D_{l+m} q) .* (D_{n-l} p),   l = 1 .. n-1
+//   du = du .+ (D_{m+n} q) .* p[2:len+1]
+// each broadcast in the reference's operation order, one thread per point.
+template <typename T>
+__global__ void __launch_bounds__(256) k_nld(const PlanDev* __restrict__ P, int len, int n, int m,
+                                             const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ du) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    auto D = [&](int k, const T* x) { return eval_term<T>(P->t[k - 1], x + 1, i, i + 1); };
+    T acc = (m > 0 ? D(m, q) : q[i + 1]) * D(n, p);
+    long long b = 1;  // binomial(n, l)
+    for (int l = 1; l <= n - 1; ++l) {
+        b = b * (n - l + 1) / l;
+        acc = acc + (T(b) * D(l + m, q)) * D(n - l, p);
+    }
+    acc = acc + D(m + n, q) * p[i + 1];
+    du[i] = acc;
+}
+
+extern "C" int deo_k_nonlinear_diffusion(const PlanDev* d_plan, int len, int n, int m, int dtype, const void* p,
+                                         const void* q, void* du, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned blocks = (unsigned)((len + 255) / 256);
+    if (dtype == 0)
+        k_nld<double><<<blocks, 256, 0, st>>>(d_plan, len, n, m, (const double*)p, (const double*)q, (double*)du);
+    else
+        k_nld<float><<<blocks, 256, 0, st>>>(d_plan, len, n, m, (const float*)p, (const float*)q, (float*)du);
+    return (int)cudaGetLastError();
+}
+
 extern "C" int deo_k_num_sms(void);
 
 extern "C" int deo_k_stage_batch(const StageDev* st, const WorkItem* items, int64_t n_items, unsigned int* counter,

@@ -27,3 +27,4 @@ mul = mul_
 from . import autodiff, batch  # noqa: E402,F401
 from .autodiff import rrule  # noqa: E402,F401
 from .batch import Batch, StageBatch  # noqa: E402,F401
+from .nonlinear import nonlinear_diffusion, nonlinear_diffusion_  # noqa: E402,F401

@@ -117,6 +117,10 @@ def lib():
     proto("deo_device_status", st, C.POINTER(C.c_uint))
     proto("deo_apply", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_apply_host", st, _vp, _vp, _vp, _vp)
+    proto("deo_nonlinear_diffusion_plan", st, C.c_int, C.c_int, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+          C.POINTER(_vp))
+    proto("deo_nonlinear_diffusion", st, _vp, _vp, _vp, _vp, _vp)
+    proto("deo_nonlinear_diffusion_destroy", None, _vp)
     proto("deo_apply_host_async", st, _vp, _vp, _vp, _vp)
     proto("deo_plan_host_sync", st, _vp)
     proto("deo_apply_adjoint", st, _vp, _vp, _vp, C.c_int, _vp)
@@ -152,7 +156,8 @@ EXPORTED = [
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
     "deo_operator_destroy", "deo_operator_array", "deo_operator_banded", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_destroy",
-    "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize",
+    "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_nonlinear_diffusion_plan", "deo_nonlinear_diffusion",
+    "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune",
 ]

@@ -252,6 +252,21 @@ deo_status deo_plan_host_sync(deo_plan* plan);
  * counterpart (the reference's adjoint(L) returns L, abstract_operator_functions.jl:130-135). */
 deo_status deo_apply_adjoint(const deo_plan* plan, const void* dbar, void* ubar, int overwrite, void* stream);
 
+/* nonlinear_diffusion!{N}(du, n, m, approx_order, p, q, dx, nknots)
+ * (derivative_operator.jl:34-66):
+ *   du = (D_m q) .* (D_n p)   (q[2:nknots+1] .* (D_n p) when m == 0)
+ *      + sum_{l=1}^{n-1} binomial(n, l) * (D_{l+m} q) .* (D_{n-l} p)
+ *      + (D_{m+n} q) .* p[2:nknots+1]
+ * with D_k = CenteredDifference(k, approx_order, dx, nknots) applied to the
+ * padded vectors p, q (nknots + 2 entries, ghosts first and last) by the
+ * generic method, in the reference's operation order.  Planned once
+ * (operators and tables), applied on device vectors p, q -> du (nknots). */
+typedef struct deo_nld deo_nld;
+deo_status deo_nonlinear_diffusion_plan(int second_order, int first_order, int approx_order, const double* dx,
+                                        int dx_len, int nknots, deo_dtype dtype, deo_nld** out);
+deo_status deo_nonlinear_diffusion(const deo_nld* plan, const void* p, const void* q, void* du, void* stream);
+void deo_nonlinear_diffusion_destroy(deo_nld* plan);
+
 /* Concretisation on the device: A_l (n x n, column-major, n = prod(sizes)) and
  * A_b (n) of the affine map, by applying the plan to unit vectors in batches.
  * For checking small operators (n <= 8192).  Allocates device scratch. */

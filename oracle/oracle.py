@@ -294,6 +294,29 @@ def abs_scale(terms, u: np.ndarray) -> np.ndarray:
     return o
 
 
+def nonlinear_diffusion(n: int, m: int, approx: int, p, q, dx, nknots: int, absolute: bool = False) -> np.ndarray:
+    """nonlinear_diffusion!{N}(du, n, m, approx, p, q, dx, nknots) as the reference
+    computes it (derivative_operator.jl:34-66): the operators by the generic
+    method on the padded vectors (orc_mul_generic), the broadcasts in numpy in
+    the reference's operation order (no contraction).  absolute=True gives the
+    same sum over |weights| and |values| (the error scale)."""
+    p = _f64(p)
+    q = _f64(q)
+
+    def D(k, x):
+        op = centered(k, approx, dx, nknots)
+        if absolute:
+            return op.abs().mul_generic(np.abs(x))
+        return op.mul_generic(x)
+    pp, qq = (np.abs(p), np.abs(q)) if absolute else (p, q)
+    du = (D(m, q) if m > 0 else qq[1:nknots + 1]) * D(n, p)
+    b = 1
+    for ell in range(1, n):
+        b = b * (n - ell + 1) // ell
+        du = du + (float(b) * D(ell + m, q)) * D(n - ell, p)
+    return du + D(m + n, q) * pp[1:nknots + 1]
+
+
 def ulp_tolerance(terms, u: np.ndarray, n_ulp: float = 4.0) -> np.ndarray:
     """Per-point tolerance: n_ulp units in the last place of sum_k |c_k u_k|."""
     return n_ulp * np.spacing(abs_scale(terms, u))
