@@ -21,6 +21,7 @@ SOURCES = {
     "deo_tma.o": ("nvcc", "deo_tma.cu"),
     "deo_shell.o": ("nvcc", "deo_shell.cu"),
     "deo_static.o": ("nvcc", "deo_static.cu"),
+    "deo_vector.o": ("nvcc", "deo_vector.cu"),
     "deo_host.o": ("cxx", "deo_host.cpp"),
 }
 
@@ -28,11 +29,14 @@ SOURCES = {
 def _cmd(kind: str, src: str, obj: str, verbose_ptxas: bool) -> list[str]:
     inc = ["-I", os.path.join(HERE, "..", "include"), "-I", CSRC]
     if kind == "nvcc":
-        c = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj, *inc]
+        c = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-c", src,
+             "-o", obj, *inc]
         if verbose_ptxas:
             c += ["-Xptxas", "-v"]
         return c
-    return ["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-c", src, "-o", obj, *inc,
+    # -ffp-contract=off: host arithmetic (Fornberg weights, BC maps) rounds every
+    # product and sum as the reference does; GCC fuses a*b+c on Arm otherwise.
+    return ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-c", src, "-o", obj, *inc,
             "-I", os.path.join(CUDA_HOME, "include")]
 
 

@@ -596,6 +596,9 @@ static void row_fill(RowSpec& r, int p0, int nk, int cidx, double c, const doubl
     }
 }
 
+// Row i of operator A as a (p0, nk, cidx, weights) record.  mode 1: the
+// BoundaryPaddedVector methods; 0: the generic AbstractVector methods; 2: the
+// vector-calculus methods (centred: coefficients[i] on every row).
 static RowSpec build_row(const deo_operator& A, int mode, bool scaled, double sgn, long i) {
     RowSpec r;
     const long len = A.len;
@@ -611,7 +614,9 @@ static RowSpec build_row(const deo_operator& A, int mode, bool scaled, double sg
             row_fill(r, (int)(i + 1 - stl / 2), stl, (int)ci, mult(ci), s);
         } else {
             const long rr = i - (len - bpc);
-            const long ci = (mode == 1) ? i : rr;  // generic right rows read coeff[1:bpc] (convolutions.jl:109)
+            // generic right rows read coeff[1:bpc] (convolutions.jl:109); the padded
+            // methods and the vector-calculus methods (mode 2) read coeff[i]
+            const long ci = (mode == 0) ? rr : i;
             row_fill(r, (int)(len + 3 - bstl), bstl, (int)ci, mult(ci), A.Hi((int)rr - 1));
         }
         return r;
@@ -1373,6 +1378,141 @@ extern "C" deo_status deo_nonlinear_diffusion(const deo_nld* nl, const void* p, 
 }
 
 extern "C" void deo_nonlinear_diffusion_destroy(deo_nld* nl) { delete nl; }
+
+// Gradient / Divergence / Curl: one row table per axis operator over the padded
+// input (ghosts = the input's own edge planes), plus negated copies for the
+// curl's subtracted terms; evaluated by the vector-calculus kernels.
+struct deo_vc {
+    deo_plan tabs;  // owns the uploaded tables (no kernels of its own)
+    deo::VcDev dev{};
+    int dtype = 0;
+    int ncomp_in = 1, ncomp_out = 1;
+};
+
+extern "C" deo_status deo_vector_calculus_plan(int kind, int ndims, const deo_operator* const* ops, deo_dtype dtype,
+                                               deo_vc** out) {
+    if (!out || !ops) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    if (kind < DEO_VC_GRADIENT || kind > DEO_VC_CURL) return fail(DEO_ERR_BAD_ARG, "unknown operator kind %d", kind);
+    if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
+    if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
+    if (kind == DEO_VC_CURL && ndims != 3) return fail(DEO_ERR_BAD_SHAPE, "Curl acts on 3-dimensional vectors");
+    for (int a = 0; a < ndims; ++a) {
+        if (!ops[a]) return fail(DEO_ERR_BAD_ARG, "null operator for axis %d", a + 1);
+        const deo_operator& A = *ops[a];
+        if (A.wind) return fail(DEO_ERR_UNSUPPORTED, "axis %d: vector-calculus operators are CenteredDifference", a + 1);
+        if (A.stl != ops[0]->stl || A.bstl != ops[0]->bstl || A.bpc != ops[0]->bpc)
+            return fail(DEO_ERR_BAD_ARG,
+                        "axis %d: the axis operators must share stencil_length, boundary_stencil_length and "
+                        "boundary_point_count (the methods take them from the first)", a + 1);
+        if (A.len < 2 * A.bpc + 1) return fail(DEO_ERR_BAD_SHAPE, "axis %d: len %d < 2*boundary_point_count+1", a + 1, A.len);
+        if (kind == DEO_VC_CURL && A.len != ops[0]->len)
+            return fail(DEO_ERR_BAD_SHAPE, "All dimensions must have equal no. of grid points");
+    }
+    auto V = std::make_unique<deo_vc>();
+    deo::VcDev& D = V->dev;
+    D.kind = kind;
+    D.nd = ndims;
+    D.quirk = (ndims == 2 || ndims == 3) ? 1 : 0;
+    D.bpc = ops[0]->bpc;
+    int64_t pv = 1, ov = 1;
+    for (int a = 0; a < ndims; ++a) {
+        D.len[a] = ops[a]->len;
+        D.pstride[a] = pv;
+        pv *= ops[a]->len + 2;
+        ov *= ops[a]->len;
+    }
+    D.pvol = pv;
+    D.ovol = ov;
+    const int mode = D.quirk ? 2 : 0;
+    for (int a = 0; a < ndims; ++a) {
+        const deo_operator& A = *ops[a];
+        for (int neg = 0; neg < (kind == DEO_VC_CURL ? 2 : 1); ++neg) {
+            TermDev& T = neg ? D.tn[a] : D.t[a];
+            T.axis = a;
+            T.len = A.len;
+            T.stride = D.pstride[a];
+            T.nvar = 1;
+            T.bc_kind = 2;
+            std::vector<int> rlo(A.len + 2, A.len + 1), rhi(A.len + 2, 0);
+            HostTab H;
+            deo_status s = compile_table(A, mode, true, 1.0, H, rlo, rhi);
+            if (s != DEO_OK) return s;
+            if (neg) {  // (-c) * s = -(c * s) exactly
+                for (double& w : H.dev.wband) w = -w;
+                for (double& w : H.W) w = -w;
+            }
+            if ((s = upload_tab(V->tabs, H, dtype, T.tab[0])) != DEO_OK) return s;
+        }
+    }
+    // unrolled interior loop: every operator's rows bpc+1 .. len-bpc are one centred band
+    int bnk = ops[0]->stl;
+    for (int a = 0; a < ndims; ++a) {
+        const RowTabDev& tb = D.t[a].tab[0];
+        if (!(tb.ilo <= D.bpc + 1 && tb.ihi >= D.len[a] - D.bpc && tb.band_nk == bnk && tb.band_p0_off == 1 - bnk / 2))
+            bnk = 0;
+    }
+    D.band_nk = (bnk == 3 || bnk == 5 || bnk == 7 || bnk == 9) ? bnk : 0;
+    V->dtype = dtype;
+    V->ncomp_in = kind == DEO_VC_GRADIENT ? 1 : (kind == DEO_VC_CURL ? 3 : ndims);
+    V->ncomp_out = kind == DEO_VC_DIVERGENCE ? 1 : (kind == DEO_VC_CURL ? 3 : ndims);
+    *out = V.release();
+    return DEO_OK;
+}
+
+static bool overlaps(const void* a, size_t na, const void* b, size_t nb) {
+    const char *pa = static_cast<const char*>(a), *pb = static_cast<const char*>(b);
+    return pa < pb + nb && pb < pa + na;
+}
+
+extern "C" deo_status deo_vector_calculus_sizes(const deo_vc* vc, int64_t* in_elems, int64_t* out_elems) {
+    if (!vc) return fail(DEO_ERR_BAD_ARG, "null plan");
+    if (in_elems) *in_elems = vc->dev.pvol * vc->ncomp_in;
+    if (out_elems) *out_elems = vc->dev.ovol * vc->ncomp_out;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_vector_calculus_apply(const deo_vc* vc, const void* M, void* out, int overwrite,
+                                                void* stream) {
+    if (!vc || !M || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const size_t es = vc->dtype == DEO_F64 ? 8 : 4;
+    if (overlaps(M, (size_t)(vc->dev.pvol * vc->ncomp_in) * es, out, (size_t)(vc->dev.ovol * vc->ncomp_out) * es))
+        return fail(DEO_ERR_BAD_ARG, "the output must not overlap the input");
+    const int e = deo_k_vector_calculus(&vc->dev, vc->dtype, M, out, overwrite ? 1 : 0, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_vector_calculus_apply launch");
+    return DEO_OK;
+}
+
+extern "C" void deo_vector_calculus_destroy(deo_vc* vc) { delete vc; }
+
+static deo_status vector_algebra(int op, deo_dtype dtype, int64_t npts, int ncomp, const void* A, const void* B,
+                                 void* u, void* stream) {
+    if (!A || !u || (op != 2 && !B)) return fail(DEO_ERR_BAD_ARG, "null argument");
+    if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
+    if (npts < 0 || ncomp < 1) return fail(DEO_ERR_BAD_SHAPE, "npts must be >= 0 and ncomp >= 1");
+    const size_t es = dtype == DEO_F64 ? 8 : 4;
+    const size_t nin = (size_t)npts * ncomp * es, nout = (size_t)npts * (op == 1 ? 3 : 1) * es;
+    if (overlaps(A, nin, u, nout) || (B && op != 2 && overlaps(B, nin, u, nout)))
+        return fail(DEO_ERR_BAD_ARG, "the output must not overlap the inputs");
+    const int e = deo_k_vector_algebra(op, dtype, npts, ncomp, A, B, u, stream);
+    if (e) return cuda_fail((cudaError_t)e, "vector algebra launch");
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_dot_product(deo_dtype dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,
+                                      void* stream) {
+    return vector_algebra(0, dtype, npts, ncomp, A, B, u, stream);
+}
+
+extern "C" deo_status deo_cross_product(deo_dtype dtype, int64_t npts, const void* A, const void* B, void* u,
+                                        void* stream) {
+    return vector_algebra(1, dtype, npts, 3, A, B, u, stream);
+}
+
+extern "C" deo_status deo_square_norm(deo_dtype dtype, int64_t npts, int ncomp, const void* A, void* u,
+                                      void* stream) {
+    return vector_algebra(2, dtype, npts, ncomp, A, nullptr, u, stream);
+}
 
 extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double* Ab) {
     if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");

@@ -174,7 +174,43 @@ struct StageDev {
     int pad_;
 };
 
+// Gradient / Divergence / Curl on a padded array (vector_calculus_*.jl).
+// t[a]: the row table of axis a's operator over the padded input (bc_kind 2,
+// stride = the padded stride); tn[a]: the same rows with negated weights
+// (the curl's `-cur_coeff * ...` terms).  quirk = 1 for the 2-D / 3-D
+// methods: the axes other than the differentiated one are read at the padded
+// index equal to the output index, and each output adds its terms in the order
+// (BC_left, interior, BC_right) x (axis 1, 2, 3); quirk = 0 for the generic
+// per-line methods (other axes at index + 1, terms in axis order).
+#define DEO_VC_GRADIENT 0
+#define DEO_VC_DIVERGENCE 1
+#define DEO_VC_CURL 2
+struct VcDev {
+    int kind;
+    int nd;
+    int quirk;
+    int bpc;             // boundary_point_count shared by the operators
+    int band_nk;         // > 0: every operator's interior rows (bpc+1 .. len-bpc) are one
+                         // band of band_nk taps centred on the point (uniform grid)
+    int pad_;
+    int64_t len[8];      // output size per axis (the operators' len)
+    int64_t pstride[8];  // strides of the padded input
+    int64_t pvol;        // points of one padded component
+    int64_t ovol;        // points of one output component
+    TermDev t[8];
+    TermDev tn[3];
+};
+
 }  // namespace deo
+
+// Launchers implemented in deo_vector.cu.  kind/nd/quirk come from V; out may
+// not overlap M.  overwrite = 1 writes A*M, 0 adds it to out (mul!).
+extern "C" int deo_k_vector_calculus(const deo::VcDev* V, int dtype, const void* M, void* out, int overwrite,
+                                     void* stream);
+// op 0: u = dot(A, B) over ncomp components; 1: u = cross(A, B) (ncomp 3);
+// 2: u = sqrt(dot(A, A)).  npts points per component, component-major.
+extern "C" int deo_k_vector_algebra(int op, int dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,
+                                    void* stream);
 
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,

@@ -28,3 +28,5 @@ from . import autodiff, batch  # noqa: E402,F401
 from .autodiff import rrule  # noqa: E402,F401
 from .batch import Batch, StageBatch  # noqa: E402,F401
 from .nonlinear import nonlinear_diffusion, nonlinear_diffusion_  # noqa: E402,F401
+from .vector import (Curl, CurlOperator, Divergence, DivergenceOperator, Gradient, GradientOperator,  # noqa: E402,F401
+                     cross_product, cross_product_, dot_product, dot_product_, square_norm, square_norm_)

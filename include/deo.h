@@ -267,6 +267,47 @@ deo_status deo_nonlinear_diffusion_plan(int second_order, int first_order, int a
 deo_status deo_nonlinear_diffusion(const deo_nld* plan, const void* p, const void* q, void* du, void* stream);
 void deo_nonlinear_diffusion_destroy(deo_nld* plan);
 
+/* ------------------------------------------------------------------------
+ * Vector calculus on padded arrays.
+ * Replaces `A * M` and `mul!(x_temp, .., A, M)` for A = Gradient / Divergence /
+ * Curl(approx_order, dx, len; coeff_func) (vector_calculus_operators.jl:7-73,
+ * vector_calculus_convolutions.jl).  ops[a] is the operator of axis a+1, i.e.
+ * the reference's A.ops[a+1] = CenteredDifference{a+1}(1, approx_order, dx[a+1],
+ * len[a+1], coeff_func) (its `c * A` scales each op's coefficients).
+ *   DEO_VC_GRADIENT:   M (len1+2, .., lenN+2)    -> out (len1, .., lenN, N)
+ *   DEO_VC_DIVERGENCE: M (len1+2, .., lenN+2, N) -> out (len1, .., lenN)
+ *   DEO_VC_CURL:       M (len+2, len+2, len+2, 3) -> out (len, len, len, 3)
+ * N = 2 and 3 follow the reference's specialised methods, including their
+ * indexing: along the differentiated axis the taps read the padded line, on
+ * the other axes the point at the padded index equal to the output index
+ * (x[i + idx - mid, j] for output (i, j)); each output adds its terms as the
+ * reference's BC_left / interior / BC_right passes do.  Other N follow the
+ * generic per-line methods (other axes at index + 1).  Column-major arrays.
+ * overwrite = 1 gives `A * M` (from zeros); 0 adds into out, as the
+ * reference's mul! always does.  out must not overlap M.
+ * ---------------------------------------------------------------------- */
+#define DEO_VC_GRADIENT 0
+#define DEO_VC_DIVERGENCE 1
+#define DEO_VC_CURL 2
+typedef struct deo_vc deo_vc;
+deo_status deo_vector_calculus_plan(int kind, int ndims, const deo_operator* const* ops, deo_dtype dtype,
+                                    deo_vc** out);
+/* Elements of M and of out (all components). */
+deo_status deo_vector_calculus_sizes(const deo_vc* plan, int64_t* in_elems, int64_t* out_elems);
+deo_status deo_vector_calculus_apply(const deo_vc* plan, const void* M, void* out, int overwrite, void* stream);
+void deo_vector_calculus_destroy(deo_vc* plan);
+
+/* Pointwise vector algebra over npts points of ncomp components stored
+ * component after component (an (s..., ncomp) column-major array).
+ * dot_product!(u, A, B) (vector_algebraic_operations.jl:11-28),
+ * cross_product!(u, A, B) (:39-52; ncomp = 3, u has 3 components),
+ * square_norm!(u, A) (:54-62).  Products are rounded before the sums.  u must
+ * not overlap the inputs. */
+deo_status deo_dot_product(deo_dtype dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,
+                           void* stream);
+deo_status deo_cross_product(deo_dtype dtype, int64_t npts, const void* A, const void* B, void* u, void* stream);
+deo_status deo_square_norm(deo_dtype dtype, int64_t npts, int ncomp, const void* A, void* u, void* stream);
+
 /* Concretisation on the device: A_l (n x n, column-major, n = prod(sizes)) and
  * A_b (n) of the affine map, by applying the plan to unit vectors in batches.
  * For checking small operators (n <= 8192).  Allocates device scratch. */

@@ -1023,4 +1023,138 @@ int orc_ssprk3(int nterms, void* const* ops, const int* axes, const void* bcs, c
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Gradient / Divergence / Curl on padded arrays
+// (vector_calculus_operators.jl:47-73, vector_calculus_convolutions.jl).
+// kind 0 Gradient: M (s1+2, .., sN+2) -> out (s1, .., sN, N);
+// kind 1 Divergence: M (s1+2, .., sN+2, N) -> out (s1, .., sN);
+// kind 2 Curl: M (s+2, s+2, s+2, 3) -> out (s, s, s, 3).
+// ops[a] is the operator of axis a+1 (CenteredDifference{a+1}(1, ...)).
+// N = 2, 3 follow the specialised methods (:186-838 and the curl's :844-1067):
+// each pass adds to out (`x_temp[...] += ...`) in the order BC_left, interior,
+// BC_right, axes in order within each; the axes other than the differentiated
+// one are read at the padded array's index equal to the output index
+// (x[i + idx - mid, j], not x[i + idx - mid, j + 1]); the right boundary rows
+// use coefficients[i].  Other N follow the generic per-line methods (:1-170),
+// one operator after the other, on the minimally padded views (other axes at
+// index + 1), whose right boundary rows read coefficients[1:bpc].
+// overwrite = 1 starts from zeros (the `*` methods), 0 adds to out (mul!).
+// absolute = 1 (with |tables| operators and |M|) gives sum_k |c_k u_k|.
+// ---------------------------------------------------------------------------
+namespace {
+struct VcTerm {
+    int in, out;  // component read (-1: scalar M) and written (-1: scalar out)
+    double sg;    // -1 where the reference negates the coefficient (`-cur_coeff * ...`)
+};
+int vc_terms(int kind, int a, VcTerm* t) {
+    if (kind == 0) {
+        t[0] = VcTerm{-1, a, 1.0};
+        return 1;
+    }
+    if (kind == 1) {
+        t[0] = VcTerm{a, -1, 1.0};
+        return 1;
+    }
+    // Curl, vector_calculus_convolutions.jl:871-907: along axis 1 x2 -= D u3, x3 += D u2;
+    // axis 2: x1 += D u3, x3 -= D u1; axis 3: x1 -= D u2, x2 += D u1.
+    static const VcTerm curl[3][2] = {{{2, 1, -1.0}, {1, 2, 1.0}},
+                                      {{2, 0, 1.0}, {0, 2, -1.0}},
+                                      {{1, 0, -1.0}, {0, 1, 1.0}}};
+    t[0] = curl[a][0];
+    t[1] = curl[a][1];
+    return 2;
+}
+}  // namespace
+
+int orc_vector_calculus(int kind, int nd, void* const* ops_, const double* M, double* out, int overwrite,
+                        int absolute) {
+    if (kind < 0 || kind > 2 || nd < 1 || nd > 8 || (kind == 2 && nd != 3)) return -1;
+    const Op* ops[8];
+    long s[8], ps[8], os[8], pvol = 1, ovol = 1;
+    for (int a = 0; a < nd; ++a) {
+        ops[a] = static_cast<const Op*>(ops_[a]);
+        s[a] = ops[a]->len;
+        ps[a] = pvol;
+        os[a] = ovol;
+        pvol *= s[a] + 2;
+        ovol *= s[a];
+    }
+    const int ncomp = kind == 1 ? 1 : (kind == 0 ? nd : 3);
+    if (overwrite)
+        for (long n = 0; n < ovol * ncomp; ++n) out[n] = 0.0;
+    g_abs = absolute != 0;
+    if (nd == 2 || nd == 3) {
+        const int bpc = ops[0]->bpc, stl = ops[0]->stl, bstl = ops[0]->bstl, mid = stl / 2;
+        for (int ph = 0; ph < 3; ++ph) {  // convolve_BC_left!, convolve_interior!, convolve_BC_right!
+            for (int a = 0; a < nd; ++a) {
+                const Op& A = *ops[a];
+                VcTerm tt[2];
+                const int nt = vc_terms(kind, a, tt);
+                for (long n = 0; n < ovol; ++n) {
+                    long o[3], r = n;
+                    for (int b = 0; b < nd; ++b) {
+                        o[b] = r % s[b];
+                        r /= s[b];
+                    }
+                    const long i = o[a] + 1, L = s[a];
+                    const int phase = i <= bpc ? 0 : (i <= L - bpc ? 1 : 2);
+                    if (phase != ph) continue;
+                    long q = 0;  // other axes at the padded index equal to the output index
+                    for (int b = 0; b < nd; ++b)
+                        if (b != a) q += o[b] * ps[b];
+                    const double* cs;
+                    int nk;
+                    long p0;  // first tap, 1-based padded position along axis a
+                    if (phase == 0) {
+                        cs = A.lo((int)i - 1);
+                        nk = bstl;
+                        p0 = 1;
+                    } else if (phase == 1) {
+                        cs = A.uniform ? A.st(0) : A.st((int)(i - bpc - 1));
+                        nk = stl;
+                        p0 = i - mid + 1;
+                    } else {
+                        cs = A.hi((int)(i - (L - bpc) - 1));
+                        nk = bstl;
+                        p0 = L - bstl + 3;
+                    }
+                    const double cc = A.coeff[i - 1];
+                    for (int k = 0; k < nt; ++k) {
+                        const double* x = M + (tt[k].in < 0 ? 0 : tt[k].in * pvol) + q;
+                        double acc = 0.0;
+                        for (int idx = 0; idx < nk; ++idx) acc += T3(tt[k].sg * cc, cs[idx], x[(p0 + idx - 1) * ps[a]]);
+                        double& y = out[n + (tt[k].out < 0 ? 0 : tt[k].out * ovol)];
+                        y = y + acc;
+                    }
+                }
+            }
+        }
+    } else {
+        if (kind == 2) {
+            g_abs = false;
+            return -1;
+        }
+        for (int a = 0; a < nd; ++a) {  // `for L in A.ops  mul!(x_temp, has_vector, L, M)`
+            const Op& A = *ops[a];
+            const long L = s[a], nlines = ovol / L;
+            for (long line = 0; line < nlines; ++line) {
+                long r = line, q = 0, ob = 0;
+                for (int b = 0; b < nd; ++b) {
+                    if (b == a) continue;
+                    const long c = r % s[b];
+                    r /= s[b];
+                    q += (c + 1) * ps[b];
+                    ob += c * os[b];
+                }
+                const double* x = M + (kind == 1 ? a * pvol : 0) + q;
+                Line Ln{x + ps[a], ps[a], x[0], x[(L + 1) * ps[a]], L};
+                double* y = out + ob + (kind == 0 ? a * ovol : 0);
+                apply_line(A, Ln, y, os[a], VecCoeff{A.coeff.data(), 1}, false, 0);
+            }
+        }
+    }
+    g_abs = false;
+    return 0;
+}
+
 }  // extern "C"

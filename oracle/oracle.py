@@ -65,6 +65,7 @@ def lib():
         L.orc_array_bc.argtypes = [C.c_void_p, C.c_long, _dp, _dp]
         L.orc_ssprk3.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
                                  C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, C.c_double, C.c_int, C.c_int]
+        L.orc_vector_calculus.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_void_p), _dp, _dp, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -315,6 +316,64 @@ def nonlinear_diffusion(n: int, m: int, approx: int, p, q, dx, nknots: int, abso
         b = b * (n - ell + 1) // ell
         du = du + (float(b) * D(ell + m, q)) * D(n - ell, p)
     return du + D(m + n, q) * pp[1:nknots + 1]
+
+
+GRADIENT, DIVERGENCE, CURL = 0, 1, 2
+
+
+def vector_calculus(kind: int, ops, M, out=None, overwrite: bool = True, absolute: bool = False) -> np.ndarray:
+    """Gradient (kind 0), Divergence (1) or Curl (2) of the padded array M as
+    the reference computes `A * M` (overwrite) or `mul!(out, .., A, M)`
+    (vector_calculus_operators.jl:47-73, vector_calculus_convolutions.jl),
+    restated in deo_oracle.cpp (orc_vector_calculus).  ops[a] is the operator
+    of axis a+1.  M and the result are Fortran-ordered: Gradient M has size
+    len + 2 on every axis and the result (len..., N); Divergence M has
+    (len + 2..., N) and the result (len...); Curl M has (len + 2 ...,3) and the
+    result (len..., 3).  absolute=True gives sum_k |c_k u_k| per entry."""
+    nd = len(ops)
+    lens = [op.len for op in ops]
+    shape = tuple(lens) + ((nd,) if kind == GRADIENT else ((3,) if kind == CURL else ()))
+    x = np.asfortranarray(np.abs(M) if absolute else M, dtype=np.float64)
+    use = [op.abs() for op in ops] if absolute else list(ops)
+    o = np.zeros(shape, order="F") if out is None else out
+    assert o.flags.f_contiguous and o.dtype == np.float64 and o.shape == shape
+    handles = (C.c_void_p * nd)(*[op.h.value for op in use])
+    rc = lib().orc_vector_calculus(kind, nd, handles, x.ctypes.data_as(_dp), o.ctypes.data_as(_dp),
+                                   int(overwrite or absolute), int(absolute))
+    if rc != 0:
+        raise AssertionError("invalid vector-calculus arguments")
+    return o
+
+
+def dot_product(A, B) -> np.ndarray:
+    """dot_product(A, B) (vector_algebraic_operations.jl:3-28): sum over the
+    last axis of A .* B, components added in order from zero, each product
+    rounded (plain Julia arithmetic)."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    u = np.zeros(A.shape[:-1])
+    for i in range(A.shape[-1]):
+        u = u + A[..., i] * B[..., i]
+    return u
+
+
+def cross_product(A, B) -> np.ndarray:
+    """cross_product(A, B) (vector_algebraic_operations.jl:30-52) of two
+    (s1, s2, s3, 3) arrays, each product rounded before the difference."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    u = np.empty(A.shape, order="F")
+    u[..., 0] = A[..., 1] * B[..., 2] - A[..., 2] * B[..., 1]
+    u[..., 1] = A[..., 2] * B[..., 0] - A[..., 0] * B[..., 2]
+    u[..., 2] = A[..., 0] * B[..., 1] - A[..., 1] * B[..., 0]
+    return u
+
+
+def square_norm(A) -> np.ndarray:
+    """square_norm(A) (vector_algebraic_operations.jl:54-62): dot_product(A, A)
+    then `u .^ 0.5`, taken here as the correctly rounded square root (Julia's
+    Float64 power is within one ulp of it)."""
+    return np.sqrt(dot_product(A, A))
 
 
 def ulp_tolerance(terms, u: np.ndarray, n_ulp: float = 4.0) -> np.ndarray:
