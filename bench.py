@@ -629,6 +629,59 @@ def run_reference(args, ws, rank):
     }
 
 
+def run_vector(args):
+    """Gradient, Divergence and Curl (4th order, uniform grid) of 256^3 padded
+    arrays, Float64 and Float32: device time per apply, grid points/s, the
+    algorithmic bytes (padded input components once, output components once)
+    against the measured HBM copy rate, and for Float64 the FP64 instructions
+    per point (NK fused multiply-adds per derivative, the adds between terms)
+    against the FP64 issue rate measured on this part (1.68 per clock per SM).
+    cpu_baseline: the oracle (one thread) on a 64^3 sample of the same operator."""
+    import time
+
+    import torch
+
+    import deo
+    n = args.n
+    hbm, _ = peaks()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    fp64_rate = 1.68 * sms * 2.07e9  # FP64 instructions/s at the maximum SM clock
+    lines = []
+    for kind, ctor, cin, cout, fp64 in (("gradient", deo.Gradient, 1, 3, 15), ("divergence", deo.Divergence, 3, 1, 17),
+                                        ("curl", deo.Curl, 3, 3, 33)):
+        for dt, es, name in ((torch.float64, 8, "f64"), (torch.float32, 4, "f32")):
+            A = ctor(4, (1.0 / (n + 1),) * 3, (n, n, n))
+            M = deo.julia_array(A.in_shape(), dt)
+            M.normal_(generator=torch.Generator(device="cuda").manual_seed(SEED))
+            out = deo.julia_array(A.out_shape(), dt)
+            t = _event_time(lambda: A.mul_(out, M, overwrite=True), args.steps, max(args.warmup, 3))
+            byts = es * ((n + 2) ** 3 * cin + n ** 3 * cout)
+            rec = {"op": kind, "dtype": name, "us_per_apply": t * 1e6, "grid_pts_per_s": n ** 3 / t,
+                   "GBps": byts / t / 1e9, "frac_hbm": byts / t / 1e9 / hbm}
+            if name == "f64":
+                rec["fp64_instr_per_pt"] = fp64
+                rec["frac_fp64_issue"] = fp64 * n ** 3 / t / fp64_rate
+            lines.append(rec)
+    cpu = None
+    if not args.no_cpu:
+        import numpy as np
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        m = 64
+        ops = [O.centered(1, 4, 1.0 / (m + 1), m, axis=a + 1) for a in range(3)]
+        Mh = np.asfortranarray(np.random.default_rng(SEED).standard_normal((m + 2,) * 3))
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 10.0:
+            O.vector_calculus(O.GRADIENT, ops, Mh)
+            reps += 1
+        cpu = {"value": reps * m ** 3 / (time.perf_counter() - t0), "unit": "grid-pts/s", "cores": 1, "kind": "port",
+               "sample": f"oracle Gradient on 64^3 Float64, {reps} applies in ~10 s"}
+    return {"metric": "grid-pts/s (Gradient 256^3 f64, 4th order)", "workload": f"vector_calculus_{n}^3",
+            "value": lines[0]["grid_pts_per_s"], "unit": "grid-pts/s", "dtype": "f64", "applies": lines,
+            "cpu_baseline": cpu, "gpu_launches_per_apply": 1}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -636,7 +689,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lap3d",
-                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld"])
+                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld", "vector"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=64)
@@ -645,11 +698,11 @@ def main():
     ap.add_argument("--serve-baseline", action="store_true")
     ap.add_argument("--batch-config", default="", help="tile,ctas_per_sm for the batch workload (skips autotuning)")
     args = ap.parse_args()
-    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld"):
+    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld", "vector"):
         import torch
         torch.cuda.set_device(0)
         fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "batch": run_batch,
-              "serve": run_serve, "nld": run_nld}[args.workload]
+              "serve": run_serve, "nld": run_nld, "vector": run_vector}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     if args.warmup < 3:

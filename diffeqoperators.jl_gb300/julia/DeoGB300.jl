@@ -169,4 +169,46 @@ function ChainRulesCore.rrule(::typeof(*), A::DeoOp, u::CuArray{T}) where {T <: 
     return y, pullback
 end
 
+# ---- vector calculus (vector_calculus_operators.jl, vector_calculus_convolutions.jl) ----
+const VC_PLANS = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
+_vc_kind(::GradientOperator) = 0
+_vc_kind(::DivergenceOperator) = 1
+_vc_kind(::CurlOperator) = 2
+const DeoVC = Union{GradientOperator, DivergenceOperator, CurlOperator}
+
+function vc_plan_for(A::DeoVC, ::Type{T}) where {T <: Union{Float32, Float64}}
+    cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), VC_PLANS, A)
+    get!(cache, T) do
+        ops = [deo_operator(L) for L in vec(A.ops)]
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        GC.@preserve ops check(ccall((:deo_vector_calculus_plan, libdeo), Cint,
+                                     (Cint, Cint, Ptr{Ptr{Cvoid}}, Cint, Ref{Ptr{Cvoid}}),
+                                     _vc_kind(A), length(ops), ops, T === Float64 ? 0 : 1, h))
+        foreach(op -> ccall((:deo_operator_destroy, libdeo), Cvoid, (Ptr{Cvoid},), op), ops)
+        h[]
+    end
+end
+
+function _vc_apply!(x_temp::CuArray{T}, A::DeoVC, M::CuArray{T}, overwrite) where {T <: Union{Float32, Float64}}
+    check(ccall((:deo_vector_calculus_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Cint, Ptr{Cvoid}),
+                vc_plan_for(A, T), M, x_temp, overwrite, _stream()))
+    return x_temp
+end
+
+# mul! accumulates, as the reference's methods do
+LinearAlgebra.mul!(x_temp::CuArray{T}, has_vector::Bool, A::Union{GradientOperator, DivergenceOperator},
+                   M::CuArray{T}; overwrite = false) where {T <: Union{Float32, Float64}} = _vc_apply!(x_temp, A, M, 0)
+LinearAlgebra.mul!(x_temp::CuArray{T, 4}, A::CurlOperator, M::CuArray{T, 4};
+                   overwrite = false) where {T <: Union{Float32, Float64}} = _vc_apply!(x_temp, A, M, 0)
+
+function Base.:*(A::GradientOperator, M::CuArray{T, N}) where {T <: Union{Float32, Float64}, N}
+    _vc_apply!(CuArray{T}(undef, (size(M) .- 2)..., N), A, M, 1)
+end
+function Base.:*(A::DivergenceOperator, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+    _vc_apply!(CuArray{T}(undef, (size(M)[1:(end - 1)] .- 2)...), A, M, 1)
+end
+function Base.:*(A::CurlOperator, M::CuArray{T, 4}) where {T <: Union{Float32, Float64}}
+    _vc_apply!(CuArray{T}(undef, (size(M)[1:3] .- 2)..., 3), A, M, 1)
+end
+
 end # module
