@@ -22,6 +22,7 @@ SOURCES = {
     "deo_shell.o": ("nvcc", "deo_shell.cu"),
     "deo_static.o": ("nvcc", "deo_static.cu"),
     "deo_vector.o": ("nvcc", "deo_vector.cu"),
+    "deo_solve.o": ("nvcc", "deo_solve.cu"),
     "deo_host.o": ("cxx", "deo_host.cpp"),
 }
 

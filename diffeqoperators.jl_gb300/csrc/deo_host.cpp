@@ -466,12 +466,13 @@ extern "C" deo_status deo_bc_array(const deo_bc* b, int N, double* QL, double* Q
 // ---------------------------------------------------------------------------
 // Array(L): concretization.jl:8-52 (centred) and :556-671 (upwind)
 // ---------------------------------------------------------------------------
-extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
-    if (!op || !M) return fail(DEO_ERR_BAD_ARG, "null argument");
+// The entries of Array(L) in the reference's assignment order: set(i, j, v)
+// for row i (1..len) and padded column j (1..len+2); later calls overwrite.
+template <class Set>
+static void array_entries(const deo_operator* op, Set set_any) {
     const long N = op->len;
-    std::fill(M, M + N * (N + 2), 0.0);
     auto set = [&](long i, long j, double v) {
-        if (i >= 1 && i <= N && j >= 1 && j <= N + 2) M[(j - 1) * N + (i - 1)] = v;
+        if (i >= 1 && i <= N && j >= 1 && j <= N + 2) set_any(i, j, v);
     };
     const int bl = op->bpc, stl = op->stl, bstl = op->bstl, off = op->off;
     auto c = [&](long i) { return op->coeff[i - 1]; };
@@ -485,7 +486,7 @@ extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
         }
         for (long i = N - bl + 1; i <= N; ++i)
             for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, c(i) * op->Hi((int)(i - N + bl - 1))[k]);
-        return DEO_OK;
+        return;
     }
     const double sg = (op->d % 2 == 0) ? 1.0 : -1.0;
     if (op->uniform) {
@@ -515,7 +516,7 @@ extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
             else
                 for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, ci * op->Hi(r - 1)[k]);
         }
-        return DEO_OK;
+        return;
     }
     for (int i = 1; i <= bl; ++i) {
         if (c(i) >= 0 && off == 0)
@@ -544,6 +545,14 @@ extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
         else
             for (int k = 0; k < bstl; ++k) set(i, N - bstl + 3 + k, c(i) * op->Hi(hr, 0)[k]);
     }
+    return;
+}
+
+extern "C" deo_status deo_operator_array(const deo_operator* op, double* M) {
+    if (!op || !M) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const long N = op->len;
+    std::fill(M, M + N * (N + 2), 0.0);
+    array_entries(op, [&](long i, long j, double v) { M[(j - 1) * N + (i - 1)] = v; });
     return DEO_OK;
 }
 
@@ -1513,6 +1522,204 @@ extern "C" deo_status deo_square_norm(deo_dtype dtype, int64_t npts, int ncomp, 
                                       void* stream) {
     return vector_algebra(2, dtype, npts, ncomp, A, nullptr, u, stream);
 }
+
+// ---------------------------------------------------------------------------
+// A \ u for A = L*Q (ghost_derivative_operator.jl:39-58): the reference
+// concretises (A_l, A_b) = sparse(A) (concretization.jl:938-958: sparse(L) *
+// sparse(Q)) and solves A_l x = u - A_b with a sparse LU.  Here A_l is the
+// same len x len band on every line along the operator's axis, factored once
+// on the host (partial pivoting), and every line is solved on the device.
+// ---------------------------------------------------------------------------
+struct deo_solve {
+    int n = 0, kl = 0, ku = 0, ldab = 0, dtype = 0;
+    int64_t stride = 1, nlines = 0, total = 0;
+    double* d_ab = nullptr;   // LU factors, band storage [ldab][n] (row r holds diagonal kl+ku-r)
+    int* d_ipiv = nullptr;
+    double* d_b = nullptr;    // A_b
+    double* d_rdiag = nullptr; // 1 / U[j][j]
+    double* d_work = nullptr; // Float32 plans: the lines in Float64 while they are solved
+    ~deo_solve() {
+        if (d_rdiag) cudaFree(d_rdiag);
+        if (d_ab) cudaFree(d_ab);
+        if (d_ipiv) cudaFree(d_ipiv);
+        if (d_b) cudaFree(d_b);
+        if (d_work) cudaFree(d_work);
+    }
+};
+
+// (A_l, A_b) of L*Q as sparse rows: A_l[i] = {column (1..n) -> value}, the
+// products L[i,j] * Q[j,c] summed in increasing j as the sparse product does.
+static deo_status ghost_rows(const deo_operator& op, const deo_bc& q, std::vector<std::vector<std::pair<long, double>>>& A,
+                             std::vector<double>& Ab) {
+    const long N = op.len;
+    std::vector<std::vector<std::pair<long, double>>> Lr(N);
+    array_entries(&op, [&](long i, long j, double v) {
+        auto& r = Lr[i - 1];
+        for (auto& e : r)
+            if (e.first == j) {
+                e.second = v;
+                return;
+            }
+        r.emplace_back(j, v);
+    });
+    if (q.kind == DEO_BC_AFFINE && (q.m_l > N || q.m_r > N)) return fail(DEO_ERR_BAD_SHAPE, "BC stencil longer than N");
+    A.assign(N, {});
+    Ab.assign(N, 0.0);
+    for (long i = 0; i < N; ++i) {
+        auto& r = Lr[i];
+        std::sort(r.begin(), r.end());
+        auto add = [&](long c, double v) {
+            for (auto& e : A[i])
+                if (e.first == c) {
+                    e.second = e.second + v;
+                    return;
+                }
+            A[i].emplace_back(c, v);
+        };
+        bool have_b = false;
+        for (const auto& e : r) {
+            const long j = e.first;
+            const double v = e.second;
+            if (j == 1 || j == N + 2) {  // a ghost: its row of Q
+                if (q.kind == DEO_BC_PERIODIC) {  // Array(PeriodicBC, N): ghost_l = u[N], ghost_r = u[1]
+                    add(j == 1 ? N : 1, v);
+                } else {
+                    const int m = j == 1 ? q.m_l : q.m_r;
+                    const double* a = j == 1 ? q.a_l : q.a_r;
+                    const long c0 = j == 1 ? 1 : N - q.m_r + 1;
+                    for (int k = 0; k < m; ++k) add(c0 + k, v * a[k]);
+                    const double bv = v * (j == 1 ? q.b_l : q.b_r);
+                    Ab[i] = have_b ? Ab[i] + bv : bv;
+                    have_b = true;
+                }
+            } else {
+                add(j - 1, v);
+            }
+        }
+    }
+    // columns in increasing order within each row, with the sums above done in
+    // increasing j: re-sort only for the band placement below
+    for (auto& r : A) std::sort(r.begin(), r.end());
+    return DEO_OK;
+}
+
+// Banded LU with partial pivoting (the unblocked LAPACK gbtf2 scheme) of the
+// n x n band with kl sub- and ku super-diagonals in AB[(kl+ku+r)...]: row r of
+// AB holds diagonal (kl + ku - r) -- entry (i, j) at AB[(kl + ku + i - j) * n + j];
+// rows 0..kl-1 receive the fill-in.
+static bool band_lu(int n, int kl, int ku, std::vector<double>& AB, std::vector<int>& ipiv) {
+    const int kv = kl + ku;
+    auto at = [&](long i, long j) -> double& { return AB[(size_t)(kv + i - j) * n + j]; };
+    ipiv.assign(n, 0);
+    long ju = 0;
+    for (long j = 0; j < n; ++j) {
+        const long km = std::min<long>(kl, n - 1 - j);
+        long jp = 0;
+        double best = std::fabs(at(j, j));
+        for (long r = 1; r <= km; ++r)
+            if (std::fabs(at(j + r, j)) > best) {
+                best = std::fabs(at(j + r, j));
+                jp = r;
+            }
+        ipiv[j] = (int)(j + jp);
+        if (at(j + jp, j) == 0.0) return false;
+        ju = std::max(ju, std::min<long>(j + ku + jp, n - 1));
+        if (jp != 0)
+            for (long c = j; c <= ju; ++c) std::swap(at(j, c), at(j + jp, c));
+        const double piv = at(j, j);
+        for (long r = 1; r <= km; ++r) at(j + r, j) = at(j + r, j) / piv;
+        for (long c = j + 1; c <= ju; ++c) {
+            const double u = at(j, c);
+            if (u == 0.0) continue;
+            for (long r = 1; r <= km; ++r) at(j + r, c) = at(j + r, c) - at(j + r, j) * u;
+        }
+    }
+    return true;
+}
+
+extern "C" deo_status deo_solve_plan(const deo_operator* op, const deo_bc* bc, int ndims, const int64_t* sizes, int axis,
+                                     deo_dtype dtype, deo_solve** out) {
+    if (!op || !bc || !sizes || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
+    if (axis < 1 || axis > ndims) return fail(DEO_ERR_BAD_SHAPE, "axis %d outside 1..%d", axis, ndims);
+    if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
+    if (sizes[axis - 1] != op->len)
+        return fail(DEO_ERR_BAD_SHAPE, "size(u, %d) = %lld but the operator has len %d", axis,
+                    (long long)sizes[axis - 1], op->len);
+    const long N = op->len;
+    std::vector<std::vector<std::pair<long, double>>> A;
+    std::vector<double> Ab;
+    deo_status st = ghost_rows(*op, *bc, A, Ab);
+    if (st != DEO_OK) return st;
+    int kl = 0, ku = 0;
+    for (long i = 0; i < N; ++i)
+        for (const auto& e : A[i]) {
+            const long c = e.first - 1;
+            kl = std::max<int>(kl, (int)(i - c));
+            ku = std::max<int>(ku, (int)(c - i));
+        }
+    const int ldab = 2 * kl + ku + 1;
+    if ((double)ldab * (double)N > 6.4e7)
+        return fail(DEO_ERR_UNSUPPORTED, "the band of A_l (%d sub-, %d super-diagonals, n = %ld) is too wide to factor",
+                    kl, ku, N);
+    std::vector<double> AB((size_t)ldab * N, 0.0);
+    for (long i = 0; i < N; ++i)
+        for (const auto& e : A[i]) {
+            const long j = e.first - 1;
+            AB[(size_t)(kl + ku + i - j) * N + j] = e.second;
+        }
+    std::vector<int> ipiv;
+    if (!band_lu((int)N, kl, ku, AB, ipiv))
+        return fail(DEO_ERR_BAD_ARG, "A_l is singular (the operator with this boundary condition has no inverse)");
+    auto S = std::make_unique<deo_solve>();
+    S->n = (int)N;
+    S->kl = kl;
+    S->ku = ku;
+    S->ldab = ldab;
+    S->dtype = dtype;
+    int64_t stride = 1, total = 1;
+    for (int k = 0; k < ndims; ++k) {
+        if (sizes[k] < 1) return fail(DEO_ERR_BAD_SHAPE, "size(u, %d) = %lld", k + 1, (long long)sizes[k]);
+        if (k < axis - 1) stride *= sizes[k];
+        total *= sizes[k];
+    }
+    S->stride = stride;
+    S->total = total;
+    S->nlines = total / N;
+    CUDA_TRY(cudaMalloc(&S->d_ab, AB.size() * sizeof(double)), "cudaMalloc(LU factors)");
+    CUDA_TRY(cudaMemcpy(S->d_ab, AB.data(), AB.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    CUDA_TRY(cudaMalloc(&S->d_ipiv, ipiv.size() * sizeof(int)), "cudaMalloc(pivots)");
+    CUDA_TRY(cudaMemcpy(S->d_ipiv, ipiv.data(), ipiv.size() * sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    CUDA_TRY(cudaMalloc(&S->d_b, Ab.size() * sizeof(double)), "cudaMalloc(A_b)");
+    CUDA_TRY(cudaMemcpy(S->d_b, Ab.data(), Ab.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    std::vector<double> rdiag(N);
+    for (long j = 0; j < N; ++j) rdiag[j] = 1.0 / AB[(size_t)(kl + ku) * N + j];
+    CUDA_TRY(cudaMalloc(&S->d_rdiag, rdiag.size() * sizeof(double)), "cudaMalloc(pivots)");
+    CUDA_TRY(cudaMemcpy(S->d_rdiag, rdiag.data(), rdiag.size() * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    if (dtype == DEO_F32) CUDA_TRY(cudaMalloc(&S->d_work, (size_t)total * sizeof(double)), "cudaMalloc(workspace)");
+    *out = S.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_solve_bands(const deo_solve* s, int* kl, int* ku) {
+    if (!s) return fail(DEO_ERR_BAD_ARG, "null plan");
+    if (kl) *kl = s->kl;
+    if (ku) *ku = s->ku;
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_solve_apply(const deo_solve* s, const void* u, void* x, void* stream) {
+    if (!s || !u || !x) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const size_t es = s->dtype == DEO_F64 ? 8 : 4, bytes = (size_t)s->total * es;
+    if (u != x && overlaps(u, bytes, x, bytes)) return fail(DEO_ERR_BAD_ARG, "x must be u itself or not overlap it");
+    const int e = deo_k_band_solve(s->n, s->kl, s->ku, s->d_ab, s->d_ipiv, s->d_b, s->d_rdiag, s->stride, s->nlines,
+                                   s->dtype, u, x, s->d_work, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_solve_apply launch");
+    return DEO_OK;
+}
+
+extern "C" void deo_solve_destroy(deo_solve* s) { delete s; }
 
 extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double* Ab) {
     if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");

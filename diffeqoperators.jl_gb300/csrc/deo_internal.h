@@ -212,6 +212,14 @@ extern "C" int deo_k_vector_calculus(const deo::VcDev* V, int dtype, const void*
 extern "C" int deo_k_vector_algebra(int op, int dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,
                                     void* stream);
 
+// Launcher implemented in deo_solve.cu: every line along an axis (stride, n
+// points) of u solved with the banded LU factors ab ([kl+ku+kl+1][n]), pivots
+// ipiv, reciprocal pivots rdiag and offset Ab: x = A_l^-1 (u - A_b).  x may be
+// u.  work: null for Float64 (x is the workspace), else total doubles.
+extern "C" int deo_k_band_solve(int n, int kl, int ku, const double* ab, const int* ipiv, const double* Ab,
+                                const double* rdiag, int64_t stride, int64_t nlines, int dtype, const void* u, void* x,
+                                double* work, void* stream);
+
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
                            void* stream);

@@ -19,8 +19,8 @@ from .operators import (  # noqa: F401
     AtomicBC, CenteredDifference, ComposedMultiDimBC, DerivativeOperator, DiffEqOperatorCombination,
     DimensionMismatch, Dirichlet0BC, DirichletBC, FieldCoefficient, GeneralBC, GhostDerivativeOperator,
     MultiDimBC, MultiDimDirectionalBC, Neumann0BC, NeumannBC, PeriodicBC, Plan, RobinBC, UpwindDifference,
-    calculate_weights, clear_plan_cache, compose, concretize, fortran_strides, julia_array, mul_,
-    operator_from_tables, plan_for, to_julia_layout, with_field,
+    calculate_weights, clear_plan_cache, compose, concretize, fortran_strides, julia_array, ldiv, ldiv_, mul_,
+    operator_from_tables, plan_for, SolvePlan, solve_plan_for, to_julia_layout, with_field,
 )
 
 mul = mul_

@@ -121,6 +121,10 @@ def lib():
           C.POINTER(_vp))
     proto("deo_nonlinear_diffusion", st, _vp, _vp, _vp, _vp, _vp)
     proto("deo_nonlinear_diffusion_destroy", None, _vp)
+    proto("deo_solve_plan", st, _vp, _vp, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(_vp))
+    proto("deo_solve_bands", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int))
+    proto("deo_solve_apply", st, _vp, _vp, _vp, _vp)
+    proto("deo_solve_destroy", None, _vp)
     proto("deo_vector_calculus_plan", st, C.c_int, C.c_int, C.POINTER(_vp), C.c_int, C.POINTER(_vp))
     proto("deo_vector_calculus_sizes", st, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64))
     proto("deo_vector_calculus_apply", st, _vp, _vp, _vp, C.c_int, _vp)
@@ -168,4 +172,5 @@ EXPORTED = [
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply",
     "deo_vector_calculus_destroy", "deo_dot_product", "deo_cross_product", "deo_square_norm",
+    "deo_solve_plan", "deo_solve_bands", "deo_solve_apply", "deo_solve_destroy",
 ]

@@ -523,6 +523,12 @@ class GhostDerivativeOperator:
     def size(self):
         return (self.L.len, self.L.len)
 
+    def ldiv(self, u, x=None):
+        """A \\ u (ghost_derivative_operator.jl:39-58): x with A_l x + A_b = u, every
+        line of u along the operator's axis solved with one banded LU of A_l.
+        x (optional) receives the result; it may be u itself."""
+        return ldiv_(x, self, u) if x is not None else ldiv(self, u)
+
     def array(self, N: int | None = None):
         """Array(L*Q) = (Array(L)*Q_L, Array(L)*Q_b) (concretization.jl:914-918), 1-D."""
         if not isinstance(self.Q, AtomicBC):
@@ -530,6 +536,71 @@ class GhostDerivativeOperator:
         A = self.L.array()
         QL, Qb = self.Q.array(self.L.len)
         return A @ QL, A @ Qb
+
+
+class SolvePlan:
+    """A compiled deo_solve: A = L*Q factored for (Julia size, dtype)."""
+
+    def __init__(self, A: "GhostDerivativeOperator", shape, dtype_code: int):
+        self.shape = tuple(int(n) for n in shape)
+        nd = len(self.shape)
+        ax = A.L.axis
+        if isinstance(A.Q, AtomicBC):
+            if nd > 1 and ax != 1:
+                raise DeoShapeError(1, "an atomic BC on an N-D array extends dimension 1; use MultiDimBC")
+            bc = A.Q
+        else:
+            bc = A.Q.bc_for(ax, nd)
+        if ax > nd:
+            raise DeoShapeError(1, f"operator axis {ax} but u has {nd} dimensions")
+        sizes = (C.c_int64 * nd)(*self.shape)
+        h = C.c_void_p()
+        check(L.lib().deo_solve_plan(A.L._h, C.byref(bc._s), nd, sizes, ax, dtype_code, C.byref(h)))
+        self._h = h
+
+    def bands(self):
+        kl, ku = C.c_int(), C.c_int()
+        check(L.lib().deo_solve_bands(self._h, C.byref(kl), C.byref(ku)))
+        return kl.value, ku.value
+
+    def __del__(self):
+        try:
+            if self._h:
+                L.lib().deo_solve_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+_solve_cache: dict = {}
+
+
+def solve_plan_for(A: "GhostDerivativeOperator", shape, dtype_code: int) -> SolvePlan:
+    key = (id(A), tuple(shape), dtype_code)
+    hit = _solve_cache.get(key)
+    if hit is not None and hit[0] is A:
+        return hit[1]
+    p = SolvePlan(A, shape, dtype_code)
+    _solve_cache[key] = (A, p)
+    return p
+
+
+def ldiv_(x, A: "GhostDerivativeOperator", u):
+    """x = A \\ u on CUDA tensors in Julia layout (x may be u)."""
+    if not isinstance(A, GhostDerivativeOperator):
+        raise DeoArgError(2, "A \\ u is defined for a single L*Q (GhostDerivativeOperator)")
+    _check_layout(u, "u")
+    _check_layout(x, "x")
+    if tuple(x.shape) != tuple(u.shape) or x.dtype != u.dtype or not u.is_cuda or x.device != u.device:
+        raise DimensionMismatch("x must be a CUDA tensor of u's size and dtype")
+    p = solve_plan_for(A, tuple(u.shape), _dtype_code(u))
+    check(L.lib().deo_solve_apply(p._h, C.c_void_p(u.data_ptr()), C.c_void_p(x.data_ptr()), _stream_ptr()))
+    return x
+
+
+def ldiv(A: "GhostDerivativeOperator", u):
+    """A \\ u (ghost_derivative_operator.jl:39-58): a new array."""
+    return ldiv_(julia_array(tuple(u.shape), u.dtype, u.device), A, u)
 
 
 class DiffEqOperatorCombination:

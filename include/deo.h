@@ -268,6 +268,25 @@ deo_status deo_nonlinear_diffusion(const deo_nld* plan, const void* p, const voi
 void deo_nonlinear_diffusion_destroy(deo_nld* plan);
 
 /* ------------------------------------------------------------------------
+ * Implicit solves: x = A \ u for A = L*Q (ghost_derivative_operator.jl:39-58).
+ * The reference concretises (A_l, A_b) = sparse(A) (concretization.jl:938-958:
+ * sparse(L) * sparse(Q), Array(PeriodicBC) wrapping around) and solves
+ * A_l x = u - A_b with a sparse LU.  Here A_l, the same n x n band for every
+ * line of u along `axis` (n = the operator's len), is factored once on the
+ * host with partial pivoting (DEO_ERR_BAD_ARG if singular), and the device
+ * solves all lines.  sizes: u's Julia size.  x may be u itself (in place) but
+ * may not otherwise overlap it.  Float32 lines are solved in Float64 and
+ * rounded once.
+ * ---------------------------------------------------------------------- */
+typedef struct deo_solve deo_solve;
+deo_status deo_solve_plan(const deo_operator* op, const deo_bc* bc, int ndims, const int64_t* sizes, int axis,
+                          deo_dtype dtype, deo_solve** out);
+/* Sub- and super-diagonals of A_l. */
+deo_status deo_solve_bands(const deo_solve* plan, int* kl, int* ku);
+deo_status deo_solve_apply(const deo_solve* plan, const void* u, void* x, void* stream);
+void deo_solve_destroy(deo_solve* plan);
+
+/* ------------------------------------------------------------------------
  * Vector calculus on padded arrays.
  * Replaces `A * M` and `mul!(x_temp, .., A, M)` for A = Gradient / Divergence /
  * Curl(approx_order, dx, len; coeff_func) (vector_calculus_operators.jl:7-73,

@@ -376,6 +376,23 @@ def square_norm(A) -> np.ndarray:
     return np.sqrt(dot_product(A, A))
 
 
+def ghost_solve(op: Op, bc: BC, u: np.ndarray, axis: int = 1):
+    """A \\ u for A = L*Q (ghost_derivative_operator.jl:39-58): (A_l, A_b) =
+    Array(L) * Array(Q) (concretization.jl:914-918; Array(PeriodicBC) wraps
+    around), then A_l x = u - A_b by a dense LU (numpy), line by line along
+    `axis` (1-based) of a Fortran-ordered array.  Returns (x, cond(A_l))."""
+    Lm = op.array()
+    QL, Qb = bc.array(op.len)
+    Al = Lm @ QL
+    Ab = Lm @ Qb
+    x = np.moveaxis(np.asarray(u, dtype=np.float64), axis - 1, 0)
+    shp = x.shape
+    rhs = x.reshape(shp[0], -1) - Ab[:, None]
+    sol = np.linalg.solve(Al, rhs)
+    out = np.moveaxis(sol.reshape(shp), 0, axis - 1)
+    return np.asfortranarray(out), float(np.linalg.cond(Al))
+
+
 def ulp_tolerance(terms, u: np.ndarray, n_ulp: float = 4.0) -> np.ndarray:
     """Per-point tolerance: n_ulp units in the last place of sum_k |c_k u_k|."""
     return n_ulp * np.spacing(abs_scale(terms, u))
