@@ -682,6 +682,59 @@ def run_vector(args):
             "cpu_baseline": cpu, "gpu_launches_per_apply": 1}
 
 
+def run_solve(args):
+    """A \\ u (ghost_derivative_operator.jl:39-58) on a 256^3 Float64 array along
+    axis 3: CenteredDifference(2, a, h, 256) with RobinBC on that axis, a = 2
+    (tridiagonal A_l) and a = 4 (4 sub- and super-diagonals after pivoting).
+    Device time per solve (factors built once, in the plan), grid points/s, the
+    algorithmic bytes (u read and x written once: 16 B/pt) and the bytes moved
+    (the forward sweep's intermediate written and read back: 32 B/pt).
+    cpu_baseline: LAPACK's banded solver (scipy.linalg.solve_banded, one thread)
+    on a 4096-line sample of the same system."""
+    import time
+
+    import torch
+
+    import deo
+    n = args.n
+    h = 1.0 / (n + 1)
+    hbm, _ = peaks()
+    out = []
+    u = deo.julia_array((n, n, n), torch.float64)
+    u.normal_(generator=torch.Generator(device="cuda").manual_seed(SEED))
+    x = deo.julia_array((n, n, n), torch.float64)
+    for a in (2, 4):
+        L = deo.CenteredDifference(2, a, h, n, axis=3)
+        A = L * deo.MultiDimBC(deo.RobinBC((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), h, a), (n, n, n), 3)
+        bands = deo.solve_plan_for(A, (n, n, n), 0).bands()
+        t = _event_time(lambda: deo.ldiv_(x, A, u), args.steps, max(args.warmup, 3))
+        out.append({"approx_order": a, "bands": list(bands), "us_per_solve": t * 1e6, "grid_pts_per_s": n ** 3 / t,
+                    "GBps_algorithmic": 16 * n ** 3 / t / 1e9, "frac_hbm": 16 * n ** 3 / t / 1e9 / hbm,
+                    "GBps_moved": 32 * n ** 3 / t / 1e9})
+    cpu = None
+    if not args.no_cpu:
+        import scipy.linalg as sl
+        L = deo.CenteredDifference(2, 2, h, n)
+        Al, Ab = (L * deo.RobinBC((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), h, 2)).array()
+        kl = ku = 1
+        band = np.zeros((kl + ku + 1, n))
+        for i in range(n):
+            for j in range(max(0, i - kl), min(n, i + ku + 1)):
+                band[ku + i - j, j] = Al[i, j]
+        rhs = np.random.default_rng(SEED).standard_normal((n, 4096)) - Ab[:, None]
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < 10.0:
+            for c in range(0, 4096, 64):
+                sl.solve_banded((kl, ku), band, rhs[:, c:c + 64], check_finite=False)
+            reps += 1
+        cpu = {"value": reps * 4096 * n / (time.perf_counter() - t0), "unit": "grid-pts/s", "cores": 1,
+               "kind": "port", "sample": f"scipy.linalg.solve_banded (LAPACK gbsv), 4096 lines of {n}, {reps} passes"}
+    return {"metric": "grid-pts/s (A \\ u, 256^3 f64 along axis 3, tridiagonal)", "workload": f"ghost_solve_{n}^3_f64",
+            "value": out[0]["grid_pts_per_s"], "unit": "grid-pts/s", "dtype": "f64", "solves": out,
+            "cpu_baseline": cpu, "gpu_launches_per_solve": 1}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -689,7 +742,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lap3d",
-                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld", "vector"])
+                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld", "vector", "solve"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=64)
@@ -698,11 +751,12 @@ def main():
     ap.add_argument("--serve-baseline", action="store_true")
     ap.add_argument("--batch-config", default="", help="tile,ctas_per_sm for the batch workload (skips autotuning)")
     args = ap.parse_args()
-    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld", "vector"):
+    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld", "vector", "solve"):
         import torch
         torch.cuda.set_device(0)
         fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "batch": run_batch,
-              "serve": run_serve, "nld": run_nld, "vector": run_vector}[args.workload]
+              "serve": run_serve, "nld": run_nld, "vector": run_vector,
+              "solve": run_solve}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     if args.warmup < 3:

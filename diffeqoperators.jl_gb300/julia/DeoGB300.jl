@@ -169,6 +169,31 @@ function ChainRulesCore.rrule(::typeof(*), A::DeoOp, u::CuArray{T}) where {T <: 
     return y, pullback
 end
 
+# ---- A \ u (ghost_derivative_operator.jl:39-58): banded LU once, every line on the GPU ----
+const SOLVES = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
+
+function solve_plan_for(A::GhostDerivativeOperator, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
+    cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), SOLVES, A)
+    get!(cache, (sz, T)) do
+        op = deo_operator(A.L)
+        bc = Ref(deo_bc(_bc_for(A.Q, _axis(A.L))))
+        sizes = Int64[sz...]
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        GC.@preserve sizes check(ccall((:deo_solve_plan, libdeo), Cint,
+                                       (Ptr{Cvoid}, Ref{DeoBC}, Cint, Ptr{Int64}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                                       op, bc, length(sz), sizes, _axis(A.L), T === Float64 ? 0 : 1, h))
+        ccall((:deo_operator_destroy, libdeo), Cvoid, (Ptr{Cvoid},), op)
+        h[]
+    end
+end
+
+function Base.:\(A::GhostDerivativeOperator, u::CuArray{T}) where {T <: Union{Float32, Float64}}
+    x = similar(u)
+    check(ccall((:deo_solve_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Ptr{Cvoid}),
+                solve_plan_for(A, size(u), T), u, x, _stream()))
+    return x
+end
+
 # ---- vector calculus (vector_calculus_operators.jl, vector_calculus_convolutions.jl) ----
 const VC_PLANS = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
 _vc_kind(::GradientOperator) = 0
