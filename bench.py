@@ -24,11 +24,16 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# optional folder for the clock samples and the autotuner cache (DEO_REPORT_DIR)
+REPORT_DIR = os.environ.get("DEO_REPORT_DIR", "") or None
+if REPORT_DIR and not os.path.isdir(REPORT_DIR):
+    REPORT_DIR = None
 sys.path.insert(0, os.path.join(ROOT, "diffeqoperators.jl_gb300"))
 
 SEED = 20251203
@@ -84,8 +89,7 @@ class ClockSampler:
     def __init__(self, index: int = 0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "",
-                                 f".clocks_{os.getpid()}.csv")
+        self.path = os.path.join(REPORT_DIR or tempfile.gettempdir(), f".clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -494,8 +498,7 @@ def run_batch(args):
     else:
         bf = deo.Batch(list(zip(plans, us, fw)))
         ba = deo.Batch(list(zip(plans, fw, bw)), adjoint=True)
-        cfg_f = bf.autotune(os.path.join(ROOT, "gpurun_out", "autotune.cache") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else None)
+        cfg_f = bf.autotune(os.path.join(REPORT_DIR, "autotune.cache") if REPORT_DIR else None)
         cfg_a = ba.autotune()
 
     def batched():

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_band_solve(int n, int kl, int ku, const
 // line is read once and written once per sweep (y between the sweeps lives in
 // x for Float64, in the workspace for Float32).  The pivots U[j][j] enter as
 // their reciprocals rdiag (the GPU has no fast FP64 divide).  W >= max(kl, kl + ku).
-template <typename T, int W>
+template <typename T, int W, int PF = 8>
 __global__ void __launch_bounds__(256) k_band_solve_w(int n, int kl, int ku, const double* __restrict__ ab,
                                                       const int* __restrict__ ipiv, const double* __restrict__ Ab,
                                                       const double* __restrict__ rdiag, int64_t stride,
@@ -74,45 +74,79 @@ __global__ void __launch_bounds__(256) k_band_solve_w(int n, int kl, int ku, con
     double f[W + 1];
 #pragma unroll
     for (int r = 0; r <= W; ++r) f[r] = (r <= kl && r < n) ? (double)ul[(int64_t)r * stride] - __ldg(Ab + r) : 0.0;
-#pragma unroll 4
-    for (int j = 0; j < n; ++j) {
-        const int p = __ldg(ipiv + j) - j;  // 0 .. kl
+    // the next PF new rows' values are loaded one block of PF steps ahead
+    double cur[PF], nxt[PF];
 #pragma unroll
-        for (int r = 1; r <= W; ++r)
-            if (r == p) {
-                const double t = f[0];
-                f[0] = f[r];
-                f[r] = t;
+    for (int k = 0; k < PF; ++k) {
+        const int jn = k + 1 + kl;
+        cur[k] = jn < n ? (double)ul[(int64_t)jn * stride] - __ldg(Ab + jn) : 0.0;
+    }
+    for (int jb = 0; jb < n; jb += PF) {
+#pragma unroll
+        for (int k = 0; k < PF; ++k) {
+            const int jn = jb + PF + k + 1 + kl;
+            nxt[k] = jn < n ? (double)ul[(int64_t)jn * stride] - __ldg(Ab + jn) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < PF; ++k) {
+            const int j = jb + k;
+            if (j < n) {
+                const int p = __ldg(ipiv + j) - j;  // 0 .. kl
+#pragma unroll
+                for (int r = 1; r <= W; ++r)
+                    if (r == p) {
+                        const double t = f[0];
+                        f[0] = f[r];
+                        f[r] = t;
+                    }
+                const double bj = f[0];
+                const int km = min(kl, n - 1 - j);
+#pragma unroll
+                for (int r = 1; r <= W; ++r)
+                    if (r <= km) f[r] = fma(-__ldg(ab + (int64_t)(kv + r) * n + j), bj, f[r]);
+                y[(int64_t)j * stride] = bj;
+                const double nv = cur[k];
+#pragma unroll
+                for (int r = 0; r < W; ++r) f[r] = (r == kl) ? nv : f[r + 1];
+                if (kl == W) f[W] = nv;
             }
-        const double bj = f[0];
-        const int km = min(kl, n - 1 - j);
+        }
 #pragma unroll
-        for (int r = 1; r <= W; ++r)
-            if (r <= km) f[r] = fma(-__ldg(ab + (int64_t)(kv + r) * n + j), bj, f[r]);
-        y[(int64_t)j * stride] = bj;
-        const int jn = j + 1 + kl;
-        const double nv = jn < n ? (double)ul[(int64_t)jn * stride] - __ldg(Ab + jn) : 0.0;
-#pragma unroll
-        for (int r = 0; r < W; ++r) f[r] = (r == kl) ? nv : f[r + 1];
-        if (kl == W) f[W] = nv;
+        for (int k = 0; k < PF; ++k) cur[k] = nxt[k];
     }
     // backward: g[r] = y[j - r]
     double g[W + 1];
 #pragma unroll
     for (int r = 0; r <= W; ++r) g[r] = (r <= kv && n - 1 - r >= 0) ? y[(int64_t)(n - 1 - r) * stride] : 0.0;
-#pragma unroll 4
-    for (int j = n - 1; j >= 0; --j) {
-        const double xj = g[0] * __ldg(rdiag + j);  // one rounding more than a division, no FP64 divide
-        if (work) x[base + (int64_t)j * stride] = (T)xj;
-        else y[(int64_t)j * stride] = xj;
 #pragma unroll
-        for (int r = 1; r <= W; ++r)
-            if (r <= kv && j - r >= 0) g[r] = fma(-__ldg(ab + (int64_t)(kv - r) * n + j), xj, g[r]);
-        const int jn = j - 1 - kv;
-        const double nv = jn >= 0 ? y[(int64_t)jn * stride] : 0.0;
+    for (int k = 0; k < PF; ++k) {
+        const int jn = n - 2 - kv - k;
+        cur[k] = jn >= 0 ? y[(int64_t)jn * stride] : 0.0;
+    }
+    for (int jb = n - 1; jb >= 0; jb -= PF) {
 #pragma unroll
-        for (int r = 0; r < W; ++r) g[r] = (r == kv) ? nv : g[r + 1];
-        if (kv == W) g[W] = nv;
+        for (int k = 0; k < PF; ++k) {
+            const int jn = jb - PF - 1 - kv - k;
+            nxt[k] = jn >= 0 ? y[(int64_t)jn * stride] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < PF; ++k) {
+            const int j = jb - k;
+            if (j >= 0) {
+                const double xj = g[0] * __ldg(rdiag + j);  // one rounding more than a division, no FP64 divide
+                if (work) x[base + (int64_t)j * stride] = (T)xj;
+                else y[(int64_t)j * stride] = xj;
+#pragma unroll
+                for (int r = 1; r <= W; ++r)
+                    if (r <= kv && j - r >= 0) g[r] = fma(-__ldg(ab + (int64_t)(kv - r) * n + j), xj, g[r]);
+                const double nv = cur[k];
+#pragma unroll
+                for (int r = 0; r < W; ++r) g[r] = (r == kv) ? nv : g[r + 1];
+                if (kv == W) g[W] = nv;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PF; ++k) cur[k] = nxt[k];
     }
 }
 
