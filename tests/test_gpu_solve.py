@@ -135,3 +135,21 @@ def test_singular_operators_raise(cuda):
         deo.ldiv(L * deo.Neumann0BC(1.0, 1), _dev(np.ones(n)))   # constants in the null space
     with pytest.raises(deo.DeoShapeError):
         deo.ldiv(L * deo.Dirichlet0BC(), _dev(np.ones(n + 1)))
+
+
+def test_full_size_residual_and_oracle(cuda):
+    """256^3 along axis 2 (the benchmark's size): against the oracle's dense
+    solve of every line, and A (A \\ u) = u through the apply."""
+    n = 256
+    h = 1.0 / (n + 1)
+    shape = (n, n, n)
+    l, r = (1.0, 0.5, 0.0), (1.0, 0.5, 0.0)
+    L = deo.CenteredDifference(2, 2, h, n, axis=2)
+    A = L * deo.MultiDimBC(deo.RobinBC(l, r, h, 2), shape, 2)
+    u = np.asfortranarray(np.random.default_rng(23).standard_normal(shape))
+    x = deo.ldiv(A, _dev(u))
+    ref, cond = O.ghost_solve(O.centered(2, 2, h, n), O.robin(l, r, h, 2), u, axis=2)
+    xh = _host(x)
+    assert np.linalg.norm(xh - ref) / np.linalg.norm(ref) < 16 * cond * EPS
+    back = _host(A * x)
+    assert np.linalg.norm(back - u) / np.linalg.norm(u) < 1e-9

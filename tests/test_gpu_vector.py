@@ -194,3 +194,19 @@ def test_errors(cuda):
     xv = torch.as_strided(buf, (8, 8, 2), (1, 8, 64), 50)
     with pytest.raises(deo.DeoArgError):
         G.mul_(xv, Mv)  # x_temp overlaps M
+
+
+@pytest.mark.parametrize("kind", ["gradient", "divergence", "curl"])
+def test_full_size_against_oracle(cuda, kind):
+    """The benchmark's size (256^3, 4th order, Float64) against the oracle, every
+    entry within 4 ulp of its absolute-value scale, and linearity in M."""
+    import torch
+    n = 256
+    A, ops = _pair(kind, 4, [1.0 / (n + 1)] * 3, (n, n, n))
+    rng = np.random.default_rng(17)
+    M = np.asfortranarray(rng.standard_normal(_in_shape(kind, (n, n, n))))
+    Md = _dev(M)
+    got = A * Md
+    _check(kind, A, ops, M, _host(got))
+    # linearity: A(2 M) = 2 A(M) exactly (scaling by 2 is exact in every tap)
+    assert torch.equal(A * (2.0 * Md), 2.0 * got)
