@@ -1481,6 +1481,12 @@ extern "C" deo_status deo_vector_calculus_sizes(const deo_vc* vc, int64_t* in_el
     return DEO_OK;
 }
 
+extern "C" deo_status deo_vector_calculus_info(const deo_vc* vc, int* band_nk) {
+    if (!vc || !band_nk) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *band_nk = vc->dev.band_nk;
+    return DEO_OK;
+}
+
 extern "C" deo_status deo_vector_calculus_apply(const deo_vc* vc, const void* M, void* out, int overwrite,
                                                 void* stream) {
     if (!vc || !M || !out) return fail(DEO_ERR_BAD_ARG, "null argument");

@@ -128,6 +128,7 @@ def lib():
     proto("deo_vector_calculus_plan", st, C.c_int, C.c_int, C.POINTER(_vp), C.c_int, C.POINTER(_vp))
     proto("deo_vector_calculus_sizes", st, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64))
     proto("deo_vector_calculus_apply", st, _vp, _vp, _vp, C.c_int, _vp)
+    proto("deo_vector_calculus_info", st, _vp, C.POINTER(C.c_int))
     proto("deo_vector_calculus_destroy", None, _vp)
     proto("deo_dot_product", st, C.c_int, C.c_int64, C.c_int, _vp, _vp, _vp, _vp)
     proto("deo_cross_product", st, C.c_int, C.c_int64, _vp, _vp, _vp, _vp)
@@ -170,7 +171,7 @@ EXPORTED = [
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_nonlinear_diffusion_plan", "deo_nonlinear_diffusion",
     "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
-    "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply",
+    "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply", "deo_vector_calculus_info",
     "deo_vector_calculus_destroy", "deo_dot_product", "deo_cross_product", "deo_square_norm",
     "deo_solve_plan", "deo_solve_bands", "deo_solve_apply", "deo_solve_destroy",
 ]

@@ -54,6 +54,13 @@ class _VectorCalculusOperator:
             h = self._plans[dtype_code] = out
         return h
 
+    def info(self, dtype_code: int = 0) -> dict:
+        """Execution choice of the plan for a dtype: the interior band width
+        of the unrolled marching kernel (0 = row tables everywhere)."""
+        nk = C.c_int()
+        check(L.lib().deo_vector_calculus_info(self._plan(dtype_code), C.byref(nk)))
+        return {"band_nk": nk.value}
+
     def __del__(self):
         try:
             for h in self._plans.values():

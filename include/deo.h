@@ -313,6 +313,10 @@ deo_status deo_vector_calculus_plan(int kind, int ndims, const deo_operator* con
                                     deo_vc** out);
 /* Elements of M and of out (all components). */
 deo_status deo_vector_calculus_sizes(const deo_vc* plan, int64_t* in_elems, int64_t* out_elems);
+/* Execution choice (no reference counterpart): *band_nk > 0 when every
+ * operator's interior rows are one centred band of that many taps (the
+ * unrolled marching kernel), 0 when every row goes through the row tables. */
+deo_status deo_vector_calculus_info(const deo_vc* plan, int* band_nk);
 deo_status deo_vector_calculus_apply(const deo_vc* plan, const void* M, void* out, int overwrite, void* stream);
 void deo_vector_calculus_destroy(deo_vc* plan);
 

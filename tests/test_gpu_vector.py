@@ -210,3 +210,32 @@ def test_full_size_against_oracle(cuda, kind):
     _check(kind, A, ops, M, _host(got))
     # linearity: A(2 M) = 2 A(M) exactly (scaling by 2 is exact in every tap)
     assert torch.equal(A * (2.0 * Md), 2.0 * got)
+
+
+def test_nonfinite_and_plan_info(cuda):
+    """Inf/NaN inputs give the oracle's non-finite pattern (0 * Inf in the
+    centre tap included); the uniform 4th-order plan takes the 5-tap marching
+    kernel; accumulating applies keep the reference's order."""
+    n = 16
+    A, ops = _pair("gradient", 4, [0.1, 0.1, 0.1], (n, n, n))
+    assert A.info(0) == {"band_nk": 5} and A.info(1) == {"band_nk": 5}
+    graded = [0.1 * (1.0 + 0.3 * np.sin(np.arange(n + 1) + a)) for a in range(3)]
+    Anu, _ = _pair("gradient", 4, graded, (n, n, n))
+    assert Anu.info(0) == {"band_nk": 0}
+    rng = np.random.default_rng(3)
+    M = np.asfortranarray(rng.standard_normal((n + 2,) * 3))
+    M[8, 9, 10] = np.inf
+    M[3, 12, 5] = np.nan
+    got = _host(A * _dev(M))
+    with np.errstate(invalid="ignore"):
+        ref = O.vector_calculus(O.GRADIENT, ops, M)
+    assert np.array_equal(np.isnan(got), np.isnan(ref)) and np.array_equal(np.isinf(got), np.isinf(ref))
+    fin = np.isfinite(ref)
+    Mf = np.where(np.isfinite(M), M, 0.0)
+    scale = O.vector_calculus(O.GRADIENT, ops, np.asfortranarray(Mf), absolute=True)
+    assert (np.abs(got[fin] - ref[fin]) <= 4 * np.spacing(scale[fin])).all()
+    x0 = np.asfortranarray(rng.standard_normal(A.out_shape()))
+    M2 = np.asfortranarray(rng.standard_normal((n + 2,) * 3))
+    xt = _dev(x0)
+    A.mul_(xt, _dev(M2))
+    _check("gradient", A, ops, M2, _host(xt), init=x0)
