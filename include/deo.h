@@ -275,8 +275,10 @@ void deo_nonlinear_diffusion_destroy(deo_nld* plan);
  * line of u along `axis` (n = the operator's len), is factored once on the
  * host with partial pivoting (DEO_ERR_BAD_ARG if singular), and the device
  * solves all lines.  sizes: u's Julia size.  x may be u itself (in place) but
- * may not otherwise overlap it.  Float32 lines are solved in Float64 and
- * rounded once.
+ * may not otherwise overlap it.  Float32 lines are solved in Float64 in a
+ * plan-owned workspace and rounded once, so the Float32 applies of one plan
+ * must be ordered on one stream (Float64 solves work in x and may run
+ * concurrently). 
  * ---------------------------------------------------------------------- */
 typedef struct deo_solve deo_solve;
 deo_status deo_solve_plan(const deo_operator* op, const deo_bc* bc, int ndims, const int64_t* sizes, int axis,
