@@ -76,3 +76,40 @@ def test_fuzz_float32(cuda, case):
     got, ref, scale = run_case(case, "f32")
     rel = np.abs(got - ref) / np.maximum(scale, 1e-300)
     assert rel.max() < 64 * 2.0 ** -24, rel.max()
+
+
+def _small(case):
+    """The case on a shape small enough for a dense concretisation (<= 4096 points)."""
+    shape = list(case["shape"])
+    while np.prod(shape) > 4096:
+        k = int(np.argmax(shape))
+        need = max(2 * (t["d"] + t["a"]) + 2 for t in case["terms"])
+        if shape[k] - 1 < need:
+            return None
+        shape[k] -= 1
+    return dict(case, shape=tuple(shape))
+
+
+ADJ = [c for c in (_small(c) for c in CASES[1::5]) if c is not None]
+
+
+@pytest.mark.parametrize("case", ADJ, ids=[f"adj{c['seed']}" for c in ADJ])
+def test_fuzz_adjoint(cuda, case):
+    """The adjoint kernel against the transpose of the oracle's concretisation
+    (64 eps of |A_l|^T |v|), and the device concretisation against it."""
+    import deo
+    import oracle as O
+    from cases import build, to_device, to_host
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    Al, Ab = O.concretize_probe(oterms, shape)
+    v = np.asfortranarray(np.random.default_rng(case["seed"]).standard_normal(shape))
+    p = deo.plan_for(A.terms(), shape, 0)
+    ub = deo.julia_array(shape)
+    p.adjoint(to_device(v), ub)
+    got = to_host(ub).ravel(order="F")
+    ref = Al.T @ v.ravel(order="F")
+    scale = np.abs(Al).T @ np.abs(v.ravel(order="F"))
+    assert np.all(np.abs(got - ref) <= 64 * np.finfo(float).eps * scale + 1e-300)
+    Dl, Db = p.concretize()
+    assert np.allclose(Dl, Al, rtol=1e-12, atol=1e-12 * np.abs(Al).max())
