@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "deo_eval.cuh"
 
@@ -50,9 +51,10 @@ __device__ __forceinline__ T vc_deriv(const TermDev& t, const T* __restrict__ M,
 
 // The 2-D / 3-D methods (vector_calculus_convolutions.jl:174-838, curl :844-1067).
 // Blocks of 32 x 8 points of one (x, y) plane; blockIdx.z walks the planes.
-// (Used for operators without a uniform interior band, and where the marching
-// kernel's grid would not fit.)  NK > 0: a derivative along an axis on which
-// the point is an interior row takes the unrolled band loop.
+// Used for Float64, for operators without a uniform interior band, and where
+// the marching kernel's grid would not fit; launched with NK = 0 (every row
+// from the row tables).  NK > 0 would give a derivative along an axis on which
+// the point is an interior row the unrolled band loop.
 template <typename T, int KIND, int ND, int NK>
 __global__ void __launch_bounds__(256) k_vc(const VcDev V, const T* __restrict__ M, T* __restrict__ out,
                                             int overwrite) {
@@ -320,10 +322,17 @@ template <typename T, int KIND, int ND>
 void launch_tiled(const VcDev& V, const T* M, T* out, int ow, cudaStream_t st) {
     // marching kernel: columns x chunks of the last axis within the grid limits
     const int64_t nm = V.len[ND - 1];
-    int64_t zb = 16;
-    while ((nm + zb - 1) / zb > 65535) zb *= 2;
     const int64_t ncol1 = ND == 3 ? (V.len[1] + 7) / 8 : 1;
-    if (V.band_nk > 0 && ncol1 <= 65535) {
+    const int64_t ncols = (ND == 3 ? (V.len[0] + 31) / 32 : (V.len[0] + 255) / 256) * ncol1;
+    // chunks of the march: short enough for many waves of blocks (the last wave's
+    // idle SMs are the tail), long enough to amortise the queue's first fill
+    int64_t zb = 4;
+    while (zb < 32 && ncols * ((nm + 2 * zb - 1) / (2 * zb)) >= 8192) zb *= 2;
+    while ((nm + zb - 1) / zb > 65535) zb *= 2;
+    // Float64 is FP64-bound either way and the per-point row-table kernel keeps
+    // the FP64 pipe busier (gradient 548 us against 624 us at 256^3), so the
+    // marching kernel serves Float32 only
+    if (V.band_nk > 0 && ncol1 <= 65535 && !std::is_same<T, double>::value) {
         const unsigned chunks = (unsigned)((nm + zb - 1) / zb);
         const dim3 grid = ND == 3 ? dim3((unsigned)((V.len[0] + 31) / 32), (unsigned)ncol1, chunks)
                                   : dim3((unsigned)((V.len[0] + 255) / 256), chunks, 1);
