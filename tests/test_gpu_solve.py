@@ -153,3 +153,13 @@ def test_full_size_residual_and_oracle(cuda):
     assert np.linalg.norm(xh - ref) / np.linalg.norm(ref) < 16 * cond * EPS
     back = _host(A * x)
     assert np.linalg.norm(back - u) / np.linalg.norm(u) < 1e-9
+
+
+def test_poisson_example(cuda):
+    """test/DerivativeOperators/poisson.jl on the GPU: (Δ * DirichletBC(-1, 2)) \\ 1."""
+    n = 10
+    h = 1.0 / (n + 1)
+    x = h * np.arange(1, n + 1)
+    ua = 0.5 * x ** 2 + (2.0 + 1.0 - 0.5) * x - 1.0
+    u = _host(deo.ldiv(deo.CenteredDifference(2, 2, h, n) * deo.DirichletBC(-1.0, 2.0), _dev(np.ones(n))))
+    assert np.allclose(u, ua, rtol=1e-12, atol=1e-12)

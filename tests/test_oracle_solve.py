@@ -46,3 +46,14 @@ def test_fourth_order_consistency():
     Al = L.array() @ Q.array(len(x))[0]
     Ab = L.array() @ Q.array(len(x))[1]
     assert np.linalg.norm(Al @ sol + Ab - u) / np.linalg.norm(u) < cond * np.finfo(float).eps
+
+
+def test_poisson_example():
+    """test/DerivativeOperators/poisson.jl: (Δ * DirichletBC(-1, 2)) \\ fill(1.0, 10)
+    equals u(x) = x^2/2 + (b - a - 1/2) x + a on the knots."""
+    n = 10
+    h = 1.0 / (n + 1)
+    x = h * np.arange(1, n + 1)
+    ua = 0.5 * x ** 2 + (2.0 + 1.0 - 0.5) * x - 1.0
+    u, _ = O.ghost_solve(O.centered(2, 2, h, n), O.dirichlet(-1.0, 2.0), np.ones(n))
+    assert np.allclose(u, ua, rtol=1e-12, atol=1e-12)
