@@ -129,6 +129,19 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
     return acc;
 }
 
+// One row of a term's table over a padded line whose ghosts are stored around
+// it (bc_kind 2), so every tap is a plain load: line position p (1-based) is
+// x0[(p - 1) * s], x0 pointing at the left ghost.  Same products and order as
+// eval_term; no field coefficient.
+template <typename T>
+__device__ __forceinline__ T eval_row_padded(const RowTabDev& tb, const T* __restrict__ x0, int64_t s, int i) {
+    const RowInfo r = row_info(tb, i);
+    const T* __restrict__ xp = x0 + (int64_t)(r.p0 - 1) * s;
+    T acc = T(0);
+    for (int k = 0; k < r.nk; ++k) acc = fma(row_w<T>(tb, r, k), __ldg(xp + (int64_t)k * s), acc);
+    return acc;
+}
+
 // Column p of one term's L (padded space) dotted with dbar along the line.
 template <typename T>
 __device__ __forceinline__ T adj_column(const TermDev& t, const T* __restrict__ d, int64_t base, int p) {

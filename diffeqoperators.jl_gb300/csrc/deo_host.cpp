@@ -1380,7 +1380,7 @@ extern "C" deo_status deo_nonlinear_diffusion(const deo_nld* nl, const void* p, 
                                               void* stream) {
     if (!nl || !p || !q || !du) return fail(DEO_ERR_BAD_ARG, "null argument");
     if (du == p || du == q) return fail(DEO_ERR_BAD_ARG, "du must not alias p or q");
-    const int e = deo_k_nonlinear_diffusion(nl->plan->d_plan, nl->len, nl->n, nl->m, nl->plan->dev.dtype, p, q, du,
+    const int e = deo_k_nonlinear_diffusion(&nl->plan->dev, nl->len, nl->n, nl->m, nl->plan->dev.dtype, p, q, du,
                                             stream);
     if (e) return cuda_fail((cudaError_t)e, "deo_nonlinear_diffusion launch");
     return DEO_OK;

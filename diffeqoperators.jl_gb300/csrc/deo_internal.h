@@ -230,8 +230,8 @@ extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
 // nonlinear_diffusion! on padded vectors p, q (length len+2): term k-1 of the
-// plan is CenteredDifference of order k (padded-input ghosts).
-extern "C" int deo_k_nonlinear_diffusion(const deo::PlanDev* d_plan, int len, int n, int m, int dtype, const void* p,
+// plan (host copy, passed by value) is CenteredDifference of order k.
+extern "C" int deo_k_nonlinear_diffusion(const deo::PlanDev* plan, int len, int n, int m, int dtype, const void* p,
                                          const void* q, void* du, void* stream);
 // TMA-fed fast path (deo_tma.cu): the interior box of a Laplacian-type plan;
 // returns cudaErrorNotSupported when the array does not meet the tensor-map

@@ -362,11 +362,12 @@ extern "C" int deo_k_apply_uniform(const UniPlan* up, const PlanDev* dp, int dty
 //   du = du .+ (D_{m+n} q) .* p[2:len+1]
 // each broadcast in the reference's operation order, one thread per point.
 template <typename T>
-__global__ void __launch_bounds__(256) k_nld(const PlanDev* __restrict__ P, int len, int n, int m,
-                                             const T* __restrict__ p, const T* __restrict__ q, T* __restrict__ du) {
+__global__ void __launch_bounds__(256) k_nld(const PlanDev P, int len, int n, int m, const T* __restrict__ p,
+                                             const T* __restrict__ q, T* __restrict__ du) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= len) return;
-    auto D = [&](int k, const T* x) { return eval_term<T>(P->t[k - 1], x + 1, i, i + 1); };
+    // the vectors hold their own ghosts: row i + 1 of D_k over x[0 .. len + 1]
+    auto D = [&](int k, const T* x) { return eval_row_padded<T>(P.t[k - 1].tab[0], x, 1, i + 1); };
     T acc = (m > 0 ? D(m, q) : q[i + 1]) * D(n, p);
     long long b = 1;  // binomial(n, l)
     for (int l = 1; l <= n - 1; ++l) {
@@ -377,14 +378,14 @@ __global__ void __launch_bounds__(256) k_nld(const PlanDev* __restrict__ P, int 
     du[i] = acc;
 }
 
-extern "C" int deo_k_nonlinear_diffusion(const PlanDev* d_plan, int len, int n, int m, int dtype, const void* p,
+extern "C" int deo_k_nonlinear_diffusion(const PlanDev* plan, int len, int n, int m, int dtype, const void* p,
                                          const void* q, void* du, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const unsigned blocks = (unsigned)((len + 255) / 256);
     if (dtype == 0)
-        k_nld<double><<<blocks, 256, 0, st>>>(d_plan, len, n, m, (const double*)p, (const double*)q, (double*)du);
+        k_nld<double><<<blocks, 256, 0, st>>>(*plan, len, n, m, (const double*)p, (const double*)q, (double*)du);
     else
-        k_nld<float><<<blocks, 256, 0, st>>>(d_plan, len, n, m, (const float*)p, (const float*)q, (float*)du);
+        k_nld<float><<<blocks, 256, 0, st>>>(*plan, len, n, m, (const float*)p, (const float*)q, (float*)du);
     return (int)cudaGetLastError();
 }
 

@@ -41,12 +41,7 @@ __device__ __forceinline__ T vc_deriv(const TermDev& t, const T* __restrict__ M,
         for (int k = 0; k < NK; ++k) acc = fma(band_w<T>(t.tab[0], k), __ldg(xp + (int64_t)k * s), acc);
         return acc;
     }
-    const RowTabDev& tb = t.tab[0];
-    const int i = (int)oa + 1;
-    const RowInfo r = row_info(tb, i);
-    const T* __restrict__ xp = M + ia + (int64_t)(r.p0 - 1 - i) * s;  // padded position p0 of the line
-    for (int k = 0; k < r.nk; ++k) acc = fma(row_w<T>(tb, r, k), __ldg(xp + (int64_t)k * s), acc);
-    return acc;
+    return eval_row_padded<T>(t.tab[0], M + ia - (oa + 1) * s, s, (int)oa + 1);  // the line's left ghost
 }
 
 // The 2-D / 3-D methods (vector_calculus_convolutions.jl:174-838, curl :844-1067).
