@@ -104,27 +104,31 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
     const RowTabDev& tb = row_variant<T>(t, base, i, c);
     const RowInfo r = row_info(tb, i);
     const int L2 = t.len + 2;
+    // (the field and no-field loops are separate so that the common no-field
+    // rows issue no c * w multiply: a speculated one would double the FP64 work)
     if (r.band && r.p0 >= 2 && r.p0 + r.nk <= L2) {
         // band row away from the ghosts: straight tap loop (same order and rounding)
         const T* __restrict__ xp = line + (int64_t)(r.p0 - 2) * s;
         T acc = T(0);
-        for (int k = 0; k < r.nk; ++k) {
-            T w = band_w<T>(tb, k);
-            if (t.has_field) w = c * w;
-            acc = fma(w, __ldg(xp + (int64_t)k * s), acc);
+        if (t.has_field) {
+            for (int k = 0; k < r.nk; ++k) acc = fma(c * band_w<T>(tb, k), __ldg(xp + (int64_t)k * s), acc);
+        } else {
+            for (int k = 0; k < r.nk; ++k) acc = fma(band_w<T>(tb, k), __ldg(xp + (int64_t)k * s), acc);
         }
         return acc;
     }
     T gl = T(0), gr = T(0);
     if (r.p0 == 1) gl = ghost_left<T>(t, line);
     if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line);
-    T acc = T(0);
-    for (int k = 0; k < r.nk; ++k) {
+    auto tap = [&](int k) {
         const int p = r.p0 + k;
-        const T x = (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
-        T w = row_w<T>(tb, r, k);
-        if (t.has_field) w = c * w;
-        acc = fma(w, x, acc);
+        return (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
+    };
+    T acc = T(0);
+    if (t.has_field) {
+        for (int k = 0; k < r.nk; ++k) acc = fma(c * row_w<T>(tb, r, k), tap(k), acc);
+    } else {
+        for (int k = 0; k < r.nk; ++k) acc = fma(row_w<T>(tb, r, k), tap(k), acc);
     }
     return acc;
 }
@@ -159,15 +163,23 @@ __device__ __forceinline__ T adj_column(const TermDev& t, const T* __restrict__ 
             return acc;
         }
     }
+    if (!t.has_field) {  // (no c * w multiply issued, see eval_term)
+        const RowTabDev& tb = t.tab[0];
+        for (int i = lo; i <= hi; ++i) {
+            const RowInfo r = row_info(tb, i);
+            const int k = p - r.p0;
+            if (k < 0 || k >= r.nk) continue;
+            acc = fma(row_w<T>(tb, r, k), __ldg(d + base + (int64_t)(i - 1) * s), acc);
+        }
+        return acc;
+    }
     for (int i = lo; i <= hi; ++i) {
         T c;
         const RowTabDev& tb = row_variant<T>(t, base, i, c);
         const RowInfo r = row_info(tb, i);
         const int k = p - r.p0;
         if (k < 0 || k >= r.nk) continue;
-        T w = row_w<T>(tb, r, k);
-        if (t.has_field) w = c * w;
-        acc = fma(w, __ldg(d + base + (int64_t)(i - 1) * s), acc);
+        acc = fma(c * row_w<T>(tb, r, k), __ldg(d + base + (int64_t)(i - 1) * s), acc);
     }
     return acc;
 }
