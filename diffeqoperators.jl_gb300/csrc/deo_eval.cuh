@@ -216,13 +216,13 @@ __device__ __forceinline__ int term_row(const PlanDev& P, const TermDev& t, int6
 
 template <typename T, bool ADJ>
 __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ u, int64_t idx) {
-    T acc = T(0);
-    for (int tt = 0; tt < P.nterms; ++tt) {
+    auto term = [&](int tt) {
         const TermDev& t = P.t[tt];
         const int i = term_row(P, t, idx);
-        const T r = ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
-        acc = (tt == 0) ? r : acc + r;
-    }
+        return ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
+    };
+    T acc = term(0);  // the first term as is, then the others added left to right
+    for (int tt = 1; tt < P.nterms; ++tt) acc = acc + term(tt);
     return ADJ ? acc : zero_fix(acc);
 }
 
