@@ -1500,6 +1500,82 @@ extern "C" deo_status deo_vector_calculus_apply(const deo_vc* vc, const void* M,
 
 extern "C" void deo_vector_calculus_destroy(deo_vc* vc) { delete vc; }
 
+// L*M / mul!(x_temp, L, M) on an already padded array (derivative_operator_functions.jl:17-69).
+struct deo_padded {
+    deo_plan tabs;  // owns the uploaded row table
+    deo::VcDev dev{};
+    int axis = 0;
+    int64_t coff = 0, in_elems = 0;
+    int dtype = 0;
+};
+
+extern "C" deo_status deo_padded_plan(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                                      const int64_t* in_sizes, deo_dtype dtype, deo_padded** out) {
+    if (!op || !out_sizes || !in_sizes || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
+    if (axis < 1 || axis > ndims) return fail(DEO_ERR_BAD_SHAPE, "axis %d outside 1..%d", axis, ndims);
+    if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
+    const int a = axis - 1;
+    for (int b = 0; b < ndims; ++b) {
+        if (out_sizes[b] < 1) return fail(DEO_ERR_BAD_SHAPE, "size(x_temp, %d) = %lld", b + 1, (long long)out_sizes[b]);
+        const bool ok = b == a ? in_sizes[b] == out_sizes[b] + 2
+                               : (in_sizes[b] == out_sizes[b] || in_sizes[b] == out_sizes[b] + 2);
+        if (!ok)
+            return fail(DEO_ERR_BAD_SHAPE, "size(M, %d) = %lld does not fit size(x_temp, %d) = %lld%s", b + 1,
+                        (long long)in_sizes[b], b + 1, (long long)out_sizes[b],
+                        b == a ? " + 2 (the differentiated dimension must be padded)" : " (or + 2)");
+    }
+    if (out_sizes[a] != op->len)
+        return fail(DEO_ERR_BAD_SHAPE, "size(x_temp, %d) = %lld but the operator has len %d", axis,
+                    (long long)out_sizes[a], op->len);
+    if (!op->wind && op->len < 2 * op->bpc + 1)
+        return fail(DEO_ERR_BAD_SHAPE, "len %d < 2*boundary_point_count+1", op->len);
+    auto P = std::make_unique<deo_padded>();
+    deo::VcDev& D = P->dev;
+    D.nd = ndims;
+    int64_t pv = 1, ov = 1, coff = 0;
+    for (int b = 0; b < ndims; ++b) {
+        D.len[b] = out_sizes[b];
+        D.pstride[b] = pv;
+        if (b != a && in_sizes[b] == out_sizes[b] + 2) coff += pv;
+        pv *= in_sizes[b];
+        ov *= out_sizes[b];
+    }
+    D.pvol = pv;
+    D.ovol = ov;
+    TermDev& T = D.t[0];
+    T.axis = a;
+    T.len = op->len;
+    T.stride = D.pstride[a];
+    T.nvar = 1;
+    T.bc_kind = 2;
+    std::vector<int> rlo(op->len + 2, op->len + 1), rhi(op->len + 2, 0);
+    HostTab H;
+    deo_status s = compile_table(*op, 0, true, 1.0, H, rlo, rhi);
+    if (s != DEO_OK) return s;
+    if ((s = upload_tab(P->tabs, H, dtype, T.tab[0])) != DEO_OK) return s;
+    P->axis = a;
+    P->coff = coff;
+    P->in_elems = pv;
+    P->dtype = dtype;
+    *out = P.release();
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_padded_apply(const deo_padded* p, const void* M, void* x_temp, int overwrite,
+                                       void* stream) {
+    if (!p || !M || !x_temp) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const size_t es = p->dtype == DEO_F64 ? 8 : 4;
+    if (overlaps(M, (size_t)p->in_elems * es, x_temp, (size_t)p->dev.ovol * es))
+        return fail(DEO_ERR_BAD_ARG, "x_temp must not overlap M");
+    const int e = deo_k_padded_apply(&p->dev, p->axis, p->coff, p->dtype, M, x_temp, overwrite ? 1 : 0, stream);
+    if (e) return cuda_fail((cudaError_t)e, "deo_padded_apply launch");
+    return DEO_OK;
+}
+
+extern "C" void deo_padded_destroy(deo_padded* p) { delete p; }
+
 static deo_status vector_algebra(int op, deo_dtype dtype, int64_t npts, int ncomp, const void* A, const void* B,
                                  void* u, void* stream) {
     if (!A || !u || (op != 2 && !B)) return fail(DEO_ERR_BAD_ARG, "null argument");

@@ -207,6 +207,11 @@ struct VcDev {
 // not overlap M.  overwrite = 1 writes A*M, 0 adds it to out (mul!).
 extern "C" int deo_k_vector_calculus(const deo::VcDev* V, int dtype, const void* M, void* out, int overwrite,
                                      void* stream);
+// L*M on a padded array: V.t[0] is the operator's table (generic methods),
+// V.len the output size, V.pstride M's strides; coff the offset of the
+// stripped edge planes of M's other axes.
+extern "C" int deo_k_padded_apply(const deo::VcDev* V, int axis, int64_t coff, int dtype, const void* M, void* out,
+                                  int overwrite, void* stream);
 // op 0: u = dot(A, B) over ncomp components; 1: u = cross(A, B) (ncomp 3);
 // 2: u = sqrt(dot(A, A)).  npts points per component, component-major.
 extern "C" int deo_k_vector_algebra(int op, int dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,

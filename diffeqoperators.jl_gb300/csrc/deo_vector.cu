@@ -266,6 +266,28 @@ __global__ void __launch_bounds__(256) k_vc_lines(const VcDev V, const T* __rest
     }
 }
 
+// L*M / mul!(x_temp, L, M; overwrite) on an already padded array M
+// (derivative_operator_functions.jl:17-69, 150-163; convolutions.jl:17-22 for
+// vectors): one thread per output point; its line along `axis` starts at the
+// left ghost, other axes at the output index + off (1 where M is padded on that
+// axis, so its edge planes are skipped; `coff` = sum of those offsets times the
+// strides); the row from the operator's table (generic methods).
+template <typename T>
+__global__ void __launch_bounds__(256) k_padded(const VcDev V, int axis, int64_t coff, const T* __restrict__ M,
+                                                T* __restrict__ out, int overwrite) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= V.ovol) return;
+    int64_t r = n, ls = coff, oa = 0;
+    for (int b = 0; b < V.nd; ++b) {
+        const int64_t o = (b == V.nd - 1) ? r : r % V.len[b];
+        r = (b == V.nd - 1) ? 0 : r / V.len[b];
+        if (b == axis) oa = o;
+        else ls += o * V.pstride[b];
+    }
+    const T d = eval_row_padded<T>(V.t[0].tab[0], M + ls, V.pstride[axis], (int)oa + 1);
+    out[n] = overwrite ? zero_fix(d) : d + out[n];
+}
+
 // Products rounded before the sums (no contraction), as plain Julia code does.
 template <typename T>
 __device__ __forceinline__ T mul_rn(T a, T b);
@@ -374,6 +396,18 @@ extern "C" int deo_k_vector_calculus(const deo::VcDev* V, int dtype, const void*
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     return dtype == 0 ? deo::launch_vc<double>(*V, M, out, overwrite, st)
                       : deo::launch_vc<float>(*V, M, out, overwrite, st);
+}
+
+extern "C" int deo_k_padded_apply(const deo::VcDev* V, int axis, int64_t coff, int dtype, const void* M, void* out,
+                                  int overwrite, void* stream) {
+    if (V->ovol <= 0) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const unsigned blocks = (unsigned)((V->ovol + 255) / 256);
+    if (dtype == 0)
+        deo::k_padded<double><<<blocks, 256, 0, st>>>(*V, axis, coff, (const double*)M, (double*)out, overwrite);
+    else
+        deo::k_padded<float><<<blocks, 256, 0, st>>>(*V, axis, coff, (const float*)M, (float*)out, overwrite);
+    return (int)cudaGetLastError();
 }
 
 extern "C" int deo_k_vector_algebra(int op, int dtype, int64_t npts, int ncomp, const void* A, const void* B, void* u,

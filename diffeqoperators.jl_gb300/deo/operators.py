@@ -199,7 +199,7 @@ class DerivativeOperator:
             return GhostDerivativeOperator(self, other)
         if isinstance(other, DerivativeOperator) or isinstance(other, numbers.Number):
             return NotImplemented
-        return _mul_padded_vector(self, other)
+        return _mul_padded(self, other)
 
     def __add__(self, other):
         return DiffEqOperatorCombination([self]) + other
@@ -805,29 +805,65 @@ def _apply_terms(ghosts, u, du=None, overwrite=True):
 
 def mul_(du, A, u, overwrite: bool = True):
     """mul!(du, A, u) for A = L*Q or a combination of L*Q terms
-    (ghost_derivative_operator.jl:15-24, composite_operators.jl:76-83)."""
+    (ghost_derivative_operator.jl:15-24, composite_operators.jl:76-83), or for
+    a DerivativeOperator on an already padded array
+    (derivative_operator_functions.jl:17-25)."""
+    if isinstance(A, DerivativeOperator):
+        return _mul_padded(A, u, du, overwrite)
     return _apply_terms(A.terms(), u, du, overwrite)
 
 
-def _mul_padded_vector(op: DerivativeOperator, x):
-    """L*x for an already padded Vector x of length len+2 (generic methods,
-    convolutions.jl:17-22): the ghosts are x[0] and x[end]."""
-    torch = _torch()
-    if isinstance(x, np.ndarray) or x.dim() != 1:
-        raise DeoArgError(2, "L*x takes a 1-D device vector of length len+2")
-    if x.shape[0] != op.len + 2:
-        raise DeoShapeError(1, f"length(x) = {x.shape[0]} but the operator needs len+2 = {op.len + 2}")
-    xs = x.detach().to("cpu", torch.float64)
-    s = BCStruct()
-    s.kind = L.DEO_BC_AFFINE
-    s.m_l = s.m_r = 0
-    s.b_l, s.b_r = float(xs[0]), float(xs[-1])
-    q = AtomicBC(s, "padding")
-    g = GhostDerivativeOperator(op, q)
-    p = Plan([g], (op.len,), _dtype_code(x), L.DEO_PATH_GENERIC)
-    u = x[1:-1].contiguous()
-    du = torch.empty_like(u)
-    return p.apply(u, du)
+class PaddedPlan:
+    """A compiled deo_padded: L on an already padded array for (sizes, dtype)."""
+
+    def __init__(self, op: DerivativeOperator, out_shape, in_shape, dtype_code: int):
+        nd = len(in_shape)
+        osz = (C.c_int64 * nd)(*out_shape)
+        isz = (C.c_int64 * nd)(*in_shape)
+        h = C.c_void_p()
+        check(L.lib().deo_padded_plan(op._h, int(op.axis), nd, osz, isz, int(dtype_code), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        try:
+            if self._h:
+                L.lib().deo_padded_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+
+_padded_cache: dict = {}
+
+
+def _mul_padded(op: DerivativeOperator, M, out=None, overwrite: bool = True):
+    """L*M and mul!(x_temp, L, M; overwrite) for an already padded array M
+    (derivative_operator_functions.jl:17-69, 150-163; convolutions.jl:17-22 for
+    vectors): M is padded along the operator's axis; along other axes it has
+    x_temp's size or 2 more (then its edge planes are skipped)."""
+    if isinstance(M, np.ndarray) or not getattr(M, "is_cuda", False):
+        raise DeoArgError(2, "L*M takes a CUDA tensor (Julia layout)")
+    _check_layout(M, "M")
+    nd = M.dim()
+    if op.axis > nd:
+        raise DeoShapeError(1, f"the operator acts on axis {op.axis} but M has {nd} dimensions")
+    if out is None:
+        oshape = tuple(n - 2 if b == op.axis - 1 else n for b, n in enumerate(M.shape))
+        if min(oshape) < 1:
+            raise DeoShapeError(1, f"M of size {tuple(M.shape)} is too small")
+        out = julia_array(oshape, M.dtype, M.device)
+        overwrite = True
+    else:
+        _check_layout(out, "x_temp")
+        if out.dim() != nd or out.dtype != M.dtype:
+            raise DeoShapeError(1, "x_temp must have M's number of dimensions and dtype")
+    key = (id(op), tuple(out.shape), tuple(M.shape), _dtype_code(M))
+    hit = _padded_cache.get(key)
+    if hit is None or hit[0] is not op:
+        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M)))
+    check(L.lib().deo_padded_apply(hit[1]._h, C.c_void_p(M.data_ptr()), C.c_void_p(out.data_ptr()),
+                                   1 if overwrite else 0, _stream_ptr()))
+    return out
 
 
 def concretize(A, shape, dtype=np.float64):

@@ -268,6 +268,22 @@ deo_status deo_nonlinear_diffusion(const deo_nld* plan, const void* p, const voi
 void deo_nonlinear_diffusion_destroy(deo_nld* plan);
 
 /* ------------------------------------------------------------------------
+ * A DerivativeOperator on an already padded array (no boundary condition):
+ * x_temp = L*M or mul!(x_temp, L, M; overwrite) with L acting along `axis`
+ * (derivative_operator_functions.jl:17-69, 150-163; convolutions.jl:17-22 for
+ * vectors), every line by the generic AbstractVector methods.  M's size along
+ * `axis` is len+2 (the ghosts are its first and last entries); along every
+ * other axis it equals x_temp's or is 2 longer, in which case its first and
+ * last planes are skipped (:47-56).  overwrite = 0 adds into x_temp.  The plan
+ * holds the row table for (operator, sizes, dtype); x_temp must not overlap M.
+ * ---------------------------------------------------------------------- */
+typedef struct deo_padded deo_padded;
+deo_status deo_padded_plan(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                           const int64_t* in_sizes, deo_dtype dtype, deo_padded** out);
+deo_status deo_padded_apply(const deo_padded* plan, const void* M, void* x_temp, int overwrite, void* stream);
+void deo_padded_destroy(deo_padded* plan);
+
+/* ------------------------------------------------------------------------
  * Implicit solves: x = A \ u for A = L*Q (ghost_derivative_operator.jl:39-58).
  * The reference concretises (A_l, A_b) = sparse(A) (concretization.jl:938-958:
  * sparse(L) * sparse(Q), Array(PeriodicBC) wrapping around) and solves

@@ -1024,6 +1024,47 @@ int orc_ssprk3(int nterms, void* const* ops, const int* axes, const void* bcs, c
 }
 
 // ---------------------------------------------------------------------------
+// mul!(x_temp, L, M; overwrite) and L*M for L = DerivativeOperator{T,N} on an
+// already padded array M (derivative_operator_functions.jl:17-69, 150-163):
+// size(M, N) = size(x_temp, N) + 2, every other axis of M equal to x_temp's or
+// 2 longer (then its first and last planes are stripped, :47-56); each line
+// along N by the generic AbstractVector methods (convolutions.jl:17-22, 27-118).
+// ---------------------------------------------------------------------------
+int orc_mul_nd(const void* op_, int axis, int nd, const long* out_sizes, const long* in_sizes, const double* M,
+               double* out, int overwrite, int absolute) {
+    const Op& A = *static_cast<const Op*>(op_);
+    const int a = axis - 1;
+    if (a < 0 || a >= nd || nd > 8) return -1;
+    long ps[8], os[8], ovol = 1, pvol = 1;
+    for (int b = 0; b < nd; ++b) {
+        if (b == a ? in_sizes[b] != out_sizes[b] + 2 : (in_sizes[b] != out_sizes[b] && in_sizes[b] != out_sizes[b] + 2))
+            return -1;
+        ps[b] = pvol;
+        os[b] = ovol;
+        pvol *= in_sizes[b];
+        ovol *= out_sizes[b];
+    }
+    if (out_sizes[a] != A.len) return -1;
+    const long L = out_sizes[a], nlines = ovol / L;
+    g_abs = absolute != 0;  // sum |c_k u_k| with the real rows (tolerance scale)
+    for (long line = 0; line < nlines; ++line) {
+        long r = line, q = 0, ob = 0;
+        for (int b = 0; b < nd; ++b) {
+            if (b == a) continue;
+            const long c = r % out_sizes[b];
+            r /= out_sizes[b];
+            q += (c + (in_sizes[b] == out_sizes[b] + 2 ? 1 : 0)) * ps[b];
+            ob += c * os[b];
+        }
+        const double* x = M + q;
+        Line Ln{x + ps[a], ps[a], x[0], x[(L + 1) * ps[a]], L};
+        apply_line(A, Ln, out + ob, os[a], VecCoeff{A.coeff.data(), 1}, overwrite != 0, 0);
+    }
+    g_abs = false;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
 // Gradient / Divergence / Curl on padded arrays
 // (vector_calculus_operators.jl:47-73, vector_calculus_convolutions.jl).
 // kind 0 Gradient: M (s1+2, .., sN+2) -> out (s1, .., sN, N);

@@ -66,6 +66,8 @@ def lib():
         L.orc_ssprk3.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
                                  C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, C.c_double, C.c_int, C.c_int]
         L.orc_vector_calculus.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_void_p), _dp, _dp, C.c_int, C.c_int]
+        L.orc_mul_nd.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_long), C.POINTER(C.c_long), _dp, _dp,
+                                 C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -316,6 +318,26 @@ def nonlinear_diffusion(n: int, m: int, approx: int, p, q, dx, nknots: int, abso
         b = b * (n - ell + 1) // ell
         du = du + (float(b) * D(ell + m, q)) * D(n - ell, p)
     return du + D(m + n, q) * pp[1:nknots + 1]
+
+
+def mul_nd(op: Op, M, out_shape=None, out=None, overwrite: bool = True, absolute: bool = False) -> np.ndarray:
+    """L*M / mul!(x_temp, L, M; overwrite) on an already padded array M
+    (derivative_operator_functions.jl:17-69, 150-163), restated in
+    deo_oracle.cpp (orc_mul_nd); the operator acts on axis op.axis.  out_shape
+    defaults to M's shape with that axis 2 shorter (L*M).  absolute=True gives
+    sum_k |c_k u_k| per point with the same rows (the tolerance scale)."""
+    M = np.asfortranarray(M, dtype=np.float64)
+    a = op.axis - 1
+    if out_shape is None:
+        out_shape = tuple(n - 2 if b == a else n for b, n in enumerate(M.shape))
+    o = np.zeros(out_shape, order="F") if out is None else out
+    nd = M.ndim
+    osz = (C.c_long * nd)(*o.shape)
+    isz = (C.c_long * nd)(*M.shape)
+    if lib().orc_mul_nd(op.h, op.axis, nd, osz, isz, M.ctypes.data_as(_dp), o.ctypes.data_as(_dp),
+                        int(overwrite or absolute), int(absolute)) != 0:
+        raise AssertionError("size mismatch between the operator, x_temp and M")
+    return o
 
 
 GRADIENT, DIVERGENCE, CURL = 0, 1, 2
