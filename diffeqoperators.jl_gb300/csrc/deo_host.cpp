@@ -1181,12 +1181,8 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
             mark(p, 2, stream);
             return 0;
         }
-        p->last_kernel = p->uni.lap ? "k_lap" : "k_uni3";
-        p->last_kernel2 = "";
-        p->ev_launches = 1;
-        const int e = deo_k_apply_uniform(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, stream);
-        mark(p, 1, stream);
-        return e;
+        // without the TMA path the generic kernel is the fastest (it outran the register-queue and
+        // rolling-window tiles it replaced by 1.1-2.9x once it stopped issuing field multiplies)
     }
     p->last_kernel = "k_apply";
     p->last_kernel2 = "";

@@ -83,12 +83,12 @@ struct PlanDev {
     TermDev t[DEO_KMAX_TERMS];
 };
 
-// Fast path of a plan whose terms all have constant interior rows (uniform
-// grid, constant coefficient along the axis) on a 2-D/3-D array: the CTA
-// stages a rolling window of (2H+1) planes of (TY+2H) x (TX+2H) points in
-// shared memory and evaluates interior points from it with the band weights;
-// points whose row along some term's axis lies outside [flo, fhi] (they read
-// ghosts or use boundary rows) take the generic evaluator.
+// The band rows of a plan whose terms all have constant interior rows (uniform
+// grid, constant coefficient along the axis) on a 2-D/3-D array.  Laplacian-
+// type plans (lap) take the TMA path: interior points, whose rows along every
+// term's axis lie in [flo, fhi] (no ghosts, no boundary rows), from staged
+// planes with the band weights; the rest of the points (the shell) from the
+// boundary rows.  Other plans run the generic evaluator.
 struct UniTerm {
     int axis;        // 0, 1, 2
     int nk;          // taps
@@ -101,7 +101,7 @@ struct UniPlan {
     int enabled;
     int radius;      // H = max |offset| over terms
     int nterms;
-    int lap;         // 1: term t acts on axis t with a centred band of 2H+1 taps (k_lap)
+    int lap;         // 1: term t acts on axis t with a centred band of 2H+1 taps (the TMA path)
     int64_t n[3];    // sizes along axes 1..3 (1 for absent axes)
     UniTerm t[DEO_KMAX_TERMS];
     // Exact-neighbour-sum evaluation (Float64, all terms share one band):
@@ -228,8 +228,6 @@ extern "C" int deo_k_band_solve(int n, int kl, int ku, const double* ab, const i
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
                            void* stream);
-extern "C" int deo_k_apply_uniform(const deo::UniPlan* up, const deo::PlanDev* d_plan, int dtype, const void* u,
-                                   void* du, int overwrite, void* stream);
 extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items, int64_t n_items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);

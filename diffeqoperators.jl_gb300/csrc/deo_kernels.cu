@@ -108,251 +108,9 @@ __global__ void __launch_bounds__(256) k_stage(const StageDev* __restrict__ st, 
     }
 }
 
-// Uniform fused apply (see UniPlan).  Block = TX x TY threads; each CTA
-// marches ZC planes along axis 3 keeping a rolling window of 2H+1 planes.
-template <typename T, int H, int TX, int TY, int ZC>
-__global__ void __launch_bounds__(TX * TY) k_uni3(const __grid_constant__ UniPlan U, const PlanDev* __restrict__ P,
-                                                  const T* __restrict__ u, T* __restrict__ du, int overwrite) {
-    constexpr int W = 2 * H + 1;
-    constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
-    __shared__ T sm[W][SY][SX];
-    const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int x = x0 + tx, y = y0 + ty;
-    const int z0 = blockIdx.z * ZC;
-    const int z1 = min(z0 + ZC, nz);
-    const int64_t sxy = (int64_t)nx * ny;
-
-    auto load_plane = [&](int z) {
-        T(*pl)[SX] = sm[((z % W) + W) % W];
-        const bool zin = (z >= 0 && z < nz);
-        for (int q = tid; q < SX * SY; q += TX * TY) {
-            const int yy = q / SX, xx = q - yy * SX;
-            const int gx = x0 + xx - H, gy = y0 + yy - H;
-            T v = T(0);
-            if (zin && gx >= 0 && gx < nx && gy >= 0 && gy < ny) v = __ldg(u + (int64_t)z * sxy + (int64_t)gy * nx + gx);
-            pl[yy][xx] = v;
-        }
-    };
-    for (int z = z0 - H; z < z0 + H; ++z) load_plane(z);
-    for (int z = z0; z < z1; ++z) {
-        load_plane(z + H);
-        __syncthreads();
-        if (x < nx && y < ny) {
-            const int64_t idx = (int64_t)z * sxy + (int64_t)y * nx + x;
-            bool fast = true;
-            for (int t = 0; t < U.nterms; ++t) {
-                const int ax = U.t[t].axis;
-                const int r = (ax == 0 ? x : (ax == 1 ? y : z)) + 1;
-                fast = fast && r >= U.t[t].flo && r <= U.t[t].fhi;
-            }
-            T total;
-            if (fast) {
-                total = T(0);
-                for (int t = 0; t < U.nterms; ++t) {
-                    const UniTerm& tm = U.t[t];
-                    T acc = T(0);
-                    for (int k = 0; k < tm.nk; ++k) {
-                        const int o = tm.off0 + k;
-                        T v;
-                        if (tm.axis == 0) v = sm[z % W][ty + H][tx + H + o];
-                        else if (tm.axis == 1) v = sm[z % W][ty + H + o][tx + H];
-                        else v = sm[(z + o + W) % W][ty + H][tx + H];
-                        acc = fma(uni_w<T>(tm, k), v, acc);
-                    }
-                    total = (t == 0) ? acc : total + acc;
-                }
-                total = zero_fix(total);
-            } else {
-                total = eval_point<T, false>(*P, u, idx);
-            }
-            du[idx] = overwrite ? total : total + du[idx];
-        }
-        __syncthreads();
-    }
-}
-
-
-// Centred-band fast path (UniPlan::lap): NT terms, term t on axis t, each a
-// band of 2H+1 taps centred on the point.  Block = TX x TY threads; every
-// thread owns one (x, y) and walks z, keeping u(x, y, z-H .. z+H) in a
-// register queue; the x/y neighbours come from a double-buffered plane tile
-// in shared memory whose next plane is prefetched into registers while the
-// current one is consumed (one barrier per plane).  Taps are unrolled, so the
-// weights are constant-bank operands.  Arithmetic per term is the same fma
-// chain as the generic evaluator, so both paths give identical bits.
-template <typename T, int H, int NT, int TX, int TY>
-__global__ void __launch_bounds__(TX * TY) k_lap(const __grid_constant__ UniPlan U, const PlanDev* __restrict__ P,
-                                                 const T* __restrict__ u, T* __restrict__ du, int overwrite, int zc) {
-    constexpr int SX = TX + 2 * H, SY = TY + 2 * H;
-    constexpr int NHALO = SX * SY - TX * TY;
-    constexpr int HPT = (NHALO + TX * TY - 1) / (TX * TY);  // halo elements per thread
-    __shared__ T sm[2][SY][SX];
-    const int nx = (int)U.n[0], ny = (int)U.n[1], nz = (int)U.n[2];
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int x = x0 + tx, y = y0 + ty;
-    const int z0 = blockIdx.z * zc;
-    const int z1 = min(z0 + zc, nz);
-    const int64_t sxy = (int64_t)nx * ny;
-    const bool inxy = x < nx && y < ny;
-    const int64_t col = (int64_t)y * nx + x;
-
-    // halo slots of this thread: (hy, hx) in the tile, or -1
-    int hyy[HPT], hxx[HPT];
-#pragma unroll
-    for (int j = 0; j < HPT; ++j) {
-        int q = tid + j * TX * TY;
-        hyy[j] = -1;
-        hxx[j] = -1;
-        if (q < NHALO) {
-            // enumerate the ring: top H rows, bottom H rows, then left/right H columns of the TY middle rows
-            if (q < H * SX) { hyy[j] = q / SX; hxx[j] = q % SX; }
-            else if (q < 2 * H * SX) { q -= H * SX; hyy[j] = H + TY + q / SX; hxx[j] = q % SX; }
-            else {
-                q -= 2 * H * SX;
-                const int r = q / (2 * H), c = q % (2 * H);
-                hyy[j] = H + r;
-                hxx[j] = c < H ? c : TX + c;
-            }
-        }
-    }
-    auto ld = [&](int gx, int gy, int z) -> T {
-        if (z < 0 || z >= nz || gx < 0 || gx >= nx || gy < 0 || gy >= ny) return T(0);
-        return __ldg(u + (int64_t)z * sxy + (int64_t)gy * nx + gx);
-    };
-
-    T q[2 * H + 1];
-#pragma unroll
-    for (int k = 0; k < 2 * H + 1; ++k) q[k] = (NT == 3 && inxy) ? ld(x, y, z0 - H + k) : T(0);
-    if (NT < 3) q[H] = inxy ? ld(x, y, z0) : T(0);
-    // tile for the first plane
-    sm[0][ty + H][tx + H] = q[H];
-#pragma unroll
-    for (int j = 0; j < HPT; ++j)
-        if (hyy[j] >= 0) sm[0][hyy[j]][hxx[j]] = ld(x0 + hxx[j] - H, y0 + hyy[j] - H, z0);
-    __syncthreads();
-    int cur = 0;
-    for (int z = z0; z < z1; ++z) {
-        // prefetch plane z+1 (halo) and u(x, y, z+1+H) (queue) into registers
-        T hv[HPT];
-        T qn = T(0);
-        const bool more = z + 1 < z1;
-        if (more) {
-#pragma unroll
-            for (int j = 0; j < HPT; ++j)
-                hv[j] = hyy[j] >= 0 ? ld(x0 + hxx[j] - H, y0 + hyy[j] - H, z + 1) : T(0);
-            if (NT == 3 && inxy) qn = ld(x, y, z + 1 + H);
-        }
-        if (inxy) {
-            const int64_t idx = (int64_t)z * sxy + col;
-            T total = T(0);
-#pragma unroll
-            for (int t = 0; t < NT; ++t) {
-                const int row = (t == 0 ? x : (t == 1 ? y : z)) + 1;
-                T acc;
-                if (row >= U.t[t].flo && row <= U.t[t].fhi) {
-                    acc = T(0);
-#pragma unroll
-                    for (int k = 0; k < 2 * H + 1; ++k) {
-                        const int o = k - H;
-                        const T v = t == 0 ? sm[cur][ty + H][tx + H + o] : (t == 1 ? sm[cur][ty + H + o][tx + H] : q[k]);
-                        const T w = uni_w<T>(U.t[t], k);  // t, k unrolled: constant-bank operand
-                        acc = fma(w, v, acc);
-                    }
-                } else {
-                    acc = eval_term<T>(P->t[t], u, idx, row);
-                }
-                total = (t == 0) ? acc : total + acc;
-            }
-            total = zero_fix(total);
-            du[idx] = overwrite ? total : total + du[idx];
-        }
-        if (more) {
-            const int nxt = cur ^ 1;
-            sm[nxt][ty + H][tx + H] = q[H + 1];
-#pragma unroll
-            for (int j = 0; j < HPT; ++j)
-                if (hyy[j] >= 0) sm[nxt][hyy[j]][hxx[j]] = hv[j];
-            if (NT < 3) sm[nxt][ty + H][tx + H] = inxy ? ld(x, y, z + 1) : T(0);
-#pragma unroll
-            for (int k = 0; k < 2 * H; ++k) q[k] = q[k + 1];
-            q[2 * H] = qn;
-            cur = nxt;
-        }
-        __syncthreads();
-    }
-}
-
 }  // namespace deo
 
 using namespace deo;
-
-template <typename T, int H, int NT>
-static int launch_lap(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int overwrite, cudaStream_t st) {
-    constexpr int TX = 32, TY = 8;
-    const int64_t nz = up->n[2];
-    const int zc = NT == 3 ? (int)std::min<int64_t>(nz, 64) : 1;
-    dim3 grid((unsigned)((up->n[0] + TX - 1) / TX), (unsigned)((up->n[1] + TY - 1) / TY),
-              (unsigned)((nz + zc - 1) / zc));
-    k_lap<T, H, NT, TX, TY><<<grid, dim3(TX, TY), 0, st>>>(*up, dp, (const T*)u, (T*)du, overwrite, zc);
-    return (int)cudaGetLastError();
-}
-
-template <typename T, int H>
-static int launch_uni(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int overwrite, cudaStream_t st) {
-    constexpr int TX = 32, TY = 8, ZC = 32;
-    dim3 grid((unsigned)((up->n[0] + TX - 1) / TX), (unsigned)((up->n[1] + TY - 1) / TY),
-              (unsigned)((up->n[2] + ZC - 1) / ZC));
-    k_uni3<T, H, TX, TY, ZC><<<grid, dim3(TX, TY), 0, st>>>(*up, dp, (const T*)u, (T*)du, overwrite);
-    return (int)cudaGetLastError();
-}
-
-template <typename T>
-static int launch_lap_any(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st) {
-    const int H = up->radius;
-    if (up->nterms == 3) {
-        switch (H) {
-            case 1: return launch_lap<T, 1, 3>(up, dp, u, du, ow, st);
-            case 2: return launch_lap<T, 2, 3>(up, dp, u, du, ow, st);
-            case 3: return launch_lap<T, 3, 3>(up, dp, u, du, ow, st);
-            case 4: return launch_lap<T, 4, 3>(up, dp, u, du, ow, st);
-        }
-    } else {
-        switch (H) {
-            case 1: return launch_lap<T, 1, 2>(up, dp, u, du, ow, st);
-            case 2: return launch_lap<T, 2, 2>(up, dp, u, du, ow, st);
-            case 3: return launch_lap<T, 3, 2>(up, dp, u, du, ow, st);
-            case 4: return launch_lap<T, 4, 2>(up, dp, u, du, ow, st);
-        }
-    }
-    return (int)cudaErrorInvalidValue;
-}
-
-extern "C" int deo_k_apply_uniform(const UniPlan* up, const PlanDev* dp, int dtype, const void* u, void* du,
-                                   int overwrite, void* stream) {
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (up->lap) return dtype == 0 ? launch_lap_any<double>(up, dp, u, du, overwrite, st)
-                                   : launch_lap_any<float>(up, dp, u, du, overwrite, st);
-    const int H = up->radius;
-    if (dtype == 0) {
-        switch (H) {
-            case 1: return launch_uni<double, 1>(up, dp, u, du, overwrite, st);
-            case 2: return launch_uni<double, 2>(up, dp, u, du, overwrite, st);
-            case 3: return launch_uni<double, 3>(up, dp, u, du, overwrite, st);
-            case 4: return launch_uni<double, 4>(up, dp, u, du, overwrite, st);
-        }
-    } else {
-        switch (H) {
-            case 1: return launch_uni<float, 1>(up, dp, u, du, overwrite, st);
-            case 2: return launch_uni<float, 2>(up, dp, u, du, overwrite, st);
-            case 3: return launch_uni<float, 3>(up, dp, u, du, overwrite, st);
-            case 4: return launch_uni<float, 4>(up, dp, u, du, overwrite, st);
-        }
-    }
-    return (int)cudaErrorInvalidValue;
-}
 
 // nonlinear_diffusion!{N}(du, n, m, approx, p, q, dx, len) on padded vectors
 // (derivative_operator.jl:34-66): with D_k the order-k centred operator (plan

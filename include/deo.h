@@ -174,11 +174,11 @@ void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
 /* Plan options (defaults 1 unless stated):
- *   DEO_OPT_FAST_PATH: 2-D/3-D plans whose terms all have constant interior
- *     rows use tiled kernels for interior points; 0 forces the generic
- *     row-table kernel.
- *   DEO_OPT_TMA: Laplacian-type plans (term t a centred band on axis t) stream
- *     planes with TMA into a shared-memory ring; 0 uses the register-queue kernel.
+ *   DEO_OPT_FAST_PATH: Laplacian-type 2-D/3-D plans (term t a centred band on
+ *     axis t) use the tiled TMA kernels below for interior points; 0 forces
+ *     the generic row-table kernel (which every other plan runs).
+ *   DEO_OPT_TMA: those plans stream planes with TMA into a shared-memory ring;
+ *     0 uses the generic kernel as well.
  *   DEO_OPT_EXACT_SUMS: Float64 Laplacian-type plans whose terms share one
  *     band evaluate interior points in integer arithmetic and round once
  *     (result within a few ulp of sum|c_k u_k| of the reference's order):
