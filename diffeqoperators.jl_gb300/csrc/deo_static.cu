@@ -2,12 +2,10 @@
 // memory.
 //
 // deo_batch_create allocates device memory for its instance table, work-list
-// and work counter.  Some callers cannot do that: a caller issuing work while
-// its stream is being captured into a CUDA graph (cudaMalloc is not allowed
-// during capture), a plug-in whose host application owns every device
-// allocation through its own pool and forbids others, or a request handler in a
-// memory-budgeted server that must not grow the device footprint after the
-// request was admitted.  deo_batch_apply_noalloc runs the same persistent
+// and work counter.  Some callers cannot do that: a plug-in whose host
+// application owns every device allocation through its own pool and forbids
+// others, or a request handler in a memory-budgeted server that must not grow
+// the device footprint after the request was admitted.  deo_batch_apply_noalloc runs the same persistent
 // batched kernel with that scratch in one file-scope device array of
 // DEO_NOALLOC_SCRATCH_BYTES bytes, which every GPU that loads libdeo holds
 // until the process exits.  The plans and each instance's input and output

@@ -396,10 +396,10 @@ typedef struct {
 deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int ctas_per_sm, deo_batch** out);
 
 /* Batched apply that allocates no device memory.  No counterpart in the
- * reference.  For callers that cannot call cudaMalloc -- a stream being
- * captured into a CUDA graph, a host application that owns every device
- * allocation, a server that must not grow its device footprint after
- * admitting a request -- this runs the same persistent kernel as
+ * reference.  For callers that cannot call cudaMalloc -- a plug-in whose host
+ * application owns every device allocation through its own pool, a server
+ * that must not grow its device footprint after admitting a request -- this
+ * runs the same persistent kernel as
  * deo_batch_run with its instance table, work-list and counter in one static
  * device array of DEO_NOALLOC_SCRATCH_BYTES (1 MiB) that every GPU loading
  * libdeo holds until process exit.  The plans (created earlier, where

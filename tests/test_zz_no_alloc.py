@@ -1,8 +1,8 @@
 """The allocation-free batched entry point (deo_batch_apply_noalloc).
 
-Callers that cannot allocate device memory -- work issued while a stream is
-being captured into a CUDA graph, plug-ins whose host owns every device
-allocation, servers that must not grow their footprint after admission --
+Callers that cannot allocate device memory -- plug-ins whose host application
+owns every device allocation, servers that must not grow their footprint after
+admission --
 use this entry point: it keeps the batched kernel's instance table, work-list
 and counter in a static device array instead of cudaMalloc'd buffers.  Its
 results must equal the allocating entry point's (same kernel), call after
