@@ -163,7 +163,11 @@ extern "C" deo_status deo_centered_difference(int d, int a, const double* dx, in
     if (!out || !dx) return fail(DEO_ERR_BAD_ARG, "null argument");
     if (a <= 1) return fail(DEO_ERR_BAD_ARG, "approximation_order must be greater than 1.");
     if (d < 0 || len < 1) return fail(DEO_ERR_BAD_ARG, "invalid derivative order or length");
-    if (ndx != 1 && ndx != len + 1) return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 or len+1 entries");
+    // The reference reads dx[1 : len+1] for the interior and dx[end-bstl+1 : end]
+    // for the high boundary rows (derivative_operator.jl:150-170), so a longer
+    // dx is accepted as it is there; a shorter one is its BoundsError.
+    if (ndx != 1 && (ndx < len + 1 || ndx < d + a))
+        return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 entry or at least max(len+1, d+a) entries");
     auto op = std::make_unique<deo_operator>();
     op->d = d; op->a = a; op->len = len;
     op->stl = d + a - 1 + (d + a) % 2;
@@ -218,7 +222,10 @@ extern "C" deo_status deo_upwind_difference(int d, int a, const double* dx, int 
     if (off < 0) return fail(DEO_ERR_BAD_ARG, "Number of offside points should be non-negative");
     if (off > (d + a - 1) / 2) return fail(DEO_ERR_BAD_ARG, "Number of offside points should not exceed the primary wind points");
     if (d < 0 || a < 1 || len < 1) return fail(DEO_ERR_BAD_ARG, "invalid derivative order or length");
-    if (ndx != 1 && ndx != len + 1) return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 or len+1 entries");
+    // The reference builds its grid x = [0; cumsum(dx)] and reads x[1 : len+2]
+    // (derivative_operator.jl:515-639): a longer dx is accepted, a shorter one
+    // is its BoundsError.
+    if (ndx != 1 && ndx < len + 1) return fail(DEO_ERR_BAD_SHAPE, "dx must have 1 entry or at least len+1 entries");
     auto op = std::make_unique<deo_operator>();
     op->d = d; op->a = a; op->len = len; op->wind = 1; op->off = off;
     op->stl = op->bstl = d + a;
@@ -246,7 +253,16 @@ extern "C" deo_status deo_upwind_difference(int d, int a, const double* dx, int 
         x[0] = 0.0;
         for (int k = 1; k <= len + 1; ++k) x[k] = x[k - 1] + dx[k - 1];
         auto X = [&](int j) { return x[j - 1]; };
-        auto sub = [&](int lo, int hi) { return std::vector<double>(x.begin() + (lo - 1), x.begin() + hi); };
+        // x[lo:hi] (1-based, inclusive); a window outside x is the reference's
+        // BoundsError for a grid too short for the stencil
+        bool outside = false;
+        auto sub = [&](int lo, int hi) {
+            if (lo < 1 || hi > len + 2 || hi - lo + 1 != bstl) {
+                outside = true;
+                return iota_d(0, bstl - 1);
+            }
+            return std::vector<double>(x.begin() + (lo - 1), x.begin() + hi);
+        };
         std::vector<double> up, dn;
         if (off == 0) {
             for (int i = 1; i <= bpc; ++i) append(up, fd_weights(d, X(i + 1), sub(i + 1, i + bstl)));
@@ -277,6 +293,7 @@ extern "C" deo_status deo_upwind_difference(int d, int a, const double* dx, int 
         op->hi = up;
         append(op->hi, dn);
         op->n_high = bpc + off;
+        if (outside) return fail(DEO_ERR_BAD_SHAPE, "grid too short for stencil");
     }
     op->coeff.assign(len, 0.0 + 1.0);
     op->cfs = 1;

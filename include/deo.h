@@ -63,7 +63,11 @@ int deo_abi_version(void);
 deo_status deo_calculate_weights(int order, double x0, const double* x, int n, double* out);
 
 /* ------------------------------------------------------------------------
- * Operators.  dx has ndx = 1 entry (uniform grid) or len+1 entries.
+ * Operators.  dx has ndx = 1 entry (uniform grid) or at least len+1 entries
+ * (non-uniform: the reference's upwind operators read dx[1:len+1], its
+ * centred ones dx[1:len+1] and the last d+a entries for the high boundary
+ * rows, so centred operators also need ndx >= d+a).  Grids too short for
+ * the stencil give DEO_ERR_BAD_SHAPE where the reference throws BoundsError.
  * ---------------------------------------------------------------------- */
 /* CenteredDifference{N}(d, a, dx, len), derivative_operator.jl:81-135 (uniform), :150-205 (non-uniform) */
 deo_status deo_centered_difference(int derivative_order, int approximation_order, const double* dx,

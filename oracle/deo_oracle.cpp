@@ -274,7 +274,16 @@ Op* upwind(int d, int a, const double* dx, int ndx, int len, int off) {
         x[0] = 0.0;
         for (int k = 1; k <= len + 1; ++k) x[k] = x[k - 1] + dx[k - 1];
         auto X = [&](int j) { return x[j - 1]; };  // Julia 1-based
-        auto sub = [&](int lo, int hi) { return vec(x.begin() + (lo - 1), x.begin() + hi); };
+        // x[lo:hi]; a window outside x is the reference's BoundsError (grid
+        // too short for the stencil): flagged, and the operator is rejected
+        bool outside = false;
+        auto sub = [&](int lo, int hi) {
+            if (lo < 1 || hi > len + 2 || hi < lo) {
+                outside = true;
+                return range_vec(0.0, bstl - 1.0);
+            }
+            return vec(x.begin() + (lo - 1), x.begin() + hi);
+        };
         // low: [upwind; downwind], each bpc rows
         vec up, dn;
         if (off == 0) {
@@ -311,6 +320,10 @@ Op* upwind(int d, int a, const double* dx, int ndx, int len, int off) {
         }
         op->high = up; op->high.insert(op->high.end(), dn.begin(), dn.end());
         op->n_high = bpc + off;
+        if (outside) {
+            delete op;
+            return nullptr;
+        }
     }
     op->coeff.assign(len, 1.0);
     op->coeff_func_sign = 1;
@@ -744,13 +757,15 @@ int orc_calculate_weights(int order, double x0, const double* x, int n, double* 
 
 void* orc_centered(int d, int a, const double* dx, int ndx, int len) {
     if (a < 2 || d < 0 || len < 1) return nullptr;
-    if (ndx != 1 && ndx != len + 1) return nullptr;
+    // dx[1:len+1] and dx[end-bstl+1:end] are read (derivative_operator.jl:150-170)
+    if (ndx != 1 && (ndx < len + 1 || ndx < d + a)) return nullptr;
     return centered(d, a, dx, ndx, len);
 }
 
 void* orc_upwind(int d, int a, const double* dx, int ndx, int len, int off) {
     if (off < 0 || off > (d + a - 1) / 2 || len < 1) return nullptr;
-    if (ndx != 1 && ndx != len + 1) return nullptr;
+    // x = [0; cumsum(dx)] is read at x[1:len+2] (derivative_operator.jl:515-639)
+    if (ndx != 1 && ndx < len + 1) return nullptr;
     return upwind(d, a, dx, ndx, len, off);
 }
 

@@ -77,6 +77,52 @@ def test_upwind_tables_bitwise(d, a, off, grid):
     _same(P.array(), Q.array())
 
 
+@pytest.mark.parametrize("kind", ["centered", "upwind"])
+def test_longer_dx_as_the_reference_reads_it(kind):
+    # The reference takes a dx longer than len+1: its upwind constructor reads
+    # x = [0; cumsum(dx)] at x[1:len+2] only, its centred constructor reads
+    # dx[1:len+1] for the interior and the last d+a entries for the high
+    # boundary rows (derivative_operator.jl:150-170, 515-639); the
+    # coefficient tests build UpwindDifference(1, 1, dxv, 3, ...) with five
+    # entries (coefficient_functions.jl:57-67).
+    rng = np.random.default_rng(5)
+    for d, a, off in ((1, 1, 0), (1, 2, 1), (2, 2, 0), (2, 3, 2)):
+        if kind == "centered":
+            a = max(a, 2)
+        n = 12
+        dx = rng.uniform(0.5, 1.5, n + 4) / n
+        P = (deo.CenteredDifference(d, a, dx, n) if kind == "centered"
+             else deo.UpwindDifference(d, a, dx, n, offside=off))
+        Q = O.centered(d, a, dx, n) if kind == "centered" else O.upwind(d, a, dx, n, offside=off)
+        st, lo, hi, co = Q.tables()
+        _same(P.stencil_coefs, st)
+        _same(P.low_boundary_coefs, lo)
+        _same(P.high_boundary_coefs, hi)
+        _same(P.array(), Q.array())
+        if kind == "upwind":  # only dx[1:len+1] matters
+            _same(P.array(), deo.UpwindDifference(d, a, dx[:n + 1], n, offside=off).array())
+
+
+@pytest.mark.parametrize("d,a,off,n,ndx", [
+    (2, 4, 0, 3, 4),     # centred: the high boundary needs the last d+a = 6 spacings
+    (1, 4, 0, 4, 4),     # too few spacings for len+1
+    (1, 4, 2, 2, 3),     # upwind, offside 2: the high downwind rows leave the grid
+    (1, 4, 2, 3, 4),
+])
+def test_grids_too_short_for_the_stencil_are_rejected(d, a, off, n, ndx):
+    # where the reference indexes outside x or dx (BoundsError), both the
+    # library and the oracle refuse the operator instead of reading past dx
+    dx = np.full(ndx, 0.1)
+    kind = "centered" if (d, a, off, n) in ((2, 4, 0, 3), (1, 4, 0, 4)) else "upwind"
+    with pytest.raises(deo.DeoShapeError):
+        if kind == "centered":
+            deo.CenteredDifference(d, a, dx, n)
+        else:
+            deo.UpwindDifference(d, a, dx, n, offside=off)
+    with pytest.raises(AssertionError):
+        O.centered(d, a, dx, n) if kind == "centered" else O.upwind(d, a, dx, n, offside=off)
+
+
 def test_bcs_bitwise():
     rng = np.random.default_rng(2)
     for order in (1, 2, 3):
