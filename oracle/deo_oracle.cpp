@@ -366,6 +366,7 @@ int robin(const double* l, const double* r, const double* dx, int ndx, int order
         out->br = gr / (ar - br * s[0] / h);
     } else {
         const int ns = order + 1;
+        if (ndx < ns) return -1;                // the reference's BoundsError
         const double* dxl = dx;                 // dx[1:ns]
         const double* dxr = dx + (ndx - ns);    // dx[end-ns+1:end]
         const double denom_l = al + bl * s[0] / dxl[0];
@@ -387,6 +388,7 @@ int general(const double* alpha_l, int nl, const double* alpha_r, int nr, const 
     out->kind = 0;
     const int wl = order + nl - 2, wr = order + nr - 2;
     if (wl - 1 > 32 || wr - 1 > 32) return -1;
+    if (ndx != 1 && (ndx < wl || ndx < wr)) return -1;  // the reference's BoundsError
     std::vector<vec> Sl(nl - 2, vec(wl, 0.0)), Sr(nr - 2, vec(wr, 0.0));
     vec dx_l, dx_r;
     if (ndx != 1) {

@@ -216,7 +216,7 @@ def robin(l, r, dx, order: int = 1) -> BC:
     lv, rv = _f64(l), _f64(r)
     dxv, n = _dx_arg(dx)
     if lib().orc_robin(_ptr(lv), _ptr(rv), _ptr(dxv), n, order, C.byref(q)) != 0:
-        raise ValueError("order too large")
+        raise ValueError("order too large or dx too short")
     return q
 
 
@@ -225,7 +225,7 @@ def general(al, ar, dx, order: int = 1) -> BC:
     alv, arv = _f64(al), _f64(ar)
     dxv, n = _dx_arg(dx)
     if lib().orc_general(_ptr(alv), len(alv), _ptr(arv), len(arv), _ptr(dxv), n, order, C.byref(q)) != 0:
-        raise ValueError("order too large")
+        raise ValueError("order too large or dx too short")
     return q
 
 
