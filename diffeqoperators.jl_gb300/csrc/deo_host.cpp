@@ -778,6 +778,10 @@ extern "C" int deo_fastdiv_probe(uint32_t n, uint32_t d) {  // host check of the
 // rotation: applies of one plan in flight at the same time on different
 // streams each need their own (up to kSchedSlots of them).
 constexpr unsigned int kSchedSlots = 1024;
+// DEO_OPT_FX_FP64_ROWS default: rows of each 32 x 8 tile of the fixed-point
+// kernel evaluated in the reference's FP64 order (FP64 pipe) beside the
+// integer-pipe rows
+constexpr int kFxFp64Rows = 2;
 
 struct deo_plan {
     PlanDev dev{};
@@ -1104,6 +1108,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             for (int t = 0; t < nterms && U.fx; ++t)
                 U.fx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
             if (U.fx) U.fx = fx_weights(U.t[0].w, H, nterms, U.fx_w, U.fx_f);
+            U.fx_rows = kFxFp64Rows;
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
             U.enabled = 0;
@@ -1219,6 +1224,10 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
             p->exact_sums = value;
             return DEO_OK;
         case DEO_OPT_CONCURRENT_SHELL: p->concurrent = value ? 1 : 0; return DEO_OK;
+        case DEO_OPT_FX_FP64_ROWS:
+            if (value < 0 || value > 8) return fail(DEO_ERR_BAD_ARG, "FP64 rows %d not in 0..8", value);
+            p->uni.fx_rows = value;
+            return DEO_OK;
         case DEO_OPT_LAUNCH_TIMING:
             if (value && !p->ev[0])
                 for (cudaEvent_t& e : p->ev) CUDA_TRY(cudaEventCreate(&e), "cudaEventCreate");
@@ -1235,6 +1244,11 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
         case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
+        case DEO_OPT_FX_FP64_ROWS:
+            return (p->dev.dtype == DEO_F64 && p->uni.enabled && p->uni.lap && p->exact_sums == 1 && p->uni.fx &&
+                    p->uni.radius <= 3)
+                       ? p->uni.fx_rows
+                       : 0;
         case DEO_OPT_CONCURRENT_SHELL:
             return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap &&
                    (p->dev.dtype == DEO_F32 || (p->exact_sums == 1 && p->uni.fx && p->uni.radius <= 3));

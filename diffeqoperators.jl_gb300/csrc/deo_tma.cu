@@ -614,55 +614,61 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
             const bool bz = (NT < 3) || (z + 1 >= U.t[NT - 1].flo && z + 1 <= U.t[NT - 1].fhi);
             if (!(live && bz)) continue;
             const int jg = gj - HZ;  // its centre plane
-            const long long* mc = dm(jg);
-            const short* ec = de(jg);
-            long long mt[2 * H][NT];  // [side * H + k - 1][axis]
-            int et[2 * H][NT];
-            const long long m0 = mc[cc];
-            const int e0 = ec[cc];
-#pragma unroll
-            for (int kk = 1; kk <= H; ++kk) {
-                mt[kk - 1][0] = mc[cc - kk];
-                et[kk - 1][0] = ec[cc - kk];
-                mt[H + kk - 1][0] = mc[cc + kk];
-                et[H + kk - 1][0] = ec[cc + kk];
-                mt[kk - 1][1] = mc[cc - kk * C::BX];
-                et[kk - 1][1] = ec[cc - kk * C::BX];
-                mt[H + kk - 1][1] = mc[cc + kk * C::BX];
-                et[H + kk - 1][1] = ec[cc + kk * C::BX];
-                if constexpr (NT == 3) {
-                    mt[kk - 1][2] = dm(jg - kk)[cc];
-                    et[kk - 1][2] = de(jg - kk)[cc];
-                    mt[H + kk - 1][2] = dm(jg + kk)[cc];
-                    et[H + kk - 1][2] = de(jg + kk)[cc];
-                }
-            }
-            int E = e0;
-#pragma unroll
-            for (int j = 0; j < 2 * H; ++j)
-#pragma unroll
-                for (int a = 0; a < NT; ++a) E = max(E, et[j][a]);
-            bool ok = E < 2047;
+            const int64_t idx = (int64_t)z * sxy + col;
             double total = 0.0;
-            if (ok) {
-                Acc128 A{0ULL, 0LL};
-                mad128(A, (long long)NT * sar64(m0, E - e0), U.fx_w[H]);
+            bool ok = false;
+            // rows ty < fx_rows of the tile (whole warps) take the reference's FP64 tap order below, on
+            // the FP64 pipe, while the other warps fill the integer pipes
+            if (ty >= U.fx_rows) {
+                const long long* mc = dm(jg);
+                const short* ec = de(jg);
+                long long mt[2 * H][NT];  // [side * H + k - 1][axis]
+                int et[2 * H][NT];
+                const long long m0 = mc[cc];
+                const int e0 = ec[cc];
 #pragma unroll
                 for (int kk = 1; kk <= H; ++kk) {
-                    long long sm = 0, sp = 0;
-#pragma unroll
-                    for (int a = 0; a < NT; ++a) {
-                        sm += sar64(mt[kk - 1][a], E - et[kk - 1][a]);
-                        sp += sar64(mt[H + kk - 1][a], E - et[H + kk - 1][a]);
+                    mt[kk - 1][0] = mc[cc - kk];
+                    et[kk - 1][0] = ec[cc - kk];
+                    mt[H + kk - 1][0] = mc[cc + kk];
+                    et[H + kk - 1][0] = ec[cc + kk];
+                    mt[kk - 1][1] = mc[cc - kk * C::BX];
+                    et[kk - 1][1] = ec[cc - kk * C::BX];
+                    mt[H + kk - 1][1] = mc[cc + kk * C::BX];
+                    et[H + kk - 1][1] = ec[cc + kk * C::BX];
+                    if constexpr (NT == 3) {
+                        mt[kk - 1][2] = dm(jg - kk)[cc];
+                        et[kk - 1][2] = de(jg - kk)[cc];
+                        mt[H + kk - 1][2] = dm(jg + kk)[cc];
+                        et[H + kk - 1][2] = de(jg + kk)[cc];
                     }
-                    mad128(A, sm, U.fx_w[H - kk]);
-                    mad128(A, sp, U.fx_w[H + kk]);
                 }
-                total = fx_round(A.hi, A.lo, ebase0 + E, ok);
+                int E = e0;
+#pragma unroll
+                for (int j = 0; j < 2 * H; ++j)
+#pragma unroll
+                    for (int a = 0; a < NT; ++a) E = max(E, et[j][a]);
+                ok = E < 2047;
+                if (ok) {
+                    Acc128 A{0ULL, 0LL};
+                    mad128(A, (long long)NT * sar64(m0, E - e0), U.fx_w[H]);
+#pragma unroll
+                    for (int kk = 1; kk <= H; ++kk) {
+                        long long sm = 0, sp = 0;
+#pragma unroll
+                        for (int a = 0; a < NT; ++a) {
+                            sm += sar64(mt[kk - 1][a], E - et[kk - 1][a]);
+                            sp += sar64(mt[H + kk - 1][a], E - et[H + kk - 1][a]);
+                        }
+                        mad128(A, sm, U.fx_w[H - kk]);
+                        mad128(A, sp, U.fx_w[H + kk]);
+                    }
+                    total = fx_round(A.hi, A.lo, ebase0 + E, ok);
+                }
             }
-            const int64_t idx = (int64_t)z * sxy + col;
             if (!ok) {
-                // Inf/NaN or an extreme exponent: the reference's per-term tap order, from global memory
+                // FP64 rows, Inf/NaN or an extreme exponent: the reference's per-term tap order, from global
+                // memory (L2-resident: the ring has just loaded these planes)
                 const int64_t st[3] = {1, (int64_t)nx, sxy};
 #pragma unroll
                 for (int t = 0; t < NT; ++t) {

@@ -692,19 +692,24 @@ class Plan:
         check(L.lib().deo_plan_set_option(self._h, int(option), int(value)))
         return self
 
-    def get_option(self, option: int) -> bool:
-        return L.lib().deo_plan_get_option(self._h, int(option)) == 1
+    def get_option(self, option: int) -> int:
+        """1 / 0 whether a switch is on and applies to this plan; the row count
+        for DEO_OPT_FX_FP64_ROWS (0 when the fixed-point kernel does not apply)."""
+        v = L.lib().deo_plan_get_option(self._h, int(option))
+        if v < 0:
+            raise DeoArgError(2, f"unknown plan option {option}")
+        return v
 
     def set_fast_path(self, enable: bool):
         return self.set_option(L.DEO_OPT_FAST_PATH, enable)
 
     @property
     def uses_fast_path(self) -> bool:
-        return self.get_option(L.DEO_OPT_FAST_PATH)
+        return self.get_option(L.DEO_OPT_FAST_PATH) == 1
 
     @property
     def uses_exact_sums(self) -> bool:
-        return self.get_option(L.DEO_OPT_EXACT_SUMS)
+        return self.get_option(L.DEO_OPT_EXACT_SUMS) == 1
 
     @property
     def kernels(self) -> tuple:

@@ -205,12 +205,21 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     plans and to the fixed-point Float64 interior (whose FP64 pipe is free
  *     for the shell); other Float64 interiors are FP64-bound and run the
  *     shell after them.  0 runs the shell after the interior always.
+ *   DEO_OPT_FX_FP64_ROWS: 0..8 (default 2): in the fixed-point Float64
+ *     interior kernel, the points of rows 0..value-1 of every 32 x 8 tile
+ *     (y mod 8 < value, y the 0-based index along axis 2; whole warps) are
+ *     evaluated in the reference's per-term tap order on the FP64 pipe,
+ *     bit-identical to the generic kernel, while the other rows use the
+ *     integer pipes; 0 evaluates every interior point in fixed point.
+ *     deo_plan_get_option returns the value when the fixed-point kernel
+ *     applies, else 0.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
 #define DEO_OPT_EXACT_SUMS 3
 #define DEO_OPT_LAUNCH_TIMING 4
 #define DEO_OPT_CONCURRENT_SHELL 5
+#define DEO_OPT_FX_FP64_ROWS 6
 deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);

@@ -303,12 +303,15 @@ def _wide_range(shape, seed):
     return np.asfortranarray(u)
 
 
+@pytest.mark.parametrize("rows", [0, 3, 8])
 @pytest.mark.parametrize("field", ["normal", "wide", "special"])
 @pytest.mark.parametrize("case", LAP_CASES, ids=["3d-a4-robin", "3d-a2-dirichlet0", "2d-a4-robin"])
-def test_fixed_point_kernel_against_integer_model(cuda, case, field):
+def test_fixed_point_kernel_against_integer_model(cuda, case, field, rows):
     """Interior points: bit for bit the integer model (tests/fx_model.py) and
-    within 2 ulp of sum|c_k u_k| of the exact rational value; shell points and
-    Inf/NaN fallbacks: bit for bit the reference's order."""
+    within 2 ulp of sum|c_k u_k| of the exact rational value; shell points,
+    Inf/NaN fallbacks and the tile rows evaluated on the FP64 pipe
+    (DEO_OPT_FX_FP64_ROWS: y mod 8 < rows, 0-based y): bit for bit the
+    reference's order."""
     import itertools
     from fractions import Fraction
     import fx_model as FX
@@ -324,6 +327,8 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field):
     ud = to_device(u)
     got_t, gen_t = deo.julia_array(shape), deo.julia_array(shape)
     p.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
+    p.set_option(deo.DEO_OPT_FX_FP64_ROWS, rows)
+    assert p.get_option(deo.DEO_OPT_FX_FP64_ROWS) == rows
     p.apply(ud, got_t)
     assert p.kernels[0] == "k_lap_fx"
     p.set_option(deo.DEO_OPT_FAST_PATH, 0)
@@ -342,6 +347,9 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field):
     worst = 0.0
     fallbacks = 0
     for idx in itertools.product(*inner):
+        if idx[1] % 8 < rows:
+            assert np.array_equal(got[idx], gen[idx], equal_nan=True), idx
+            continue
         m = FX.fx_point(u, idx, w, H, nt)
         if m is None:
             fallbacks += 1
@@ -354,7 +362,10 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field):
                 err = abs(Fraction(float(got[idx])) - val)
                 worst = max(worst, float(err / Fraction(float(np.spacing(float(scale))))))
     assert worst <= 2.0, worst
-    assert (fallbacks > 0) == (field == "special")
+    if rows == 0:
+        assert (fallbacks > 0) == (field == "special")
+    elif field != "special":
+        assert fallbacks == 0
     assert deo.device_status() == 0
 
 
