@@ -1536,22 +1536,38 @@ struct deo_padded {
     int dtype = 0;
 };
 
-extern "C" deo_status deo_padded_plan(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
-                                      const int64_t* in_sizes, deo_dtype dtype, deo_padded** out) {
+// starts = null: M's size along every axis but `axis` equals x_temp's or is 2
+// longer (then its edge planes are skipped, the stripping of
+// derivative_operator_functions.jl:47-56); else M is the view of the array
+// with sizes in_sizes that begins at 0-based index starts[b] along axis b.
+static deo_status padded_plan(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                              const int64_t* in_sizes, const int64_t* starts, deo_dtype dtype, deo_padded** out) {
     if (!op || !out_sizes || !in_sizes || !out) return fail(DEO_ERR_BAD_ARG, "null argument");
     *out = nullptr;
     if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
     if (axis < 1 || axis > ndims) return fail(DEO_ERR_BAD_SHAPE, "axis %d outside 1..%d", axis, ndims);
     if (dtype != DEO_F64 && dtype != DEO_F32) return fail(DEO_ERR_BAD_ARG, "unknown dtype");
     const int a = axis - 1;
+    int64_t start[DEO_MAX_DIMS];
     for (int b = 0; b < ndims; ++b) {
         if (out_sizes[b] < 1) return fail(DEO_ERR_BAD_SHAPE, "size(x_temp, %d) = %lld", b + 1, (long long)out_sizes[b]);
+        if (starts) {
+            start[b] = starts[b];
+            const bool ok = b == a ? (start[b] == 0 && in_sizes[b] >= out_sizes[b] + 2)
+                                   : (start[b] >= 0 && start[b] + out_sizes[b] <= in_sizes[b]);
+            if (!ok)
+                return fail(DEO_ERR_BAD_SHAPE, "view of M along %d (start %lld, size(M) %lld) does not hold x_temp's %lld%s",
+                            b + 1, (long long)start[b], (long long)in_sizes[b], (long long)out_sizes[b],
+                            b == a ? " + 2 from index 0 (the differentiated dimension)" : "");
+            continue;
+        }
         const bool ok = b == a ? in_sizes[b] == out_sizes[b] + 2
                                : (in_sizes[b] == out_sizes[b] || in_sizes[b] == out_sizes[b] + 2);
         if (!ok)
             return fail(DEO_ERR_BAD_SHAPE, "size(M, %d) = %lld does not fit size(x_temp, %d) = %lld%s", b + 1,
                         (long long)in_sizes[b], b + 1, (long long)out_sizes[b],
                         b == a ? " + 2 (the differentiated dimension must be padded)" : " (or + 2)");
+        start[b] = (b != a && in_sizes[b] == out_sizes[b] + 2) ? 1 : 0;
     }
     if (out_sizes[a] != op->len)
         return fail(DEO_ERR_BAD_SHAPE, "size(x_temp, %d) = %lld but the operator has len %d", axis,
@@ -1565,7 +1581,7 @@ extern "C" deo_status deo_padded_plan(const deo_operator* op, int axis, int ndim
     for (int b = 0; b < ndims; ++b) {
         D.len[b] = out_sizes[b];
         D.pstride[b] = pv;
-        if (b != a && in_sizes[b] == out_sizes[b] + 2) coff += pv;
+        coff += start[b] * pv;
         pv *= in_sizes[b];
         ov *= out_sizes[b];
     }
@@ -1588,6 +1604,18 @@ extern "C" deo_status deo_padded_plan(const deo_operator* op, int axis, int ndim
     P->dtype = dtype;
     *out = P.release();
     return DEO_OK;
+}
+
+extern "C" deo_status deo_padded_plan(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                                      const int64_t* in_sizes, deo_dtype dtype, deo_padded** out) {
+    return padded_plan(op, axis, ndims, out_sizes, in_sizes, nullptr, dtype, out);
+}
+
+extern "C" deo_status deo_padded_plan_view(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                                           const int64_t* in_sizes, const int64_t* starts, deo_dtype dtype,
+                                           deo_padded** out) {
+    if (!starts) return fail(DEO_ERR_BAD_ARG, "null starts");
+    return padded_plan(op, axis, ndims, out_sizes, in_sizes, starts, dtype, out);
 }
 
 extern "C" deo_status deo_padded_apply(const deo_padded* p, const void* M, void* x_temp, int overwrite,

@@ -124,6 +124,8 @@ def lib():
     proto("deo_nonlinear_diffusion_destroy", None, _vp)
     proto("deo_padded_plan", st, _vp, C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int,
           C.POINTER(_vp))
+    proto("deo_padded_plan_view", st, _vp, C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+          C.POINTER(C.c_int64), C.c_int, C.POINTER(_vp))
     proto("deo_padded_apply", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_padded_destroy", None, _vp)
     proto("deo_solve_plan", st, _vp, _vp, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(_vp))
@@ -179,5 +181,5 @@ EXPORTED = [
     "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply", "deo_vector_calculus_info",
     "deo_vector_calculus_destroy", "deo_dot_product", "deo_cross_product", "deo_square_norm",
     "deo_solve_plan", "deo_solve_bands", "deo_solve_apply", "deo_solve_destroy",
-    "deo_padded_plan", "deo_padded_apply", "deo_padded_destroy",
+    "deo_padded_plan", "deo_padded_plan_view", "deo_padded_apply", "deo_padded_destroy",
 ]

@@ -622,6 +622,8 @@ class DiffEqOperatorCombination:
             return DiffEqOperatorCombination([op * other for op in self.ops])
         if all(isinstance(o, GhostDerivativeOperator) for o in self.ops):
             return _apply_terms(self.ops, other)
+        if self.ops and all(isinstance(o, DerivativeOperator) for o in self.ops):
+            return _combination_times_padded(self.ops, other)
         raise DeoArgError(2, "apply a boundary condition first: (A*Q)*u")
 
     def terms(self):
@@ -815,18 +817,24 @@ def mul_(du, A, u, overwrite: bool = True):
     (derivative_operator_functions.jl:17-25)."""
     if isinstance(A, DerivativeOperator):
         return _mul_padded(A, u, du, overwrite)
+    if isinstance(A, DiffEqOperatorCombination) and A.ops and all(isinstance(o, DerivativeOperator) for o in A.ops):
+        return _combination_mul_padded(du, A.ops, u)
     return _apply_terms(A.terms(), u, du, overwrite)
 
 
 class PaddedPlan:
     """A compiled deo_padded: L on an already padded array for (sizes, dtype)."""
 
-    def __init__(self, op: DerivativeOperator, out_shape, in_shape, dtype_code: int):
+    def __init__(self, op: DerivativeOperator, out_shape, in_shape, dtype_code: int, starts=None):
         nd = len(in_shape)
         osz = (C.c_int64 * nd)(*out_shape)
         isz = (C.c_int64 * nd)(*in_shape)
         h = C.c_void_p()
-        check(L.lib().deo_padded_plan(op._h, int(op.axis), nd, osz, isz, int(dtype_code), C.byref(h)))
+        if starts is None:
+            check(L.lib().deo_padded_plan(op._h, int(op.axis), nd, osz, isz, int(dtype_code), C.byref(h)))
+        else:
+            st = (C.c_int64 * nd)(*starts)
+            check(L.lib().deo_padded_plan_view(op._h, int(op.axis), nd, osz, isz, st, int(dtype_code), C.byref(h)))
         self._h = h
 
     def __del__(self):
@@ -869,6 +877,67 @@ def _mul_padded(op: DerivativeOperator, M, out=None, overwrite: bool = True):
     check(L.lib().deo_padded_apply(hit[1]._h, C.c_void_p(M.data_ptr()), C.c_void_p(out.data_ptr()),
                                    1 if overwrite else 0, _stream_ptr()))
     return out
+
+
+def _padded_view_apply(op: DerivativeOperator, M, out, starts, overwrite: bool):
+    """mul!(out, op, view(M, ...)) with the view beginning at the 0-based
+    `starts` (0 along op's axis) and out's size along the other axes."""
+    key = ("view", id(op), tuple(out.shape), tuple(M.shape), tuple(starts), _dtype_code(M))
+    hit = _padded_cache.get(key)
+    if hit is None or hit[0] is not op:
+        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M), starts))
+    check(L.lib().deo_padded_apply(hit[1]._h, C.c_void_p(M.data_ptr()), C.c_void_p(out.data_ptr()),
+                                   1 if overwrite else 0, _stream_ptr()))
+    return out
+
+
+def _combination_times_padded(ops, M):
+    """(L1 + L2 + ...) * M = sum(op -> op * M, ops) (composite_operators.jl:64-65)
+    for DerivativeOperators on an already padded M: the first product written,
+    the others added in order (every product must have the first one's size)."""
+    out = _mul_padded(ops[0], M)
+    for op in ops[1:]:
+        oshape = tuple(n - 2 if b == op.axis - 1 else n for b, n in enumerate(M.shape))
+        if oshape != tuple(out.shape):
+            raise DimensionMismatch(f"dimensions must match: a has dims {tuple(out.shape)}, b has dims {oshape}")
+        _mul_padded(op, M, out, overwrite=False)
+    return out
+
+
+def _combination_mul_padded(x_temp, ops, M):
+    """mul!(x_temp, L1 + L2 + ..., M) for DerivativeOperators on an already
+    padded M.  Vectors: the first operator written, the others added through a
+    cache (composite_operators.jl:76-83).  2-D and 3-D arrays: the reference's
+    composite method (derivative_operator_functions.jl:203-463, 466-802) with
+    its fallback branch, the one publicly constructed operators reach (their
+    coefficients are Vectors): each operator reads view(M, 1:x_temp_1, ...,
+    1:(x_temp_k + 2), ...) -- starting at index 1 along the other axes even
+    where M is padded there -- except, in 2-D, along an axis no operator of
+    the sum acts on, where it reads M whole (and _mul! strips M's edge planes
+    if it is padded there).  The first operator overwrites, the others add."""
+    if x_temp is None:
+        raise DeoArgError(2, "mul!(x_temp, A, M) needs x_temp")
+    _check_layout(M, "M")
+    _check_layout(x_temp, "x_temp")
+    nd = M.dim()
+    if x_temp.dim() != nd or x_temp.dtype != M.dtype:
+        raise DeoShapeError(1, "x_temp must have M's number of dimensions and dtype")
+    if nd == 1:
+        for k, op in enumerate(ops):
+            _mul_padded(op, M, x_temp, overwrite=(k == 0))
+        return x_temp
+    if nd not in (2, 3):
+        raise DeoArgError(2, f"no mul! method for a sum of operators on a {nd}-D array (2-D and 3-D only)")
+    operated = {op.axis for op in ops}
+    for k, op in enumerate(ops):
+        if op.axis > nd:
+            raise DeoShapeError(1, f"the operator acts on axis {op.axis} but M has {nd} dimensions")
+        others = [b for b in range(1, nd + 1) if b != op.axis]
+        if nd == 2 and not (set(others) & operated):
+            _mul_padded(op, M, x_temp, overwrite=(k == 0))
+            continue
+        _padded_view_apply(op, M, x_temp, [0] * nd, overwrite=(k == 0))
+    return x_temp
 
 
 def concretize(A, shape, dtype=np.float64):

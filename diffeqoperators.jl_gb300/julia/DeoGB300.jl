@@ -136,7 +136,9 @@ _stream() = CUDA.stream().handle
 
 # mul!(du, A*Q, u) and (A*Q)*u on the GPU (ghost_derivative_operator.jl:15-37,
 # composite_operators.jl:64-83)
-const DeoOp = Union{GhostDerivativeOperator, DiffEqOperatorCombination}
+const GhostCombination = DiffEqOperatorCombination{<:Any, <:Tuple{Vararg{GhostDerivativeOperator}}}
+const DerivCombination = DiffEqOperatorCombination{<:Any, <:Tuple{Vararg{DerivativeOperator}}}
+const DeoOp = Union{GhostDerivativeOperator, GhostCombination}
 
 function LinearAlgebra.mul!(du::CuArray{T}, A::DeoOp, u::CuArray{T}; overwrite = true) where {T <: Union{Float32, Float64}}
     size(du) == size(u) || throw(DimensionMismatch("du and u differ in size"))
@@ -153,6 +155,87 @@ end
 
 # (L)(du, u, p, t) right-hand-side interface (DiffEqOperators.jl:67-76)
 (A::GhostDerivativeOperator)(du::CuArray, u::CuArray, p, t) = mul!(du, A, u)
+
+# ---- L*M and mul!(x_temp, L, M) on an already padded array -------------------
+# (derivative_operator_functions.jl:17-69, 150-163; convolutions.jl:17-22), and
+# sums of DerivativeOperators on one (composite_operators.jl:64-83 and the
+# 2-D / 3-D method of derivative_operator_functions.jl:203-802, whose fallback
+# branch -- the one operators with Vector coefficients take -- reads views of
+# M that begin at index 1 on the other axes: deo_padded_plan_view)
+const PADDED = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
+
+function padded_plan_for(L::DerivativeOperator, osz::Dims, isz::Dims, ::Type{T},
+                         starts) where {T <: Union{Float32, Float64}}
+    cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), PADDED, L)
+    get!(cache, (osz, isz, T, starts)) do
+        op = deo_operator(L)
+        o, i = Int64[osz...], Int64[isz...]
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        dt = T === Float64 ? 0 : 1
+        if starts === nothing
+            GC.@preserve o i check(ccall((:deo_padded_plan, libdeo), Cint,
+                                         (Ptr{Cvoid}, Cint, Cint, Ptr{Int64}, Ptr{Int64}, Cint, Ref{Ptr{Cvoid}}),
+                                         op, _axis(L), length(osz), o, i, dt, h))
+        else
+            st = Int64[starts...]
+            GC.@preserve o i st check(ccall((:deo_padded_plan_view, libdeo), Cint,
+                                            (Ptr{Cvoid}, Cint, Cint, Ptr{Int64}, Ptr{Int64}, Ptr{Int64}, Cint,
+                                             Ref{Ptr{Cvoid}}), op, _axis(L), length(osz), o, i, st, dt, h))
+        end
+        ccall((:deo_operator_destroy, libdeo), Cvoid, (Ptr{Cvoid},), op)
+        h[]
+    end
+end
+
+function _padded!(x_temp::CuArray{T}, L::DerivativeOperator, M::CuArray{T}, overwrite::Bool,
+                  starts = nothing) where {T <: Union{Float32, Float64}}
+    p = padded_plan_for(L, size(x_temp), size(M), T, starts)
+    check(ccall((:deo_padded_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Cint, Ptr{Cvoid}),
+                p, M, x_temp, overwrite, _stream()))
+    return x_temp
+end
+
+function LinearAlgebra.mul!(x_temp::CuArray{T}, L::DerivativeOperator, M::CuArray{T};
+                            overwrite = true) where {T <: Union{Float32, Float64}}
+    return _padded!(x_temp, L, M, overwrite)
+end
+
+function Base.:*(L::DerivativeOperator, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+    N = _axis(L)
+    return _padded!(similar(M, ntuple(b -> b == N ? size(M, b) - 2 : size(M, b), ndims(M))), L, M, true)
+end
+
+function LinearAlgebra.mul!(x_temp::CuArray{T}, A::DerivCombination, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+    nd = ndims(M)
+    if nd == 1
+        for (k, L) in enumerate(A.ops)
+            _padded!(x_temp, L, M, k == 1)
+        end
+        return x_temp
+    end
+    nd in (2, 3) || throw(MethodError(mul!, (x_temp, A, M)))
+    operated = Set(_axis(L) for L in A.ops)
+    for (k, L) in enumerate(A.ops)
+        others = setdiff(1:nd, (_axis(L),))
+        if nd == 2 && isempty(intersect(others, operated))
+            _padded!(x_temp, L, M, k == 1)
+        else
+            _padded!(x_temp, L, M, k == 1, ntuple(_ -> 0, nd))
+        end
+    end
+    return x_temp
+end
+
+function Base.:*(A::DerivCombination, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+    x = A.ops[1] * M
+    for L in A.ops[2:end]
+        N = _axis(L)
+        sz = ntuple(b -> b == N ? size(M, b) - 2 : size(M, b), ndims(M))
+        sz == size(x) || throw(DimensionMismatch("dimensions must match: a has dims $(size(x)), b has dims $sz"))
+        _padded!(x, L, M, false)
+    end
+    return x
+end
 
 # ---- ChainRulesCore.rrule: pullback = adjoint kernel ------------------------
 using ChainRulesCore

@@ -295,6 +295,15 @@ deo_status deo_padded_plan(const deo_operator* op, int axis, int ndims, const in
                            const int64_t* in_sizes, deo_dtype dtype, deo_padded** out);
 deo_status deo_padded_apply(const deo_padded* plan, const void* M, void* x_temp, int overwrite, void* stream);
 void deo_padded_destroy(deo_padded* plan);
+/* The same on a view of M: M has sizes in_sizes and the operator reads the
+ * block that starts at 0-based index starts[b] along axis b and has x_temp's
+ * size there (starts[axis-1] = 0: the first len+2 entries along the
+ * differentiated axis).  Replaces the `view(M, 1:x_temp_1, ..., 1:(x_temp_k+2),
+ * ...)` calls of mul!(x_temp, A::DiffEqOperatorCombination, M) for 2-D and
+ * 3-D arrays (derivative_operator_functions.jl:380-463, 742-800), which begin
+ * at index 1 along the other axes even where M is padded there. */
+deo_status deo_padded_plan_view(const deo_operator* op, int axis, int ndims, const int64_t* out_sizes,
+                                const int64_t* in_sizes, const int64_t* starts, deo_dtype dtype, deo_padded** out);
 
 /* ------------------------------------------------------------------------
  * Implicit solves: x = A \ u for A = L*Q (ghost_derivative_operator.jl:39-58).

@@ -340,6 +340,40 @@ def mul_nd(op: Op, M, out_shape=None, out=None, overwrite: bool = True, absolute
     return o
 
 
+def mul_combination(ops, M, x_temp, absolute: bool = False) -> np.ndarray:
+    """mul!(x_temp, L1 + L2 + ..., M) for DerivativeOperators on an already
+    padded M, restated from the reference: vectors through the cache loop of
+    composite_operators.jl:76-83; 2-D and 3-D arrays through the fallback
+    branch of derivative_operator_functions.jl:380-463 (2-D) and 771-800 (3-D),
+    which every operator with Vector coefficients takes: operator k reads
+    view(M, 1:x_temp_1, ..., 1:(x_temp_axis + 2), ...), i.e. the block of M
+    that begins at index 1 on every axis, except that in 2-D an operator whose
+    other axis no operator of the sum acts on reads M whole.  The first
+    operator overwrites x_temp, the others add into it (mul!(...; overwrite =
+    false)).  absolute=True gives sum_k |c_k u_k| over all operators' rows (the
+    tolerance scale)."""
+    M = np.asfortranarray(M, dtype=np.float64)
+    nd = M.ndim
+    if nd not in (1, 2, 3):
+        raise AssertionError("mul! of a sum of operators is defined for vectors and 2-D / 3-D arrays")
+    operated = {op.axis for op in ops}
+    for k, op in enumerate(ops):
+        V = M
+        others = {b for b in range(1, nd + 1) if b != op.axis}
+        if nd == 3 or (nd == 2 and others & operated):
+            V = np.asfortranarray(M[tuple(slice(0, x_temp.shape[b - 1] + (2 if b == op.axis else 0))
+                                          for b in range(1, nd + 1))])
+        if not absolute:
+            mul_nd(op, V, out_shape=x_temp.shape, out=x_temp, overwrite=(k == 0))
+            continue
+        a = mul_nd(op, V, out_shape=x_temp.shape, absolute=True)
+        if k == 0:
+            x_temp[...] = a
+        else:
+            x_temp += a
+    return x_temp
+
+
 GRADIENT, DIVERGENCE, CURL = 0, 1, 2
 
 
