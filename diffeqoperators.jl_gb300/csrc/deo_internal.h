@@ -108,7 +108,7 @@ struct UniPlan {
     // r = c0[mask]*u0 + sum_{o != 0} w[o] * S_o, where S_o = the exact sum of
     // the |mask| neighbours at offset o (one per axis), rounded once.
     int ens;
-    int fx_rows;  // fixed-point kernel: rows ty < fx_rows of each 32 x 8 tile use the reference's FP64 order
+    int fx_rows;  // fixed-point kernel: fx_rows of each 32 x 8 tile's rows (rotating) use the FP64 order
     double ens_c0[8];             // merged centre weight for each mask of axes
     double ens_w[DEO_MAX_NW];     // band weight at offset k - H (index k)
     // Fixed-point evaluation (Float64, one shared band of nonzero normal

@@ -617,9 +617,11 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
             const int64_t idx = (int64_t)z * sxy + col;
             double total = 0.0;
             bool ok = false;
-            // rows ty < fx_rows of the tile (whole warps) take the reference's FP64 tap order below, on
-            // the FP64 pipe, while the other warps fill the integer pipes
-            if (ty >= U.fx_rows) {
+            // fx_rows of the tile's 8 rows (whole warps) take the reference's FP64 tap order below, on
+            // the FP64 pipe, while the other warps fill the integer pipes; the rows rotate with the
+            // tile row and the plane, (ty - fx_rows * (tyi + z)) mod 8 < fx_rows, so that the FP64
+            // warps take turns on the SM's four sub-partitions (warp ty runs on sub-partition ty mod 4)
+            if (((ty - U.fx_rows * (tyi + z)) & 7) >= U.fx_rows) {
                 const long long* mc = dm(jg);
                 const short* ec = de(jg);
                 long long mt[2 * H][NT];  // [side * H + k - 1][axis]

@@ -206,11 +206,12 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     for the shell); other Float64 interiors are FP64-bound and run the
  *     shell after them.  0 runs the shell after the interior always.
  *   DEO_OPT_FX_FP64_ROWS: 0..8 (default 2): in the fixed-point Float64
- *     interior kernel, the points of rows 0..value-1 of every 32 x 8 tile
- *     (y mod 8 < value, y the 0-based index along axis 2; whole warps) are
- *     evaluated in the reference's per-term tap order on the FP64 pipe,
- *     bit-identical to the generic kernel, while the other rows use the
- *     integer pipes; 0 evaluates every interior point in fixed point.
+ *     interior kernel, the points with ((y mod 8) - value * (floor(y/8) + z))
+ *     mod 8 < value (y, z the 0-based indices along axes 2 and 3, z = 0 in
+ *     2-D: `value` of every 8 rows of a 32 x 8 tile, rotating from plane to
+ *     plane; whole warps) are evaluated in the reference's per-term tap order
+ *     on the FP64 pipe, bit-identical to the generic kernel, while the others
+ *     use the integer pipes; 0 evaluates every interior point in fixed point.
  *     deo_plan_get_option returns the value when the fixed-point kernel
  *     applies, else 0.
  * No reference counterpart (execution choices only). */

@@ -310,8 +310,8 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field, rows):
     """Interior points: bit for bit the integer model (tests/fx_model.py) and
     within 2 ulp of sum|c_k u_k| of the exact rational value; shell points,
     Inf/NaN fallbacks and the tile rows evaluated on the FP64 pipe
-    (DEO_OPT_FX_FP64_ROWS: y mod 8 < rows, 0-based y): bit for bit the
-    reference's order."""
+    (DEO_OPT_FX_FP64_ROWS: ((y mod 8) - rows * (floor(y/8) + z)) mod 8 < rows,
+    0-based y, z): bit for bit the reference's order."""
     import itertools
     from fractions import Fraction
     import fx_model as FX
@@ -347,7 +347,7 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field, rows):
     worst = 0.0
     fallbacks = 0
     for idx in itertools.product(*inner):
-        if idx[1] % 8 < rows:
+        if (idx[1] % 8 - rows * (idx[1] // 8 + (idx[2] if nt == 3 else 0))) % 8 < rows:
             assert np.array_equal(got[idx], gen[idx], equal_nan=True), idx
             continue
         m = FX.fx_point(u, idx, w, H, nt)
