@@ -223,3 +223,24 @@ def test_banded_matrix_export(kind, d, a, grid):
     assert (lo, up) == want
     assert data.shape == (lo + up + 1, n + 2)
     _same(_from_band(data, lo, up, n), Q.array())
+
+
+def test_padded_view_plan_rejects_bad_views():
+    # deo_padded_plan_view validates the view before it touches the device:
+    # starts[axis-1] must be 0 with len+2 entries there, and the block must fit in M
+    import ctypes as C
+    lib = deo.lib()
+    L = deo.CenteredDifference(2, 2, 1.0, 10, axis=1)
+    h = C.c_void_p()
+    I64 = C.c_int64 * 2
+
+    def plan(out, inn, starts):
+        return lib.deo_padded_plan_view(L._h, 1, 2, I64(*out), I64(*inn), None if starts is None else I64(*starts),
+                                        0, C.byref(h))
+    assert plan((10, 8), (12, 10), None) == 2                         # null starts: DEO_ERR_BAD_ARG
+    assert plan((10, 8), (12, 10), (1, 0)) == 1                       # the differentiated axis starts at 0
+    assert b"differentiated" in lib.deo_last_error()
+    assert plan((10, 8), (11, 10), (0, 0)) == 1                       # len + 2 entries along it
+    assert plan((10, 8), (12, 10), (0, 3)) == 1                       # 3 + 8 > 10 along axis 2
+    assert plan((10, 8), (12, 10), (0, -1)) == 1
+    assert not h.value
