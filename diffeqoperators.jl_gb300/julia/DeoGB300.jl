@@ -140,7 +140,7 @@ const GhostCombination = DiffEqOperatorCombination{<:Any, <:Tuple{Vararg{GhostDe
 const DerivCombination = DiffEqOperatorCombination{<:Any, <:Tuple{Vararg{DerivativeOperator}}}
 const DeoOp = Union{GhostDerivativeOperator, GhostCombination}
 
-function LinearAlgebra.mul!(du::CuArray{T}, A::DeoOp, u::CuArray{T}; overwrite = true) where {T <: Union{Float32, Float64}}
+function _ghost_mul!(du::CuArray{T}, A::DeoOp, u::CuArray{T}, overwrite) where {T <: Union{Float32, Float64}}
     size(du) == size(u) || throw(DimensionMismatch("du and u differ in size"))
     p = plan_for(A, size(u), T)
     check(ccall((:deo_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Cint, Ptr{Cvoid}),
@@ -148,10 +148,24 @@ function LinearAlgebra.mul!(du::CuArray{T}, A::DeoOp, u::CuArray{T}; overwrite =
     return du
 end
 
-function Base.:*(A::DeoOp, u::CuArray{T}) where {T <: Union{Float32, Float64}}
-    du = similar(u)
-    return mul!(du, A, u)
+# Every method below is strictly more specific than the reference method it
+# shadows (the reference defines each for AbstractVecOrMat and AbstractArray,
+# its sums also for 2-D and 3-D arrays), so no call is ambiguous.
+const FT = Union{Float32, Float64}
+for CA in (:CuVecOrMat, :CuArray)
+    @eval begin
+        LinearAlgebra.mul!(du::$CA{T}, A::GhostDerivativeOperator, u::$CA{T}; overwrite = true) where {T <: FT} =
+            _ghost_mul!(du, A, u, overwrite)
+        Base.:*(A::GhostDerivativeOperator, u::$CA{T}) where {T <: FT} = _ghost_mul!(similar(u), A, u, true)
+        Base.:*(A::GhostCombination, u::$CA{T}) where {T <: FT} = _ghost_mul!(similar(u), A, u, true)
+    end
 end
+for Nd in 1:3
+    @eval LinearAlgebra.mul!(du::CuArray{T, $Nd}, A::GhostCombination, u::CuArray{T, $Nd};
+                             overwrite = true) where {T <: FT} = _ghost_mul!(du, A, u, overwrite)
+end
+LinearAlgebra.mul!(du::CuArray{T}, A::GhostCombination, u::CuArray{T}; overwrite = true) where {T <: FT} =
+    _ghost_mul!(du, A, u, overwrite)
 
 # (L)(du, u, p, t) right-hand-side interface (DiffEqOperators.jl:67-76)
 (A::GhostDerivativeOperator)(du::CuArray, u::CuArray, p, t) = mul!(du, A, u)
@@ -195,17 +209,12 @@ function _padded!(x_temp::CuArray{T}, L::DerivativeOperator, M::CuArray{T}, over
     return x_temp
 end
 
-function LinearAlgebra.mul!(x_temp::CuArray{T}, L::DerivativeOperator, M::CuArray{T};
-                            overwrite = true) where {T <: Union{Float32, Float64}}
-    return _padded!(x_temp, L, M, overwrite)
-end
-
-function Base.:*(L::DerivativeOperator, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+function _padded_times(L::DerivativeOperator, M::CuArray{T}) where {T <: FT}
     N = _axis(L)
     return _padded!(similar(M, ntuple(b -> b == N ? size(M, b) - 2 : size(M, b), ndims(M))), L, M, true)
 end
 
-function LinearAlgebra.mul!(x_temp::CuArray{T}, A::DerivCombination, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+function _comb_mul!(x_temp::CuArray{T}, A::DerivCombination, M::CuArray{T}) where {T <: FT}
     nd = ndims(M)
     if nd == 1
         for (k, L) in enumerate(A.ops)
@@ -226,8 +235,8 @@ function LinearAlgebra.mul!(x_temp::CuArray{T}, A::DerivCombination, M::CuArray{
     return x_temp
 end
 
-function Base.:*(A::DerivCombination, M::CuArray{T}) where {T <: Union{Float32, Float64}}
-    x = A.ops[1] * M
+function _comb_times(A::DerivCombination, M::CuArray{T}) where {T <: FT}
+    x = _padded_times(A.ops[1], M)
     for L in A.ops[2:end]
         N = _axis(L)
         sz = ntuple(b -> b == N ? size(M, b) - 2 : size(M, b), ndims(M))
@@ -235,6 +244,19 @@ function Base.:*(A::DerivCombination, M::CuArray{T}) where {T <: Union{Float32, 
         _padded!(x, L, M, false)
     end
     return x
+end
+
+for CA in (:CuVecOrMat, :CuArray)
+    @eval begin
+        LinearAlgebra.mul!(x_temp::$CA{T}, L::DerivativeOperator{T, N}, M::$CA{T};
+                           overwrite = true) where {T <: FT, N} = _padded!(x_temp, L, M, overwrite)
+        Base.:*(L::DerivativeOperator{T, N}, M::$CA{T}) where {T <: FT, N} = _padded_times(L, M)
+        Base.:*(A::DerivCombination, M::$CA{T}) where {T <: FT} = _comb_times(A, M)
+    end
+end
+for Nd in 1:3
+    @eval LinearAlgebra.mul!(x_temp::CuArray{T, $Nd}, A::DerivCombination, M::CuArray{T, $Nd}) where {T <: FT} =
+        _comb_mul!(x_temp, A, M)
 end
 
 # ---- ChainRulesCore.rrule: pullback = adjoint kernel ------------------------
@@ -270,12 +292,16 @@ function solve_plan_for(A::GhostDerivativeOperator, sz::Dims, ::Type{T}) where {
     end
 end
 
-function Base.:\(A::GhostDerivativeOperator, u::CuArray{T}) where {T <: Union{Float32, Float64}}
+function _ghost_ldiv(A::GhostDerivativeOperator, u::CuArray{T}) where {T <: FT}
     x = similar(u)
     check(ccall((:deo_solve_apply, libdeo), Cint, (Ptr{Cvoid}, CuPtr{T}, CuPtr{T}, Ptr{Cvoid}),
                 solve_plan_for(A, size(u), T), u, x, _stream()))
     return x
 end
+# the reference defines \ for AbstractVector, AbstractMatrix and AbstractArray
+Base.:\(A::GhostDerivativeOperator, u::CuVector{T}) where {T <: FT} = _ghost_ldiv(A, u)
+Base.:\(A::GhostDerivativeOperator, u::CuMatrix{T}) where {T <: FT} = _ghost_ldiv(A, u)
+Base.:\(A::GhostDerivativeOperator, u::CuArray{T}) where {T <: FT} = _ghost_ldiv(A, u)
 
 # ---- vector calculus (vector_calculus_operators.jl, vector_calculus_convolutions.jl) ----
 const VC_PLANS = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
@@ -303,19 +329,25 @@ function _vc_apply!(x_temp::CuArray{T}, A::DeoVC, M::CuArray{T}, overwrite) wher
     return x_temp
 end
 
-# mul! accumulates, as the reference's methods do
+# mul! accumulates, as the reference's methods do; the 2-D and 3-D methods
+# shadow the reference's own dimension-specific ones
 LinearAlgebra.mul!(x_temp::CuArray{T}, has_vector::Bool, A::Union{GradientOperator, DivergenceOperator},
-                   M::CuArray{T}; overwrite = false) where {T <: Union{Float32, Float64}} = _vc_apply!(x_temp, A, M, 0)
+                   M::CuArray{T}; overwrite = false) where {T <: FT} = _vc_apply!(x_temp, A, M, 0)
+for MT in (2, 3)
+    @eval LinearAlgebra.mul!(x_temp::CuArray{T}, has_vector::Bool,
+                             A::Union{GradientOperator{T, $MT}, DivergenceOperator{T, $MT}},
+                             M::CuArray{T}; overwrite = false) where {T <: FT} = _vc_apply!(x_temp, A, M, 0)
+end
 LinearAlgebra.mul!(x_temp::CuArray{T, 4}, A::CurlOperator, M::CuArray{T, 4};
-                   overwrite = false) where {T <: Union{Float32, Float64}} = _vc_apply!(x_temp, A, M, 0)
+                   overwrite = false) where {T <: FT} = _vc_apply!(x_temp, A, M, 0)
 
-function Base.:*(A::GradientOperator, M::CuArray{T, N}) where {T <: Union{Float32, Float64}, N}
+function Base.:*(A::GradientOperator{T}, M::CuArray{T, N}) where {T <: FT, N}
     _vc_apply!(CuArray{T}(undef, (size(M) .- 2)..., N), A, M, 1)
 end
-function Base.:*(A::DivergenceOperator, M::CuArray{T}) where {T <: Union{Float32, Float64}}
+function Base.:*(A::DivergenceOperator{T}, M::CuArray{T, N}) where {T <: FT, N}
     _vc_apply!(CuArray{T}(undef, (size(M)[1:(end - 1)] .- 2)...), A, M, 1)
 end
-function Base.:*(A::CurlOperator, M::CuArray{T, 4}) where {T <: Union{Float32, Float64}}
+function Base.:*(A::CurlOperator{T}, M::CuArray{T, 4}) where {T <: FT}
     _vc_apply!(CuArray{T}(undef, (size(M)[1:3] .- 2)..., 3), A, M, 1)
 end
 
