@@ -16,6 +16,7 @@ where it was built.  The same C ABI is exercised from Python (deo/_lib.py).
 module DeoGB300
 
 using LinearAlgebra
+using Libdl
 using CUDA
 using DiffEqOperators
 using DiffEqOperators: DerivativeOperator, GhostDerivativeOperator, DiffEqOperatorCombination,
@@ -112,12 +113,35 @@ _bc_for(Q::ComposedMultiDimBC, ax) = first(Q.BCs[ax])
 _ghosts(A::GhostDerivativeOperator) = (A,)
 _ghosts(A::DiffEqOperatorCombination) = Tuple(op for op in A.ops)
 
-# ---- plans (cached per operator object, size and element type) --------------
+# Device plans hold the operators' coefficients.  update_coefficients!
+# (abstract_operator_functions.jl:190-194) lets a coeff_func rewrite
+# L.coefficients in place, so every cache key below carries the coefficient
+# values: a changed vector builds a new plan instead of reusing a stale one.
+_coeff_key(L::DerivativeOperator) = hash(L.coefficients)
+_coeff_key(A::GhostDerivativeOperator) = _coeff_key(A.L)
+_coeff_key(A::DiffEqOperatorCombination) = hash(map(_coeff_key, A.ops))
+
+# The plan of `cache` for (shape key, coefficient key); plans built for earlier
+# coefficient values of the same shape are destroyed (`destroy`, a libdeo
+# *_destroy symbol) so that a coeff_func updated every step does not pile up plans.
+function _cached!(make, cache::Dict, shape_key, ckey, destroy::Symbol)
+    k = (shape_key, ckey)
+    haskey(cache, k) && return cache[k]
+    for kk in collect(keys(cache))
+        if kk[1] == shape_key
+            h = pop!(cache, kk)
+            ccall(Libdl.dlsym(Libdl.dlopen(libdeo), destroy), Cvoid, (Ptr{Cvoid},), h)
+        end
+    end
+    return cache[k] = make()
+end
+
+# ---- plans (cached per operator object, size, element type and coefficients) -
 const PLANS = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
 
 function plan_for(A, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
     cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), PLANS, A)
-    get!(cache, (sz, T)) do
+    _cached!(cache, (sz, T), _coeff_key(A), :deo_plan_destroy) do
         gs = _ghosts(A)
         ops = [deo_operator(g.L) for g in gs]
         bcs = [deo_bc(_bc_for(g.Q, _axis(g.L))) for g in gs]
@@ -181,7 +205,7 @@ const PADDED = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
 function padded_plan_for(L::DerivativeOperator, osz::Dims, isz::Dims, ::Type{T},
                          starts) where {T <: Union{Float32, Float64}}
     cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), PADDED, L)
-    get!(cache, (osz, isz, T, starts)) do
+    _cached!(cache, (osz, isz, T, starts), _coeff_key(L), :deo_padded_destroy) do
         op = deo_operator(L)
         o, i = Int64[osz...], Int64[isz...]
         h = Ref{Ptr{Cvoid}}(C_NULL)
@@ -279,7 +303,7 @@ const SOLVES = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
 
 function solve_plan_for(A::GhostDerivativeOperator, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
     cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), SOLVES, A)
-    get!(cache, (sz, T)) do
+    _cached!(cache, (sz, T), _coeff_key(A), :deo_solve_destroy) do
         op = deo_operator(A.L)
         bc = Ref(deo_bc(_bc_for(A.Q, _axis(A.L))))
         sizes = Int64[sz...]
@@ -312,7 +336,7 @@ const DeoVC = Union{GradientOperator, DivergenceOperator, CurlOperator}
 
 function vc_plan_for(A::DeoVC, ::Type{T}) where {T <: Union{Float32, Float64}}
     cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), VC_PLANS, A)
-    get!(cache, T) do
+    _cached!(cache, T, hash(map(_coeff_key, vec(A.ops))), :deo_vector_calculus_destroy) do
         ops = [deo_operator(L) for L in vec(A.ops)]
         h = Ref{Ptr{Cvoid}}(C_NULL)
         GC.@preserve ops check(ccall((:deo_vector_calculus_plan, libdeo), Cint,

@@ -174,6 +174,7 @@ typedef struct {
 
 deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
                            deo_plan** out);
+/* Frees the plan's device tables, streams and events (cudaFree waits for the device). */
 void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
