@@ -207,6 +207,9 @@ class DerivativeOperator:
     def __neg__(self):
         return (-1.0) * self
 
+    def __call__(self, *args):
+        return _ode_call(self, args)
+
     def array(self, N: int | None = None) -> np.ndarray:
         """Array(L): len x (len+2) (concretization.jl:8-52, :556-671)."""
         M = np.zeros((self.len, self.len + 2), order="F")
@@ -223,6 +226,17 @@ class DerivativeOperator:
         data = np.zeros((lo.value + up.value + 1, self.len + 2), order="F")
         check(L.lib().deo_operator_banded(self._h, C.byref(lo), C.byref(up), data.ctypes.data_as(_dp)))
         return data, (lo.value, up.value)
+
+
+def _ode_call(A, args):
+    """(A)(u, p, t) = A*u and (A)(du, u, p, t) = mul!(du, A, u), the (u,p,t)
+    interface of DiffEqOperators.jl:67-76 and abstract_operator_functions.jl:197-198
+    (update_coefficients! changes nothing for these types there)."""
+    if len(args) == 3:
+        return A * args[0]
+    if len(args) == 4:
+        return mul_(args[0], A, args[1])
+    raise TypeError("call as A(u, p, t) or A(du, u, p, t)")
 
 
 class DimensionMismatch(DeoShapeError):
@@ -520,6 +534,9 @@ class GhostDerivativeOperator:
     def __mul__(self, u):
         return _apply_terms(self.terms(), u)
 
+    def __call__(self, *args):
+        return _ode_call(self, args)
+
     def size(self):
         return (self.L.len, self.L.len)
 
@@ -628,6 +645,9 @@ class DiffEqOperatorCombination:
 
     def terms(self):
         return self.ops
+
+    def __call__(self, *args):
+        return _ode_call(self, args)
 
 
 # ---------------------------------------------------------------------------

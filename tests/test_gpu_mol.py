@@ -67,3 +67,23 @@ def test_heat_equation_sine_decay(cuda):
     u = deo.autodiff.ssprk3_solve(A, _dev(ua(knots, 0.0)), t1 / steps, steps).cpu().numpy()
     ref = ua(knots, t1)
     assert np.linalg.norm(u - ref) <= 1e-3 * max(np.linalg.norm(u), np.linalg.norm(ref))
+
+
+def test_ode_call_interface(cuda):
+    """(A)(u, p, t) = A*u and (A)(du, u, p, t) = mul!(du, A, u) (DiffEqOperators.jl:67-76)
+    for L*Q, sums of them, and a DerivativeOperator on a padded vector."""
+    import torch
+    rng = np.random.default_rng(8)
+    h = 0.01
+    L = deo.CenteredDifference(2, 4, h, 64)
+    A = L * deo.RobinBC((1.0, 0.5, 0.2), (1.0, 0.5, -0.1), h, 1)
+    B = A + deo.UpwindDifference(1, 2, h, 64, -0.7) * deo.Dirichlet0BC(np.float64)
+    u = _dev(rng.standard_normal(64))
+    for op in (A, B):
+        ref = (op * u).cpu().numpy()
+        assert np.array_equal(op(u, None, 0.0).cpu().numpy(), ref)
+        du = torch.empty_like(u)
+        op(du, u, None, 0.0)
+        assert np.array_equal(du.cpu().numpy(), ref)
+    M = _dev(rng.standard_normal(66))
+    assert np.array_equal(L(M, None, 0.0).cpu().numpy(), (L * M).cpu().numpy())
