@@ -119,6 +119,8 @@ class DerivativeOperator:
         self._h = C.c_void_p(handle)
         self.axis = int(axis)
         self._desc = L.OperatorDesc()
+        self.coeff_func = None  # a 4-argument function (coefficients, u, p, t) set by `f * L`
+        self._version = 0       # bumped when update_coefficients rewrites the coefficients
         self._refresh()
 
     def _refresh(self):
@@ -179,11 +181,22 @@ class DerivativeOperator:
     def copy(self) -> "DerivativeOperator":
         h = C.c_void_p()
         check(L.lib().deo_operator_clone(self._h, C.byref(h)))
-        return DerivativeOperator(h.value, self.axis)
+        out = DerivativeOperator(h.value, self.axis)
+        out.coeff_func = self.coeff_func  # c * L keeps A.coeff_func (derivative_operator_functions.jl:165-197)
+        return out
 
     # algebra ------------------------------------------------------------
     def __rmul__(self, c):
-        """c * L scales the coefficients (derivative_operator_functions.jl:165-197)."""
+        """c * L scales the coefficients (derivative_operator_functions.jl:165-197);
+        f * L for a function f keeps them and stores f as the coefficient function
+        that update_coefficients calls (abstract_operator_functions.jl:174-194)."""
+        if callable(c) and not isinstance(c, (numbers.Number, np.ndarray)):
+            out = self.copy()
+            cv = self.coefficients
+            check(L.lib().deo_operator_set_coefficients(out._h, _ptr(cv), cv.size, 0))
+            out._refresh()
+            out.coeff_func = c
+            return out
         if isinstance(c, numbers.Number) or (isinstance(c, np.ndarray) and c.ndim <= 1):
             cv = _f64(c)
             if cv.size not in (1, self.len):
@@ -208,7 +221,21 @@ class DerivativeOperator:
         return (-1.0) * self
 
     def __call__(self, *args):
-        return _ode_call(self, args)
+        return _ode_call(self, args, update=False)
+
+    def update_coefficients(self, u, p, t):
+        """update_coefficients!(L, u, p, t) (abstract_operator_functions.jl:190-194):
+        coeff_func(coefficients, u, p, t) rewrites the coefficient vector in place."""
+        if self.coeff_func is None:
+            return
+        cv = self.coefficients
+        self.coeff_func(cv, u, p, t)
+        cv = _f64(cv)
+        if cv.size != self.len:
+            raise DimensionMismatch(f"the coefficient function left {cv.size} coefficients, len is {self.len}")
+        check(L.lib().deo_operator_set_coefficients(self._h, _ptr(cv), cv.size, 0))
+        self._refresh()
+        self._version += 1
 
     def array(self, N: int | None = None) -> np.ndarray:
         """Array(L): len x (len+2) (concretization.jl:8-52, :556-671)."""
@@ -228,10 +255,13 @@ class DerivativeOperator:
         return data, (lo.value, up.value)
 
 
-def _ode_call(A, args):
+def _ode_call(A, args, update: bool):
     """(A)(u, p, t) = A*u and (A)(du, u, p, t) = mul!(du, A, u), the (u,p,t)
-    interface of DiffEqOperators.jl:67-76 and abstract_operator_functions.jl:197-198
-    (update_coefficients! changes nothing for these types there)."""
+    interface: L*Q terms and their sums first run update_coefficients
+    (DiffEqOperators.jl:67-76), a bare DerivativeOperator does not
+    (abstract_operator_functions.jl:197-198)."""
+    if update and len(args) in (3, 4):
+        A.update_coefficients(*args[-3:])
     if len(args) == 3:
         return A * args[0]
     if len(args) == 4:
@@ -535,7 +565,18 @@ class GhostDerivativeOperator:
         return _apply_terms(self.terms(), u)
 
     def __call__(self, *args):
-        return _ode_call(self, args)
+        return _ode_call(self, args, update=True)
+
+    def update_coefficients(self, u, p, t):
+        """update_coefficients!(A::GhostDerivativeOperator, u, p, t) (ghost_derivative_operator.jl:61-63)."""
+        self.L.update_coefficients(u, p, t)
+
+    def __rmul__(self, c):
+        """c * (L*Q) = (c*L)*Q for a number, a vector or a function (ghost_derivative_operator.jl:66-76)."""
+        out = c * self.L
+        if out is NotImplemented:
+            return NotImplemented
+        return GhostDerivativeOperator(out, self.Q, self.field)
 
     def size(self):
         return (self.L.len, self.L.len)
@@ -595,10 +636,10 @@ _solve_cache: dict = {}
 def solve_plan_for(A: "GhostDerivativeOperator", shape, dtype_code: int) -> SolvePlan:
     key = (id(A), tuple(shape), dtype_code)
     hit = _solve_cache.get(key)
-    if hit is not None and hit[0] is A:
+    if hit is not None and hit[0] is A and hit[2] == A.L._version:
         return hit[1]
     p = SolvePlan(A, shape, dtype_code)
-    _solve_cache[key] = (A, p)
+    _solve_cache[key] = (A, p, A.L._version)
     return p
 
 
@@ -647,7 +688,13 @@ class DiffEqOperatorCombination:
         return self.ops
 
     def __call__(self, *args):
-        return _ode_call(self, args)
+        return _ode_call(self, args, update=True)
+
+    def update_coefficients(self, u, p, t):
+        for op in self.ops:
+            upd = getattr(op, "update_coefficients", None)
+            if upd is not None:
+                upd(u, p, t)
 
 
 # ---------------------------------------------------------------------------
@@ -802,9 +849,11 @@ _plan_cache: dict = {}
 def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO) -> Plan:
     key = (tuple(id(g) for g in ghosts), tuple(shape), dtype_code, path,
            tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts))
+    versions = tuple(g.L._version for g in ghosts)
     p = _plan_cache.get(key)
-    if p is None:
+    if p is None or p._versions != versions:  # a plan of earlier coefficient values is replaced
         p = Plan(ghosts, shape, dtype_code, path)
+        p._versions = versions
         # keep the ghosts alive with the plan so ids stay unique
         p._ghosts = list(ghosts)
         _plan_cache[key] = p
@@ -892,8 +941,9 @@ def _mul_padded(op: DerivativeOperator, M, out=None, overwrite: bool = True):
             raise DeoShapeError(1, "x_temp must have M's number of dimensions and dtype")
     key = (id(op), tuple(out.shape), tuple(M.shape), _dtype_code(M))
     hit = _padded_cache.get(key)
-    if hit is None or hit[0] is not op:
-        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M)))
+    if hit is None or hit[0] is not op or hit[2] != op._version:
+        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M)),
+                                    op._version)
     check(L.lib().deo_padded_apply(hit[1]._h, C.c_void_p(M.data_ptr()), C.c_void_p(out.data_ptr()),
                                    1 if overwrite else 0, _stream_ptr()))
     return out
@@ -904,8 +954,9 @@ def _padded_view_apply(op: DerivativeOperator, M, out, starts, overwrite: bool):
     `starts` (0 along op's axis) and out's size along the other axes."""
     key = ("view", id(op), tuple(out.shape), tuple(M.shape), tuple(starts), _dtype_code(M))
     hit = _padded_cache.get(key)
-    if hit is None or hit[0] is not op:
-        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M), starts))
+    if hit is None or hit[0] is not op or hit[2] != op._version:
+        hit = _padded_cache[key] = (op, PaddedPlan(op, tuple(out.shape), tuple(M.shape), _dtype_code(M), starts),
+                                    op._version)
     check(L.lib().deo_padded_apply(hit[1]._h, C.c_void_p(M.data_ptr()), C.c_void_p(out.data_ptr()),
                                    1 if overwrite else 0, _stream_ptr()))
     return out

@@ -191,8 +191,10 @@ end
 LinearAlgebra.mul!(du::CuArray{T}, A::GhostCombination, u::CuArray{T}; overwrite = true) where {T <: FT} =
     _ghost_mul!(du, A, u, overwrite)
 
-# (L)(du, u, p, t) right-hand-side interface (DiffEqOperators.jl:67-76)
-(A::GhostDerivativeOperator)(du::CuArray, u::CuArray, p, t) = mul!(du, A, u)
+# The (L)(du, u, p, t) right-hand-side interface needs no method here: the
+# reference's own (DiffEqOperators.jl:67-76) runs update_coefficients! and then
+# mul!, which dispatches to the CuArray methods above; the plan caches are keyed
+# on the coefficient values, so updated coefficients reach the device.
 
 # ---- L*M and mul!(x_temp, L, M) on an already padded array -------------------
 # (derivative_operator_functions.jl:17-69, 150-163; convolutions.jl:17-22), and

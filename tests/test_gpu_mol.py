@@ -87,3 +87,26 @@ def test_ode_call_interface(cuda):
         assert np.array_equal(du.cpu().numpy(), ref)
     M = _dev(rng.standard_normal(66))
     assert np.array_equal(L(M, None, 0.0).cpu().numpy(), (L * M).cpu().numpy())
+
+
+def test_time_dependent_coefficients(cuda):
+    """(A)(du, u, p, t) runs update_coefficients! before the apply
+    (DiffEqOperators.jl:67-76): with coeff_func(c, u, p, t) = (c .= 1 + t) the
+    applies at t = 0 and t = 1 use coefficients 1 and 2, and a cached device
+    plan never serves the old values."""
+    import oracle as O
+    import torch
+    rng = np.random.default_rng(9)
+    h = 0.02
+    f = lambda c, u, p, t: c.__setitem__(slice(None), 1.0 + t)
+    A = (f * deo.UpwindDifference(1, 2, h, 48, 1.0)) * deo.RobinBC((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), h, 1)
+    u_np = rng.standard_normal(48)
+    u = _dev(u_np)
+    du = torch.empty_like(u)
+    q = O.robin((1.0, 0.5, 0.0), (1.0, 0.5, 0.0), h, 1)
+    for t in (0.0, 1.0, 0.0):
+        A(du, u, None, t)
+        Lo = O.upwind(1, 2, h, 48, np.full(48, 1.0 + t))
+        ref = O.apply([(Lo, q)], u_np)
+        tol = 4 * np.spacing(O.abs_scale([(Lo, q)], u_np))
+        assert (np.abs(du.cpu().numpy() - ref) <= tol).all(), t

@@ -82,3 +82,40 @@ def test_second_order_periodic_check():
     # the library's concretisation of L*Q gives the same periodic matrices
     AL, Ab = (deo.CenteredDifference(2, 2, h, N) * deo.PeriodicBC(np.float64)).array()
     assert _approx(AL, M) and not Ab.any()
+
+
+def _copy_u(c, u, p, t):
+    c[:] = u  # the reference's coeff_func(du, u, p, t) = (du .= u)
+
+
+def test_coefficient_functions_and_updates():
+    # f * L keeps the coefficients and stores f (abstract_operator_functions.jl:174-186);
+    # update_coefficients!(L, u, p, t) calls f(L.coefficients, u, p, t) (:190-194), also
+    # through L*Q and sums (ghost_derivative_operator.jl:61-76); c * L keeps f
+    # (derivative_operator_functions.jl:165-197).  The bc_coeff_compositions.jl:52-70 pattern.
+    rng = np.random.default_rng(12)
+    N = 20
+    Q = deo.RobinBC((0.3, 0.6, 0.1), (0.2, 0.4, 0.7), 0.05)
+    L = deo.CenteredDifference(4, 4, 0.05, N)
+    L1 = deo.UpwindDifference(1, 1, 0.05, N, 1.0)
+    for op in (L, L1):
+        cL = _copy_u * op
+        assert np.array_equal(cL.coefficients, op.coefficients) and cL.coeff_func is _copy_u
+        coeffs = rng.random(N)
+        v0 = cL._version
+        cL.update_coefficients(coeffs, None, 0.0)
+        assert np.array_equal(cL.coefficients, coeffs) and cL._version == v0 + 1
+        cA = cL * Q
+        coeffs = rng.random(N)
+        cA.update_coefficients(coeffs, None, 0.0)
+        assert np.array_equal(cA.L.coefficients, coeffs)
+        assert (2.0 * cL).coeff_func is _copy_u
+    A = L * Q
+    c2A = _copy_u * A
+    coeffs = rng.random(N)
+    (c2A + L1 * Q).update_coefficients(coeffs, None, 0.0)
+    assert np.array_equal(c2A.L.coefficients, coeffs)
+    # an operator without a coefficient function is left as it is
+    before = L.coefficients
+    L.update_coefficients(coeffs, None, 0.0)
+    assert np.array_equal(L.coefficients, before)
