@@ -552,6 +552,8 @@ def with_field(op: DerivativeOperator, field) -> FieldCoefficient:
 class GhostDerivativeOperator:
     """L*Q (ghost_derivative_operator.jl:1-37)."""
 
+    __array_ufunc__ = None  # `c * (L*Q)` with a numpy vector c goes to __rmul__
+
     def __init__(self, Lop: DerivativeOperator, Q, field=None):
         self.L, self.Q, self.field = Lop, Q, field
 

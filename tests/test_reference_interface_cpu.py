@@ -119,3 +119,18 @@ def test_coefficient_functions_and_updates():
     before = L.coefficients
     L.update_coefficients(coeffs, None, 0.0)
     assert np.array_equal(L.coefficients, before)
+
+
+def test_coefficients_times_ghost_operator():
+    # c * (L*Q) = (c*L)*Q for a number and a vector (ghost_derivative_operator.jl:66-72)
+    rng = np.random.default_rng(13)
+    L = deo.CenteredDifference(2, 2, 0.1, 12)
+    Q = deo.Dirichlet0BC(np.float64)
+    c = rng.random(12)
+    for k in (2.5, c):
+        A = k * (L * Q)
+        assert isinstance(A, deo.GhostDerivativeOperator)
+        assert np.array_equal(A.L.coefficients, (k * L).coefficients)
+        assert np.array_equal(A.array()[0], ((k * L) * Q).array()[0])
+    with pytest.raises(deo.DeoShapeError):
+        np.ones(5) * (L * Q)
