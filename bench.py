@@ -175,6 +175,27 @@ def max_over_ranks(x: float, ws: int) -> float:
     return float(t.item())
 
 
+# FP64 issue rate of this part, measured with a throughput probe on the GPU
+# machine (1216 CTAs x 256 threads, 8 independent DFMA chains per thread, best
+# of 5): 1.68 DFMA per clock per SM.
+FP64_PER_CLK_PER_SM = 1.68
+NUM_SMS = 152
+
+
+def fp64_order_bound(achieved_gbs: float, bytes_per_point: float, fp64_per_point: int = 17,
+                     sm_mhz: float = 2070.0) -> dict:
+    """The FP64 roofline of evaluating every point in the reference's tap order
+    (17 FP64 instructions per point for the 4th-order 3-D Laplacian: 3 x 5 taps
+    + 2 term sums), as algorithmic GB/s, beside the HBM one: `frac` > 1 means
+    the kernel outruns what FP64 arithmetic could reach (the fixed-point
+    interior issues no FP64 instruction for most points)."""
+    pts = FP64_PER_CLK_PER_SM * NUM_SMS * sm_mhz * 1e6 / fp64_per_point
+    gbs = pts * bytes_per_point / 1e9
+    return {"gbs": gbs, "frac": achieved_gbs / gbs, "fp64_per_point": fp64_per_point,
+            "basis": f"{FP64_PER_CLK_PER_SM} FP64 instructions per clock per SM (measured), {NUM_SMS} SMs, "
+                     f"{sm_mhz:.0f} MHz"}
+
+
 def shard(n: int, rank: int, ws: int) -> range:
     """Instances (batched / served workloads) owned by `rank`: a contiguous
     block, sizes differing by at most one.  Ranks run independent replicas of
@@ -330,6 +351,11 @@ def run_ours(args, ws, rank):
                      "step_achieved": step_achieved, "step_frac": step_achieved / hbm},
         "clocks": clk.summary(),
     }
+    if dtype_name == "f64":
+        # the min(HBM, FP64) view: the FP64 bound of evaluating in the reference's tap order
+        fb = fp64_order_bound(achieved, k_bytes / box ** 3)
+        line["roofline"]["fp64_order_bound"] = fb
+        line["roofline"]["frac_of_min_hbm_fp64"] = achieved / min(hbm, fb["gbs"])
     if rank == 0 and not args.no_cpu:
         t_one = cpu_oracle_lap3d(np.asarray(u_host, dtype=np.float64), n, 1, 1)
         reps = int(max(1, min(30, 10.0 // max(t_one, 1e-3))))  # about 10 s of CPU work
