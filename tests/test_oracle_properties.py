@@ -57,13 +57,15 @@ def _case(seed):
 @pytest.mark.parametrize("seed", range(120))
 def test_apply_matches_concretisation(seed):
     rng, op, q, n, const = _case(seed)
-    if not const:
-        pytest.skip("coefficient vectors: the reference's methods and Array(L) read different entries")
     A = op.array()
     x = rng.standard_normal(n + 2)
     y = op.mul_generic(x)
     scale = np.abs(A) @ np.abs(x)
-    assert (np.abs(y - A @ x) <= 64 * np.finfo(float).eps * scale + 1e-300).all()
+    # with a coefficient vector only the generic method's right boundary rows read other entries
+    keep = slice(None) if const else slice(0, n - op.n_high)
+    assert (np.abs(y - A @ x)[keep] <= 64 * np.finfo(float).eps * scale[keep] + 1e-300).all()
+    if not const:
+        return
     u = rng.standard_normal(n)
     QL, Qb = q.array(n)
     got = O.apply([(op, q)], u)
