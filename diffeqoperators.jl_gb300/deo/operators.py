@@ -805,6 +805,8 @@ class Plan:
             raise DeoArgError(2, "dtype does not match the plan")
         if not (u.is_cuda and du.is_cuda):
             raise DeoArgError(2, "device tensors required (use apply_host for host arrays)")
+        if u.device != du.device:
+            raise DeoArgError(2, "u and du must be on one device")
 
     def apply(self, u, du, overwrite: bool = True):
         self._check(u, du)
@@ -939,6 +941,8 @@ def _mul_padded(op: DerivativeOperator, M, out=None, overwrite: bool = True):
         overwrite = True
     else:
         _check_layout(out, "x_temp")
+        if getattr(out, "device", None) != M.device:
+            raise DeoArgError(2, "x_temp must be a CUDA tensor on M's device")
         if out.dim() != nd or out.dtype != M.dtype:
             raise DeoShapeError(1, "x_temp must have M's number of dimensions and dtype")
     key = (id(op), tuple(out.shape), tuple(M.shape), _dtype_code(M))
@@ -990,6 +994,8 @@ def _combination_mul_padded(x_temp, ops, M):
     if it is padded there).  The first operator overwrites, the others add."""
     if x_temp is None:
         raise DeoArgError(2, "mul!(x_temp, A, M) needs x_temp")
+    if not getattr(M, "is_cuda", False) or getattr(x_temp, "device", None) != M.device:
+        raise DeoArgError(2, "M and x_temp must be CUDA tensors on one device")
     _check_layout(M, "M")
     _check_layout(x_temp, "x_temp")
     nd = M.dim()
