@@ -211,3 +211,41 @@ def test_combination_product_sizes_must_match(cuda):
     Md = deo.julia_array((N + 2, N + 2), fill=1.0)
     with pytest.raises(deo.DeoShapeError):
         A * Md  # (N, N+2) + (N+2, N): DimensionMismatch in the reference too
+
+
+@pytest.mark.parametrize("axes,nd", [((1, 2), 2), ((1, 1), 2), ((2, 2), 2), ((2, 1, 2), 2), ((1,), 2),
+                                     ((1, 2, 3), 3), ((1, 1), 3), ((3,), 3), ((2, 3), 3), ((1, 1, 1), 1)])
+def test_library_dispatch_matches_the_oracle(monkeypatch, axes, nd):
+    """The library's choice per operator (M whole, or the view from index 1
+    along the other axes; the first operator overwriting) is the oracle's:
+    both are recorded on the CPU with the applies replaced by recorders."""
+    import deo
+    from deo import operators as ops
+    calls = []
+    monkeypatch.setattr(ops, "_check_layout", lambda x, what="u": None)
+    monkeypatch.setattr(ops, "_mul_padded", lambda op, M, out=None, overwrite=True:
+                        calls.append(("whole", op.axis, overwrite)))
+    monkeypatch.setattr(ops, "_padded_view_apply", lambda op, M, out, starts, overwrite:
+                        calls.append(("view", op.axis, overwrite)))
+
+    class Dev:
+        is_cuda = True
+        device = "cuda:0"
+        dtype = "f64"
+
+        def __init__(self, nd):
+            self.nd = nd
+
+        def dim(self):
+            return self.nd
+
+    lib_ops = [deo.CenteredDifference(2, 2, 0.1, 6, axis=a) for a in axes]
+    ops._combination_mul_padded(Dev(nd), lib_ops, Dev(nd))
+    # the oracle's decision (oracle.mul_combination): a view unless 1-D, or 2-D with the other axis unoperated
+    operated = set(axes)
+    expect = []
+    for k, a in enumerate(axes):
+        others = {b for b in range(1, nd + 1) if b != a}
+        view = nd == 3 or (nd == 2 and bool(others & operated))
+        expect.append(("view" if view else "whole", a, k == 0))
+    assert calls == expect
