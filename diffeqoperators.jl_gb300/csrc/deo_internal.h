@@ -228,6 +228,9 @@ extern "C" int deo_k_band_solve(int n, int kl, int ku, const double* ab, const i
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
                            void* stream);
+// Commits k_batch's module image and launch resources on the current device
+// (one empty launch of each instantiation; *counter is bumped, nothing else).
+extern "C" int deo_k_batch_prepare(unsigned int* counter, void* stream);
 extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items, int64_t n_items,
                            unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
                            void* stream);

@@ -189,6 +189,26 @@ extern "C" int deo_k_num_sms(void) {
     return n;
 }
 
+// Loads the four k_batch instantiations onto the current device and runs each
+// once over an empty work-list (one CTA; it only bumps *counter), so that the
+// module image and the resources a launch of them takes are committed now:
+// with lazy module loading (the CUDA default) that would otherwise happen at
+// their first real launch.
+extern "C" int deo_k_batch_prepare(unsigned int* counter, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, k_batch<double, false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<double, true>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<float, false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<float, true>);
+    if (e != cudaSuccess) return (int)e;
+    k_batch<double, false><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
+    k_batch<double, true><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
+    k_batch<float, false><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
+    k_batch<float, true><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
+    return (int)cudaGetLastError();
+}
+
 extern "C" int deo_k_batch(const InstDev* inst, const WorkItem* items, int64_t n_items, unsigned int* counter,
                            int dtype, int adjoint, int ctas_per_sm, int threads, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);

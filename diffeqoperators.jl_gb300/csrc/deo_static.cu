@@ -5,11 +5,15 @@
 // and work counter.  Some callers cannot do that: a plug-in whose host
 // application owns every device allocation through its own pool and forbids
 // others, or a request handler in a memory-budgeted server that must not grow
-// the device footprint after the request was admitted.  deo_batch_apply_noalloc runs the same persistent
-// batched kernel with that scratch in one file-scope device array of
-// DEO_NOALLOC_SCRATCH_BYTES bytes, which every GPU that loads libdeo holds
-// until the process exits.  The plans and each instance's input and output
-// buffers are still the caller's.
+// the device footprint after the request was admitted.  deo_batch_apply_noalloc
+// runs the same persistent batched kernel with that scratch in one file-scope
+// device array of DEO_NOALLOC_SCRATCH_BYTES bytes.  CUDA loads the module that
+// holds the array (and the one that holds the kernel) lazily, so the array
+// and the kernel's image occupy a device from the first call on it -- a call
+// with n = 0 does only that set-up -- until the process exits.  The plans and
+// each instance's input and output buffers are still the caller's.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -35,14 +39,68 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[DEO_NOALLOC_SCR
 constexpr int kMaxDevices = 64;
 constexpr size_t kCounterBytes = 256;
 std::mutex g_mu;
-void* g_scratch_dev[kMaxDevices];                          // device address of the array, per device
+// Per device: the array's device address and the id of the CUDA context it
+// was looked up in.  After a device reset the primary context is a new one
+// with a new id, so the address is looked up (and the kernel prepared) again.
+struct DevScratch {
+    unsigned long long ctx_id;
+    void* ptr;
+};
+DevScratch g_dev[kMaxDevices];
 alignas(256) unsigned char g_stage[DEO_NOALLOC_SCRATCH_BYTES];  // host image of the block (guarded by g_mu)
+
+// The current context's unique id (cuCtxGetId), through the runtime's driver
+// entry points so that the library needs no link against libcuda; 0 if the
+// driver does not provide it.
+unsigned long long current_ctx_id() {
+    static PFN_cuCtxGetCurrent_v4000 get_cur = nullptr;
+    static PFN_cuCtxGetId_v12000 get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Set-up for the current device, with it current (caller holds g_mu): the
+// array's device address, and every operation a call issues done once (the
+// host-to-device copy, the counter's memset, k_batch's launches over an empty
+// work-list), so that later calls on this device change its footprint no more.
+deo_status prepare(int dev, cudaStream_t st, unsigned char** base) {
+    const unsigned long long id = current_ctx_id();
+    DevScratch& d = g_dev[dev];
+    if (!d.ptr || id == 0 || d.ctx_id != id) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString(e));
+        std::memset(g_stage, 0, kCounterBytes);
+        e = cudaMemcpyAsync(p, g_stage, kCounterBytes, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, kCounterBytes, st);
+        if (e != cudaSuccess) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString(e));
+        const int r = deo_k_batch_prepare(static_cast<unsigned int*>(p), st);
+        if (r) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString((cudaError_t)r));
+        d.ptr = p;
+        d.ctx_id = id;
+    }
+    *base = static_cast<unsigned char*>(d.ptr);
+    return DEO_OK;
+}
 
 }  // namespace
 
 extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, int adjoint, int tile, void* stream) {
     if (n < 0 || (n > 0 && !inst)) return deo_set_error(DEO_ERR_BAD_ARG, "null or negative instance list");
-    if (n == 0) return DEO_OK;
     const int64_t t = tile > 0 ? tile : 8192;
     int dtype = -1;
     int64_t items = 0;
@@ -66,15 +124,11 @@ extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, i
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return deo_set_error(DEO_ERR_CUDA, "cudaGetDevice failed");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_dev[dev]) {
-        // once per device, with that device current: the array's device address
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString(e));
-        g_scratch_dev[dev] = p;
-    }
-    unsigned char* base = static_cast<unsigned char*>(g_scratch_dev[dev]);
+    unsigned char* base = nullptr;
+    const deo_status ps = prepare(dev, st, &base);
+    if (ps != DEO_OK || n == 0) return ps;
     std::memset(g_stage, 0, kCounterBytes);
     deo::InstDev* hi = reinterpret_cast<deo::InstDev*>(g_stage + inst_off);
     deo::WorkItem* hw = reinterpret_cast<deo::WorkItem*>(g_stage + item_off);
@@ -84,9 +138,9 @@ extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, i
         const int64_t np = deo_plan_points(inst[i].plan);
         for (int64_t s = 0; s < np; s += t) hw[m++] = deo::WorkItem{i, (int)std::min<int64_t>(t, np - s), s};
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // From pageable host memory the copy returns once the staging buffer has
-    // been consumed, so g_stage may be reused as soon as the lock is released.
+    // The copy is ordered after earlier work on `stream` by the stream itself.
+    // From pageable host memory CUDA stages the data before cudaMemcpyAsync
+    // returns, so g_stage may be refilled once the lock is released.
     cudaError_t e = cudaMemcpyAsync(base, g_stage, bytes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString(e));
     const int r = deo_k_batch(reinterpret_cast<const deo::InstDev*>(base + inst_off),

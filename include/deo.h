@@ -425,15 +425,20 @@ deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int 
  * that must not grow its device footprint after admitting a request -- this
  * runs the same persistent kernel as
  * deo_batch_run with its instance table, work-list and counter in one static
- * device array of DEO_NOALLOC_SCRATCH_BYTES (1 MiB) that every GPU loading
- * libdeo holds until process exit.  The plans (created earlier, where
- * allocation was possible) and the instances' buffers are the caller's.
- * Limit: 256 + 24*n (rounded up to 256) + 16*ceil(points_i / tile) summed over
- * instances bytes; larger batches return DEO_ERR_UNSUPPORTED.  tile = 0 means
- * 8192 points per work item.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress) and should come before any
- * stream capture.  Each call copies its work-list from host memory, which
- * waits for earlier work on `stream`.  Every call reuses the same array (the
+ * device array of DEO_NOALLOC_SCRATCH_BYTES (1 MiB).  The plans (created
+ * earlier, where allocation was possible) and the instances' buffers are the
+ * caller's.  Limit: 256 + 24*n (rounded up to 256) + 16*ceil(points_i / tile)
+ * summed over instances bytes; larger batches return DEO_ERR_UNSUPPORTED.
+ * tile = 0 means 8192 points per work item.
+ * Footprint: CUDA loads modules lazily, so the array and the kernel's image
+ * take device memory at the FIRST call on a device (it looks up the array's
+ * address with cudaGetSymbolAddress and launches the kernel once over an empty
+ * work-list), not when the library is loaded; they stay until the process
+ * exits.  A call with n = 0 does only this set-up: make it where the footprint
+ * may still grow (before admitting requests), and before any stream capture.
+ * After a device reset the next call repeats the set-up.
+ * Each call copies its work-list from host memory on `stream`; calls on one
+ * stream are ordered by that stream.  Every call reuses the same array (the
  * counter is cleared each time), so calls that overlap on the GPU -- on
  * different streams or host threads -- race and must be serialised by the
  * caller. */

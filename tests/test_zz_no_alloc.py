@@ -6,9 +6,10 @@ admission --
 use this entry point: it keeps the batched kernel's instance table, work-list
 and counter in a static device array instead of cudaMalloc'd buffers.  Its
 results must equal the allocating entry point's (same kernel), call after
-call, since every call reuses and re-clears the same array.  Kept in a file
-collected last so that a failure here stops a `-x` run only after every other
-test has run.
+call, since every call reuses and re-clears the same array; and once the
+set-up call (n = 0) has run on a device, later calls must leave the device's
+free memory unchanged.  Kept in a file collected last so that a failure here
+stops a `-x` run only after every other test has run.
 """
 import ctypes as C
 
@@ -94,3 +95,27 @@ def test_noalloc_rejects_batches_beyond_its_scratch(cuda):
     torch.cuda.synchronize()
     for a, b in zip(outs_new, outs_ref):
         assert torch.equal(a, b)
+
+
+def test_noalloc_calls_leave_free_device_memory_unchanged(cuda):
+    """After the set-up call (n = 0), calls of several sizes, tiles and both
+    directions allocate nothing: the driver's free-memory figure stays put."""
+    import torch
+    plans, us, outs_ref, outs_new, arr, ref = _setup(0)
+    lib = deo.lib()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.deo_batch_apply_noalloc(0, None, 0, 0, stream) == 0, lib.deo_last_error().decode()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for k, (count, tile, adj) in enumerate([(len(plans), 0, 0), (5, 512, 1), (len(plans), 4096, 0), (1, 0, 1)]):
+        st = lib.deo_batch_apply_noalloc(count, arr, adj, tile, stream)
+        assert st == 0, lib.deo_last_error().decode()
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0, f"call {k}: free device memory changed by {free0 - free1} bytes"
+    # the last forward call over every instance still matches the allocating entry point
+    assert lib.deo_batch_apply_noalloc(len(plans), arr, 0, 0, stream) == 0
+    torch.cuda.synchronize()
+    for a, b in zip(outs_new, outs_ref):
+        assert torch.equal(a, b)
+    assert torch.cuda.mem_get_info()[0] == free0
