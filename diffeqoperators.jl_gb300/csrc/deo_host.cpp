@@ -1163,7 +1163,8 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
         if (p->uni.lap && p->use_tma && deo_k_tma_ok(&p->uni, p->dev.dtype, u)) {
             // overlap only pays beside an interior kernel that leaves the FP64 pipe free: the fixed-point
             // kernel (Float64) or any Float32 kernel; the FP64-bound interiors run the shell after them
-            const bool fx = p->dev.dtype == DEO_F64 && p->exact_sums == 1 && p->uni.fx && p->uni.radius <= 3;
+            const bool fx = p->dev.dtype == DEO_F64 && (p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx &&
+                            p->uni.radius <= 3;
             const bool conc = p->concurrent && p->side && p->d_shell && (p->dev.dtype == DEO_F32 || fx);
             const char* k = "";
             const char* k2 = "";
@@ -1220,13 +1221,18 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
         case DEO_OPT_FAST_PATH: p->fast_path = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_TMA: p->use_tma = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_EXACT_SUMS:
-            if (value < 0 || value > 3) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..3", value);
+            if (value < 0 || value > 4) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..4", value);
             p->exact_sums = value;
             return DEO_OK;
         case DEO_OPT_CONCURRENT_SHELL: p->concurrent = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_FX_FP64_ROWS:
             if (value < 0 || value > 8) return fail(DEO_ERR_BAD_ARG, "FP64 rows %d not in 0..8", value);
             p->uni.fx_rows = value;
+            return DEO_OK;
+        case DEO_OPT_TEST_WITHHOLD:
+            if (value < 0 || value > 64) return fail(DEO_ERR_BAD_ARG, "withheld plane %d not in 0..64", value);
+            p->uni.test_withhold = value;
+            p->uni.wait_polls = value ? 64u : 0u;
             return DEO_OK;
         case DEO_OPT_LAUNCH_TIMING:
             if (value && !p->ev[0])
@@ -1244,14 +1250,17 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
         case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
+        case DEO_OPT_TEST_WITHHOLD: return p->uni.test_withhold;
         case DEO_OPT_FX_FP64_ROWS:
-            return (p->dev.dtype == DEO_F64 && p->uni.enabled && p->uni.lap && p->exact_sums == 1 && p->uni.fx &&
+            return (p->dev.dtype == DEO_F64 && p->uni.enabled && p->uni.lap &&
+                    (p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx &&
                     p->uni.radius <= 3)
                        ? p->uni.fx_rows
                        : 0;
         case DEO_OPT_CONCURRENT_SHELL:
             return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap &&
-                   (p->dev.dtype == DEO_F32 || (p->exact_sums == 1 && p->uni.fx && p->uni.radius <= 3));
+                   (p->dev.dtype == DEO_F32 ||
+                    ((p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx && p->uni.radius <= 3));
     }
     return -1;
 }

@@ -117,6 +117,12 @@ struct UniPlan {
     int fx;
     int fx_f;
     long long fx_w[DEO_MAX_NW];
+    // Bounded waits: mbarrier polls before a wait in a TMA kernel gives up
+    // (0: the default 2^22), and, for the tests of that path only, the index
+    // (>= 1) of the plane (box, for the shell) of each CTA's first unit whose
+    // copy the kernels withhold, so that its wait runs out (0: none).
+    unsigned int wait_polls;
+    int test_withhold;
 };
 
 // Boundary rows of the terms of a Laplacian-type plan (the rows outside each

@@ -178,15 +178,18 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
         bd[0] = G.box[A][0];
         bd[1] = G.box[A][1];
         bd[2] = G.box[A][2];
-        if (threadIdx.x == 0) {
+        // test hook: each CTA's first box copy withheld, so that its wait runs out
+        const bool withheld = U.test_withhold > 0 && blk == (int)blockIdx.x;
+        if (threadIdx.x == 0 && !withheld) {
             mbar_expect_tx(&mbar, (uint32_t)G.box_bytes[A]);
             tma_load_3d(smem, A == 0 ? &m0 : (A == 1 ? &m1 : &m2), &mbar, org[0], org[1], org[2]);
         }
         bool timeout = false;
         {
+            const unsigned int polls = U.wait_polls ? U.wait_polls : (1u << 22);
             uint32_t it = 0;
             while (!mbar_try_wait(&mbar, phase)) {
-                if (++it > (1u << 22)) {
+                if (++it > polls) {
                     timeout = true;
                     break;
                 }
@@ -195,8 +198,9 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
         if (__syncthreads_or(timeout)) {
             if (threadIdx.x == 0) {
                 atomicOr(&g_deo_shell_status, 1u);
-                for (uint32_t it = 0; it < (1u << 22); ++it)  // the copy may still be in flight
-                    if (mbar_try_wait(&mbar, phase)) break;
+                if (!withheld)
+                    for (uint32_t it = 0; it < (1u << 22); ++it)  // the copy may still be in flight
+                        if (mbar_try_wait(&mbar, phase)) break;
             }
             return;
         }

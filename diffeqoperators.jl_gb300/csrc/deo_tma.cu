@@ -536,6 +536,7 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
     const int cc = (ty + H) * C::BX + tx + C::HR;
     // result exponent: A * 2^(E - 1075 - S + fx_f) with |A| = N * 2^-lz, mantissa = N >> 75
     const int ebase0 = 75 - S + U.fx_f;
+    const unsigned int polls = U.wait_polls ? U.wait_polls : (1u << 22);
     if (tid == 0) {
         for (int s = 0; s < F::P; ++s) mbar_init(&mbar[s], 1);
         fence_mbar_init();
@@ -571,6 +572,7 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
         if (tid == 0) {
             const int pre = min(F::P, npl);
             for (int j = 0; j < pre; ++j) {
+                if (base == 0 && U.test_withhold > 0 && j == U.test_withhold) continue;  // test hook
                 const int s = (base + j) & (F::P - 1);
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                 tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
@@ -585,7 +587,7 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
                 const uint32_t par = (uint32_t)((gj / F::P) & 1);
                 uint32_t it = 0;
                 while (!mbar_try_wait(&mbar[gj & (F::P - 1)], par)) {
-                    if (++it > (1u << 22)) {
+                    if (++it > polls) {
                         timeout = true;
                         break;
                     }
@@ -603,7 +605,8 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
                 break;
             }
             // every thread has decomposed plane p: its raw slot takes plane p + P
-            if (tid == 0 && p + F::P < npl) {
+            if (tid == 0 && p + F::P < npl &&
+                !(base == 0 && U.test_withhold > 0 && p + F::P == U.test_withhold)) {
                 const int s = gj & (F::P - 1);
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                 tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + p + F::P);
@@ -689,6 +692,7 @@ __global__ void __launch_bounds__(256) k_lap_fx(const __grid_constant__ CUtensor
         atomicOr(&g_deo_status, 1u);
         // wait (bounded) for this CTA's copies still in flight before its shared memory is released
         for (int j = waited; j < issued; ++j) {
+            if (base == 0 && U.test_withhold > 0 && j == U.test_withhold) continue;  // never issued
             const int gj = base + j;
             const uint32_t par = (uint32_t)((gj / F::P) & 1);
             for (uint32_t it = 0; it < (1u << 22); ++it)
@@ -749,6 +753,7 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * C::TX + tx;
     const int64_t sxy = (int64_t)nx * ny;
     const int c0 = (ty * RY + H) * C::BX + tx + C::HR;  // the first own row's point inside a slot
+    const unsigned int polls = U.wait_polls ? U.wait_polls : (1u << 22);
     T w[NT][K];
 #pragma unroll
     for (int t = 0; t < NT; ++t)
@@ -786,6 +791,7 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
         if (tid == 0) {
             const int pre = min(C::P, npl);
             for (int j = 0; j < pre; ++j) {
+                if (base == 0 && U.test_withhold > 0 && j == U.test_withhold) continue;  // test hook
                 const int s = (base + j) & (C::P - 1);
                 mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
                 tma_load_3d(smem + s * C::SLOT, &tmap, &mbar[s], x0 - C::HR, y0 - H, z0 - HZ + j);
@@ -805,7 +811,7 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
                     const uint32_t par = (uint32_t)((gj / C::P) & 1);
                     uint32_t it = 0;
                     while (!mbar_try_wait(&mbar[gj & (C::P - 1)], par)) {
-                        if (++it > (1u << 22)) {
+                        if (++it > polls) {
                             timeout = true;
                             break;
                         }
@@ -861,7 +867,8 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
                     break;
                 }
                 // every thread is done with plane p - HZ: its slot takes plane p - HZ + P
-                if (tid == 0 && p >= HZ && p - HZ + C::P < npl) {
+                if (tid == 0 && p >= HZ && p - HZ + C::P < npl &&
+                    !(base == 0 && U.test_withhold > 0 && p - HZ + C::P == U.test_withhold)) {
                     const int jn = p - HZ + C::P;
                     const int s = (base + jn) & (C::P - 1);
                     mbar_expect_tx(&mbar[s], C::PLANE_BYTES);
@@ -876,6 +883,7 @@ __global__ void __launch_bounds__(256) k_lap_q(const __grid_constant__ CUtensorM
         atomicOr(&g_deo_status, 1u);
         // wait (bounded) for this CTA's copies still in flight before its shared memory is released
         for (int j = waited; j < issued; ++j) {
+            if (base == 0 && U.test_withhold > 0 && j == U.test_withhold) continue;  // never issued
             const int gj = base + j;
             const uint32_t par = (uint32_t)((gj / C::P) & 1);
             for (uint32_t it = 0; it < (1u << 22); ++it)
@@ -1133,7 +1141,7 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
     if (!up->lap || up->nterms < 2 || up->nterms > 3) return (int)cudaErrorNotSupported;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int H = up->radius, NT = up->nterms;
-    if (dtype == 0 && use_ens == 1 && up->fx) {
+    if (dtype == 0 && (use_ens == 1 || use_ens == 4) && up->fx) {
         if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
@@ -1141,7 +1149,7 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
         if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
     }
-    if (dtype == 0 && (use_ens == 1 || use_ens == 3) && up->ens) {
+    if (dtype == 0 && (use_ens == 1 || use_ens == 3 || use_ens == 4) && up->ens) {
         if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_ens2<1, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
         if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_ens2<2, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
         if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_ens2<3, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");

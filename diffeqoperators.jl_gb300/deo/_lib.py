@@ -20,6 +20,7 @@ DEO_BC_AFFINE, DEO_BC_PERIODIC = 0, 1
 DEO_PATH_AUTO, DEO_PATH_PADDED, DEO_PATH_GENERIC = 0, 1, 2
 DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS, DEO_OPT_LAUNCH_TIMING, DEO_OPT_CONCURRENT_SHELL = 1, 2, 3, 4, 5
 DEO_OPT_FX_FP64_ROWS = 6
+DEO_OPT_TEST_WITHHOLD = 7
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)

@@ -194,6 +194,8 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *         every use (kept for comparison);
  *       3 the same sums from values decomposed once per plane, one int64 ->
  *         double conversion and one FMA per offset;
+ *       4 the per-point fixed-point kernel when the band's weights allow it
+ *         (what 1 picks where no other kernel comes first), else variant 3;
  *       0 the reference's per-term tap order, bit-identical to the generic
  *         kernel.
  *   DEO_OPT_LAUNCH_TIMING: 1 records CUDA events around every kernel launch
@@ -215,6 +217,13 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     use the integer pipes; 0 evaluates every interior point in fixed point.
  *     deo_plan_get_option returns the value when the fixed-point kernel
  *     applies, else 0.
+ *   DEO_OPT_TEST_WITHHOLD: 0 (default) or k in 1..64, for tests of the
+ *     bounded waits only: the TMA kernels (interior and shell) withhold the
+ *     copy of plane k of each CTA's first unit (the shell: each CTA's first
+ *     box) and give up on a wait after 64 polls instead of 2^22, so the wait
+ *     for that copy runs out: the kernel sets its device status bit, waits for
+ *     its other copies in flight and returns, leaving its points unwritten.
+ *     deo_device_status then reports DEO_ERR_TIMEOUT.  Nothing faults.
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
@@ -222,6 +231,7 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
 #define DEO_OPT_LAUNCH_TIMING 4
 #define DEO_OPT_CONCURRENT_SHELL 5
 #define DEO_OPT_FX_FP64_ROWS 6
+#define DEO_OPT_TEST_WITHHOLD 7
 deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);
