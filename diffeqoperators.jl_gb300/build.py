@@ -46,6 +46,7 @@ def _stale(obj: str, src: str) -> bool:
         return True
     deps = [src, os.path.join(CSRC, "deo_internal.h"), os.path.join(CSRC, "deo_eval.cuh"),
             os.path.join(CSRC, "deo_rows.cuh"), os.path.join(CSRC, "deo_ptx.cuh"), os.path.join(CSRC, "deo_fx.cuh"),
+            os.path.join(CSRC, "deo_bfx.cuh"),
             os.path.join(HERE, "..", "include", "deo.h"),
             os.path.abspath(__file__)]
     t = os.path.getmtime(obj)

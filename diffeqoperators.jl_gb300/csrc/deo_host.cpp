@@ -962,6 +962,76 @@ static bool fx_weights(const double* w, int H, int nt, long long* W, int& f) {
     return true;
 }
 
+// Block fixed point (k_lap_bfx, three axes sharing the band w[0..2H]): the
+// weights' exact integer images W[k] on one exponent f (w[k] = W[k] * 2^f),
+// the merged centre 3 W[H], and the centre threshold.  Values carry G0 = 7
+// bits below their 53-bit mantissas; each group of the 3 neighbours at one
+// offset then carries less than 4 units of truncation, so the kernel's error
+// is below (4/3) r 2^(Tc - G0 + 1) ulp of sum|c_k u_k| (r = sum_{k != H} |w_k|
+// / |w_H|) when the centre value is at least 2^-Tc of the plane tile's largest
+// binade; Tc is the largest value keeping that bound at 2 ulp (at most G0, so
+// that the centre itself is exact).  The centre test is |m_0| >= 2^tshift
+// units, tshift = 53 + G0 - 1 - Tc.  The kernel folds each weight's sign into
+// its group sum S (|S| < 3 * 2^60), adds 2^62, splits that at bit 31 and |W|
+// at bit 29, and accumulates the four unsigned 32 x 32-bit partial products
+// in uint64 columns: false when one could overflow, when the band's signs do
+// not alternate from the centre, when a weight is zero or not normal, or when
+// the images need more than 58 bits.
+static bool bfx_weights(const double* w, int H, deo::UniPlan& U) {
+    constexpr int G0 = 7;
+    const int K = 2 * H + 1;
+    long long M[DEO_MAX_NW];
+    int fk[DEO_MAX_NW];
+    int fmin = INT_MAX, fmax = INT_MIN;
+    for (int k = 0; k < K; ++k) {
+        if (std::fpclassify(w[k]) != FP_NORMAL) return false;
+        int ex = 0;
+        const double fr = std::frexp(std::fabs(w[k]), &ex);
+        M[k] = (long long)std::ldexp(fr, 53);
+        fk[k] = ex - 53;
+        fmin = std::min(fmin, fk[k]);
+        fmax = std::max(fmax, fk[k]);
+    }
+    if (53 + (fmax - fmin) > 58) return false;  // 3 W[H] < 2^60 as well
+    long double all = 0.0L;
+    for (int k = 0; k < K; ++k) {
+        U.bfx_w[k] = (w[k] < 0 ? -1 : 1) * (M[k] << (fk[k] - fmin));
+        if (k != H) all += std::fabs((long double)w[k]);
+    }
+    U.bfx_c0 = 3 * U.bfx_w[H];
+    // signs alternating from the centre (every centred even-derivative band)
+    const bool cneg = w[H] < 0;
+    for (int k = 0; k < K; ++k)
+        if ((w[k] < 0) != (cneg != (((k - H) & 1) != 0))) return false;
+    // column bounds: S' = sgn(W) S + 2^62 = s1 2^31 + s0 (|S| < 3 2^60), |W| = w1 2^29 + w0
+    unsigned __int128 c0 = 0, c31 = 0, c29 = 0, c60 = 0, ksum = 0;
+    const unsigned __int128 s0max = (1u << 31) - 1;
+    const unsigned __int128 s1max = (((unsigned __int128)1 << 62) + 3 * ((unsigned __int128)1 << 60)) >> 31;
+    for (int k = 0; k < K; ++k) {
+        const long long W = k == H ? U.bfx_c0 : U.bfx_w[k];
+        const unsigned __int128 aw = (unsigned __int128)(W < 0 ? -W : W);
+        const unsigned __int128 w0 = aw & 0x1FFFFFFFu, w1 = aw >> 29;
+        c0 += s0max * w0;
+        c31 += s1max * w0;
+        c29 += s0max * w1;
+        c60 += s1max * w1;
+        ksum += aw;
+    }
+    const unsigned __int128 lim = ~(unsigned __int128)0 >> 64;  // 2^64 - 1
+    if (c0 > lim || c31 > lim || c29 > lim || c60 > lim) return false;
+    const long double per = (4.0L / 3.0L) * (all / std::fabs((long double)w[H])) * std::ldexp(1.0L, 1 - G0);
+    int Tc = G0;
+    while (Tc >= 0 && per * std::ldexp(1.0L, Tc) > 2.0L) --Tc;
+    if (Tc < 0) return false;
+    const unsigned __int128 kk = ksum << 62;
+    U.bfx_k_lo = (unsigned long long)kk;
+    U.bfx_k_hi = (unsigned long long)(kk >> 64);
+    U.bfx_cneg = cneg ? 1 : 0;
+    U.bfx_f = fmin;
+    U.bfx_tshift = 53 + G0 - 1 - Tc;
+    return true;
+}
+
 extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms,
                                       const deo_term* terms, deo_plan** out) {
     if (!out || !sizes || !terms) return fail(DEO_ERR_BAD_ARG, "null argument");
@@ -1109,6 +1179,11 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
                 U.fx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
             if (U.fx) U.fx = fx_weights(U.t[0].w, H, nterms, U.fx_w, U.fx_f);
             U.fx_rows = kFxFp64Rows;
+            // block fixed point: three axes sharing one band
+            U.bfx = U.lap && dtype == DEO_F64 && H <= 3 && nterms == 3;
+            for (int t = 0; t < nterms && U.bfx; ++t)
+                U.bfx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
+            if (U.bfx) U.bfx = bfx_weights(U.t[0].w, H, U);
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
         } else {
             U.enabled = 0;
@@ -1163,7 +1238,9 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
         if (p->uni.lap && p->use_tma && deo_k_tma_ok(&p->uni, p->dev.dtype, u)) {
             // overlap only pays beside an interior kernel that leaves the FP64 pipe free: the fixed-point
             // kernel (Float64) or any Float32 kernel; the FP64-bound interiors run the shell after them
-            const bool fx = p->dev.dtype == DEO_F64 && (p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx &&
+            const bool fx = p->dev.dtype == DEO_F64 &&
+                            ((p->exact_sums == 5 && (p->uni.fx || p->uni.bfx)) ||
+                             ((p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx)) &&
                             p->uni.radius <= 3;
             const bool conc = p->concurrent && p->side && p->d_shell && (p->dev.dtype == DEO_F32 || fx);
             const char* k = "";
@@ -1221,7 +1298,7 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
         case DEO_OPT_FAST_PATH: p->fast_path = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_TMA: p->use_tma = value ? 1 : 0; return DEO_OK;
         case DEO_OPT_EXACT_SUMS:
-            if (value < 0 || value > 4) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..4", value);
+            if (value < 0 || value > 5) return fail(DEO_ERR_BAD_ARG, "exact-sums variant %d not in 0..5", value);
             p->exact_sums = value;
             return DEO_OK;
         case DEO_OPT_CONCURRENT_SHELL: p->concurrent = value ? 1 : 0; return DEO_OK;
@@ -1248,19 +1325,23 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
     switch (option) {
         case DEO_OPT_FAST_PATH: return p->fast_path && p->uni.enabled;
         case DEO_OPT_TMA: return p->use_tma && p->uni.enabled && p->uni.lap;
-        case DEO_OPT_EXACT_SUMS: return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx);
+        case DEO_OPT_EXACT_SUMS:
+            return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx || p->uni.bfx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
         case DEO_OPT_TEST_WITHHOLD: return p->uni.test_withhold;
         case DEO_OPT_FX_FP64_ROWS:
             return (p->dev.dtype == DEO_F64 && p->uni.enabled && p->uni.lap &&
-                    (p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx &&
+                    (p->exact_sums == 1 || p->exact_sums == 4 || (p->exact_sums == 5 && !p->uni.bfx)) &&
+                    p->uni.fx &&
                     p->uni.radius <= 3)
                        ? p->uni.fx_rows
                        : 0;
         case DEO_OPT_CONCURRENT_SHELL:
             return p->concurrent && p->side && p->d_shell && p->uni.enabled && p->uni.lap &&
                    (p->dev.dtype == DEO_F32 ||
-                    ((p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx && p->uni.radius <= 3));
+                    (((p->exact_sums == 5 && (p->uni.fx || p->uni.bfx)) ||
+                      ((p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx)) &&
+                     p->uni.radius <= 3));
     }
     return -1;
 }

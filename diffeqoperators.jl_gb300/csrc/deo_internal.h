@@ -117,6 +117,19 @@ struct UniPlan {
     int fx;
     int fx_f;
     long long fx_w[DEO_MAX_NW];
+    // Block fixed point (Float64, three axes, k_lap_bfx): values aligned once
+    // per plane to one exponent per plane tile.  Band weight at offset k - H =
+    // bfx_w[k] * 2^bfx_f exactly; bfx_c0 = 3 * bfx_w[H] (the merged centre).
+    // A point whose centre has magnitude below 2^bfx_tshift units of its
+    // scale (and whose planes were not all aligned exactly) is evaluated in
+    // the reference's tap order instead (the error bound needs it).
+    int bfx;
+    int bfx_tshift;
+    int bfx_f;
+    int bfx_cneg;  // the centre weight is negative (the band's signs alternate from the centre)
+    long long bfx_c0;
+    long long bfx_w[DEO_MAX_NW];
+    unsigned long long bfx_k_lo, bfx_k_hi;  // 2^62 * (|bfx_c0| + sum_{k != H} |bfx_w[k]|), a 128-bit constant
     // Bounded waits: mbarrier polls before a wait in a TMA kernel gives up
     // (0: the default 2^22), and, for the tests of that path only, the index
     // (>= 1) of the plane (box, for the shell) of each CTA's first unit whose

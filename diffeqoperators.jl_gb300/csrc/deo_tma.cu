@@ -134,6 +134,12 @@ __device__ __forceinline__ int claim_unit(const LapGrid& g, int& s_next, int k_s
     return s_next;
 }
 
+}  // namespace deo
+
+#include "deo_bfx.cuh"
+
+namespace deo {
+
 template <typename T, int H, int NT, bool ENS>
 __global__ void __launch_bounds__(256) k_lap_tma(const __grid_constant__ CUtensorMap tmap,
                                                  const __grid_constant__ UniPlan U, const LapGrid g,
@@ -1125,6 +1131,28 @@ static int launch_fx(const UniPlan* up, unsigned int* sched, const void* u, void
     return (int)cudaGetLastError();
 }
 
+template <int H, bool CNEG>
+static int launch_bfx(const UniPlan* up, unsigned int* sched, const void* u, void* du, int ow, cudaStream_t st) {
+    using C = BfxCfg<H>;
+    CUtensorMap map;
+    if (!make_map(map, u, 8, up->n[0], up->n[1], up->n[2], C::BX, C::BY)) return (int)cudaErrorNotSupported;
+    static int64_t G = 0;
+    if (!G) {
+        const int e = occupancy_grid(k_lap_bfx<H, CNEG>, C::NTHR, C::SMEM, G);
+        if (e) return e;
+    }
+    const LapGrid g = make_grid(up, C::TX, C::TY, H, 3, G);
+    LapGrid g2 = g;
+    g2.sched = sched;
+    if (sched) {
+        const cudaError_t e = cudaMemsetAsync(sched, 0, sizeof(unsigned int), st);
+        if (e != cudaSuccess) return (int)e;
+    }
+    const int grid = (int)std::min<int64_t>(G, g.units);
+    k_lap_bfx<H, CNEG><<<grid, dim3(C::TXT, C::TYT), C::SMEM, st>>>(map, *up, g2, (const double*)u, (double*)du, ow);
+    return (int)cudaGetLastError();
+}
+
 #define DEO_TRY_KERNEL(call, name)                            \
     do {                                                      \
         const int e_ = (call);                                \
@@ -1141,7 +1169,16 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
     if (!up->lap || up->nterms < 2 || up->nterms > 3) return (int)cudaErrorNotSupported;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int H = up->radius, NT = up->nterms;
-    if (dtype == 0 && (use_ens == 1 || use_ens == 4) && up->fx) {
+    if (dtype == 0 && use_ens == 5 && up->bfx && NT == 3) {
+        const bool cn = up->bfx_cneg != 0;
+        if (H == 1) DEO_TRY_KERNEL((cn ? launch_bfx<1, true>(up, sched, u, du, overwrite, st)
+                                       : launch_bfx<1, false>(up, sched, u, du, overwrite, st)), "k_lap_bfx");
+        if (H == 2) DEO_TRY_KERNEL((cn ? launch_bfx<2, true>(up, sched, u, du, overwrite, st)
+                                       : launch_bfx<2, false>(up, sched, u, du, overwrite, st)), "k_lap_bfx");
+        if (H == 3) DEO_TRY_KERNEL((cn ? launch_bfx<3, true>(up, sched, u, du, overwrite, st)
+                                       : launch_bfx<3, false>(up, sched, u, du, overwrite, st)), "k_lap_bfx");
+    }
+    if (dtype == 0 && (use_ens == 1 || use_ens == 4 || use_ens == 5) && up->fx) {
         if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_fx<1, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 3>(up, sched, u, du, overwrite, st)), "k_lap_fx");
@@ -1149,7 +1186,7 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
         if (NT == 2 && H == 2) DEO_TRY_KERNEL((launch_fx<2, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
         if (NT == 2 && H == 3) DEO_TRY_KERNEL((launch_fx<3, 2>(up, sched, u, du, overwrite, st)), "k_lap_fx");
     }
-    if (dtype == 0 && (use_ens == 1 || use_ens == 3 || use_ens == 4) && up->ens) {
+    if (dtype == 0 && (use_ens == 1 || use_ens == 3 || use_ens == 4 || use_ens == 5) && up->ens) {
         if (NT == 3 && H == 1) DEO_TRY_KERNEL((launch_ens2<1, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
         if (NT == 3 && H == 2) DEO_TRY_KERNEL((launch_ens2<2, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");
         if (NT == 3 && H == 3) DEO_TRY_KERNEL((launch_ens2<3, 3>(up, dp, u, du, overwrite, st)), "k_lap_ens2");

@@ -187,15 +187,20 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *   DEO_OPT_EXACT_SUMS: Float64 Laplacian-type plans whose terms share one
  *     band evaluate interior points in integer arithmetic and round once
  *     (result within a few ulp of sum|c_k u_k| of the reference's order):
- *       1 the best variant that applies (default): the fixed-point kernel
- *         (no FP64 instruction per point) when the band's weights allow it,
+ *       1 the best variant that applies (default): the per-point
+ *         fixed-point kernel (variant 4) when the band's weights allow it,
  *         else variant 3;
+ *       5 for three axes the block fixed-point kernel (values aligned once
+ *         per plane to one exponent per plane tile, no FP64 instruction per
+ *         point; points near a zero of u, where that alignment cannot bound
+ *         the error, in the reference's order; as fast as variant 4 at 256^3,
+ *         kept for comparison), else as 1;
  *       2 exact sums of the equal-weight neighbours, decomposing values at
  *         every use (kept for comparison);
  *       3 the same sums from values decomposed once per plane, one int64 ->
  *         double conversion and one FMA per offset;
- *       4 the per-point fixed-point kernel when the band's weights allow it
- *         (what 1 picks where no other kernel comes first), else variant 3;
+ *       4 the per-point fixed-point kernel when the band's weights allow it,
+ *         else variant 3;
  *       0 the reference's per-term tap order, bit-identical to the generic
  *         kernel.
  *   DEO_OPT_LAUNCH_TIMING: 1 records CUDA events around every kernel launch

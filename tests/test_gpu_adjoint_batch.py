@@ -117,7 +117,8 @@ def test_fast_path_bitwise_equals_generic(cuda, case):
     tol = 4 * np.spacing(O.abs_scale(oterms, u))
     outs = {}
     # (fast path, TMA ring, exact neighbour sums)
-    for name, opts in {"tma-ens": (1, 1, 1), "tma-ens-v2": (1, 1, 3), "tma-ens-v1": (1, 1, 2), "tma-fma": (1, 1, 0),
+    for name, opts in {"tma-ens": (1, 1, 1), "tma-bfx": (1, 1, 5), "tma-ens-v2": (1, 1, 3), "tma-ens-v1": (1, 1, 2),
+                       "tma-fma": (1, 1, 0),
                        "queue": (1, 0, 0), "generic": (0, 0, 0)}.items():
         p.set_option(deo.DEO_OPT_FAST_PATH, opts[0])
         p.set_option(deo.DEO_OPT_TMA, opts[1])
@@ -263,8 +264,8 @@ def test_full_size_laplacian_against_oracle(cuda, dtype):
     ud = deo.julia_array((n, n, n), tdt)
     ud.copy_(torch.from_numpy(u).to(tdt))
     report = {}
-    modes = ({"exact-sums": 1, "exact-sums-v2": 3, "exact-sums-v1": 2, "reference-order": 0} if dtype == "f64"
-             else {"default": 1})
+    modes = ({"exact-sums": 1, "block-fixed-point": 5, "exact-sums-v2": 3, "exact-sums-v1": 2, "reference-order": 0}
+             if dtype == "f64" else {"default": 1})
     for name, ens in modes.items():
         plan.set_option(deo.DEO_OPT_EXACT_SUMS, ens)
         du = deo.julia_array((n, n, n), tdt)
@@ -280,6 +281,7 @@ def test_full_size_laplacian_against_oracle(cuda, dtype):
             assert report[name]["max_rel_to_scale"] < 64 * 2.0 ** -24
     if dtype == "f64":
         assert report["kernels"]["exact-sums"][0] == "k_lap_fx"
+        assert report["kernels"]["block-fixed-point"][0] == "k_lap_bfx"
         assert report["kernels"]["exact-sums-v2"][0] == "k_lap_ens2"
     plan.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
     assert deo.device_status() == 0
@@ -326,7 +328,7 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field, rows):
     p = deo.Plan(A.terms(), shape, 0)
     ud = to_device(u)
     got_t, gen_t = deo.julia_array(shape), deo.julia_array(shape)
-    p.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
+    p.set_option(deo.DEO_OPT_EXACT_SUMS, 4)  # the per-point fixed-point kernel
     p.set_option(deo.DEO_OPT_FX_FP64_ROWS, rows)
     assert p.get_option(deo.DEO_OPT_FX_FP64_ROWS) == rows
     p.apply(ud, got_t)
@@ -371,12 +373,14 @@ def test_fixed_point_kernel_against_integer_model(cuda, case, field, rows):
 
 def test_fixed_point_kernel_not_used_for_wide_weight_ratios(cuda):
     """A 6th-order Laplacian (outer weight 1/90 of the centre's scale) fails the
-    kernel's error-bound rule and runs the per-offset exact-sum kernel."""
+    per-point fixed-point kernel's error-bound rule (and the block kernel's
+    weight-width rule): the plan runs the per-offset exact-sum kernel."""
     case = dict(shape=(24, 20, 18), terms=[T("centered", 2, 6, axis=k, h=0.05, bc=("dirichlet0",))
                                            for k in (1, 2, 3)], seed=9)
     A, oterms, u = build(case)
     shape = tuple(case["shape"])
     p = deo.Plan(A.terms(), shape, 0)
+    p.set_option(deo.DEO_OPT_EXACT_SUMS, 4)
     out = deo.julia_array(shape)
     p.apply(to_device(u), out)
     assert p.kernels[0] == "k_lap_ens2"
@@ -397,7 +401,7 @@ def test_launch_timing(cuda):
     p.apply(to_device(u), out)
     assert p.kernels == ("k_apply",) and len(p.launch_times()) == 1
     with pytest.raises(deo.DeoArgError):
-        p.set_option(deo.DEO_OPT_EXACT_SUMS, 7)
+        p.set_option(deo.DEO_OPT_EXACT_SUMS, 6)
 
 
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
