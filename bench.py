@@ -432,6 +432,18 @@ def nonuniform2d_ops(n, field_dev=None):
     return ops, (al, ar, dx)
 
 
+def nonuniform2d_inputs(n, dx):
+    """The coefficient field a(x, y) = cos(2 pi x) sin(2 pi y) on the grid's
+    nodes and u ~ N(0, 1) smoothed by 5 Jacobi passes (seeded), Julia layout."""
+    x = np.cumsum(dx)[:n]  # the grid's nodes
+    a = np.asfortranarray(np.cos(2 * np.pi * x[:, None]) * np.sin(2 * np.pi * x[None, :]))
+    rng = np.random.default_rng(SEED + 3)
+    u = rng.standard_normal((n, n))
+    for _ in range(5):  # Jacobi smoothing
+        u[1:-1, 1:-1] = 0.25 * (u[:-2, 1:-1] + u[2:, 1:-1] + u[1:-1, :-2] + u[1:-1, 2:])
+    return np.asfortranarray(u), a
+
+
 def run_nonuniform2d(args):
     """2048^2 non-uniform grid: centred d1/d2 a6 on both axes + upwind d1 a3
     with the field a(x,y) = cos(2 pi x) sin(2 pi y), GeneralBC; per op and fused."""
@@ -440,15 +452,10 @@ def run_nonuniform2d(args):
     import deo
     n = 2048
     ops, (_, _, dx) = nonuniform2d_ops(n)
-    x = np.cumsum(dx)[:n]  # the grid's nodes
-    a = np.asfortranarray(np.cos(2 * np.pi * x[:, None]) * np.sin(2 * np.pi * x[None, :]))
+    u, a = nonuniform2d_inputs(n, dx)
     fdev = deo.julia_array((n, n)); fdev.copy_(torch.from_numpy(a))
     ops, _ = nonuniform2d_ops(n, fdev)
-    rng = np.random.default_rng(SEED + 3)
-    u = rng.standard_normal((n, n))
-    for _ in range(5):  # Jacobi smoothing
-        u[1:-1, 1:-1] = 0.25 * (u[:-2, 1:-1] + u[2:, 1:-1] + u[1:-1, :-2] + u[1:-1, 2:])
-    ud = deo.julia_array((n, n)); ud.copy_(torch.from_numpy(np.asfortranarray(u)))
+    ud = deo.julia_array((n, n)); ud.copy_(torch.from_numpy(u))
     outs = [deo.julia_array((n, n)) for _ in range(2)]
     res = {"metric": "grid-pts/s (2-D 2048^2 non-uniform)", "workload": "nonuniform2d_2048_f64", "dtype": "f64",
            "per_op": {}}
@@ -469,11 +476,10 @@ def run_nonuniform2d(args):
     return res
 
 
-def batch_instances(count=4096, seed=SEED, scale=1.0):
-    """4096 instances: 70% 1-D (N log-uniform [64, 65536]), 30% 2-D (sides
-    log-uniform [32, 1024]); d in 1..4, a in {2,4,6,8}; uniform or graded grid
-    50/50; Dirichlet or Robin per instance."""
-    import deo
+def batch_specs(count=4096, seed=SEED, scale=1.0):
+    """4096 instance specs (shape, d, a, graded, robin): 70% 1-D (N
+    log-uniform [64, 65536]), 30% 2-D (sides log-uniform [32, 1024]); d in
+    1..4, a in {2,4,6,8}; uniform or graded grid 50/50; Dirichlet or Robin."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
@@ -484,20 +490,38 @@ def batch_instances(count=4096, seed=SEED, scale=1.0):
             shape = (max(16, int(np.exp(rng.uniform(np.log(64), np.log(65536))) * scale)),)
         else:
             shape = tuple(max(16, int(np.exp(rng.uniform(np.log(32), np.log(1024))) * scale)) for _ in range(2))
-        terms = []
-        for ax, n in enumerate(shape):
-            if graded:
-                i = np.arange(n + 1)
-                dx = 1.0 + 0.5 * np.sin(2 * np.pi * i / (n + 1))
-                dx = dx / dx.sum()
-                bc = deo.RobinBC((1.0, 0.5, 0.1), (1.0, 0.5, -0.1), dx, 1) if robin else deo.DirichletBC(0.1, -0.2)
-            else:
-                dx = 1.0 / (n + 1)
-                bc = deo.RobinBC((1.0, 0.5, 0.1), (1.0, 0.5, -0.1), dx, 1) if robin else deo.DirichletBC(0.1, -0.2)
-            L = deo.CenteredDifference(d, a, dx, n, axis=ax + 1)
-            terms.append(L * (bc if len(shape) == 1 else deo.MultiDimDirectionalBC(bc, ax + 1, shape)))
-        out.append((shape, terms))
+        out.append((shape, d, a, graded, robin))
     return out
+
+
+def batch_grid(n, graded):
+    """dx of one axis: uniform 1/(n+1), or graded h(1 + 0.5 sin(2 pi i/(n+1))) normalised to 1."""
+    if not graded:
+        return 1.0 / (n + 1)
+    i = np.arange(n + 1)
+    dx = 1.0 + 0.5 * np.sin(2 * np.pi * i / (n + 1))
+    return dx / dx.sum()
+
+
+ROBIN_L, ROBIN_R, DIRICHLET_LR = (1.0, 0.5, 0.1), (1.0, 0.5, -0.1), (0.1, -0.2)
+
+
+def batch_terms(spec):
+    """The terms (L * Q per axis) of one instance spec."""
+    import deo
+    shape, d, a, graded, robin = spec
+    terms = []
+    for ax, n in enumerate(shape):
+        dx = batch_grid(n, graded)
+        bc = deo.RobinBC(ROBIN_L, ROBIN_R, dx, 1) if robin else deo.DirichletBC(*DIRICHLET_LR)
+        L = deo.CenteredDifference(d, a, dx, n, axis=ax + 1)
+        terms.append(L * (bc if len(shape) == 1 else deo.MultiDimDirectionalBC(bc, ax + 1, shape)))
+    return terms
+
+
+def batch_instances(count=4096, seed=SEED, scale=1.0):
+    """(shape, terms) of the batched workload's instances (batch_specs)."""
+    return [(spec[0], batch_terms(spec)) for spec in batch_specs(count, seed, scale)]
 
 
 def run_batch(args):
