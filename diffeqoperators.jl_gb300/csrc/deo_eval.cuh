@@ -20,9 +20,32 @@ __device__ __forceinline__ float band_w<float>(const RowTabDev& tb, int k) {
     return reinterpret_cast<const float*>(tb.wband)[k];
 }
 
+// The per-line BC record of the line starting at flat index `base`
+// (multi_dim_bc_operators.jl:28-52: the BC at the line's index over the other axes).
+__device__ __forceinline__ const double* line_bc(const TermDev& t, int64_t base) {
+    const int64_t lo = base % t.stride, hi = base / (t.stride * (int64_t)t.len);
+    return t.lbc + (lo + hi * t.stride) * (int64_t)t.lbc_stride;
+}
+
+// Ghosts from one line's own BC record: BCs[I, J] * u[I, :, J], the 1-D ghost
+// fill (a periodic BC wraps around its line, bc_operators.jl:188-193).
 template <typename T>
-__device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ line) {
+__device__ __noinline__ T ghost_line(const TermDev& t, const T* __restrict__ line, int64_t base, bool left) {
     const int64_t s = t.stride;
+    const double* q = line_bc(t, base);
+    if (q[0] != 0.0) return left ? line[(int64_t)(t.len - 1) * s] : line[0];
+    const int m = (int)(left ? q[1] : q[2]);
+    const double* a = q + 5 + (left ? 0 : t.lbc_mw);
+    const int64_t o = left ? 0 : (int64_t)(t.len - m);
+    T d = T(0);
+    for (int j = 0; j < m; ++j) d = (j == 0) ? T(a[0]) * line[o * s] : fma(T(a[j]), line[(o + j) * s], d);
+    return d + T(left ? q[3] : q[4]);
+}
+
+template <typename T>
+__device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ line, int64_t base) {
+    const int64_t s = t.stride;
+    if (t.lbc) return ghost_line<T>(t, line, base, true);
     if (t.bc_kind == 1) return t.periodic_nd ? line[0] : line[(int64_t)(t.len - 1) * s];
     if (t.bc_kind == 2) return line[-s];  // padded input: the ghost is stored before the line
     T d = T(0);
@@ -31,8 +54,9 @@ __device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ 
 }
 
 template <typename T>
-__device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__ line) {
+__device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__ line, int64_t base) {
     const int64_t s = t.stride;
+    if (t.lbc) return ghost_line<T>(t, line, base, false);
     if (t.bc_kind == 1) return t.periodic_nd ? line[(int64_t)(t.len - 1) * s] : line[0];
     if (t.bc_kind == 2) return line[(int64_t)t.len * s];  // padded input: the ghost is stored after the line
     T d = T(0);
@@ -118,8 +142,8 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
         return acc;
     }
     T gl = T(0), gr = T(0);
-    if (r.p0 == 1) gl = ghost_left<T>(t, line);
-    if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line);
+    if (r.p0 == 1) gl = ghost_left<T>(t, line, base);
+    if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line, base);
     auto tap = [&](int k) {
         const int p = r.p0 + k;
         return (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
@@ -189,6 +213,18 @@ __device__ __forceinline__ T adj_term(const TermDev& t, const T* __restrict__ d,
     const int64_t base = idx - (int64_t)(j - 1) * t.stride;
     const int L = t.len;
     T w = adj_column<T>(t, d, base, j + 1);
+    if (t.lbc) {  // this line's own BC
+        const double* q = line_bc(t, base);
+        if (q[0] != 0.0) {  // periodic line: the left ghost is u[len], the right u[1]
+            if (j == L) w += adj_column<T>(t, d, base, 1);
+            if (j == 1) w += adj_column<T>(t, d, base, L + 2);
+        } else {
+            const int ml = (int)q[1], mr = (int)q[2];
+            if (j <= ml) w = fma(T(q[5 + j - 1]), adj_column<T>(t, d, base, 1), w);
+            if (j > L - mr) w = fma(T(q[5 + t.lbc_mw + j - 1 - (L - mr)]), adj_column<T>(t, d, base, L + 2), w);
+        }
+        return w;
+    }
     if (t.bc_kind == 0) {
         if (j <= t.ml) w = fma(T(t.al[j - 1]), adj_column<T>(t, d, base, 1), w);
         if (j > L - t.mr) w = fma(T(t.ar[j - 1 - (L - t.mr)]), adj_column<T>(t, d, base, L + 2), w);

@@ -1057,17 +1057,70 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         if (tm.path < DEO_PATH_AUTO || tm.path > DEO_PATH_GENERIC)
             return fail(DEO_ERR_BAD_ARG, "term %d: unknown path %d", t + 1, tm.path);
         const int mode = tm.path == DEO_PATH_PADDED ? 1 : tm.path == DEO_PATH_GENERIC ? 0 : (ndims == 1 ? 1 : 0);
-        if (!tm.op || !tm.bc) return fail(DEO_ERR_BAD_ARG, "term %d: null operator or boundary condition", t + 1);
+        if (!tm.op || (!tm.bc && !tm.line_bcs))
+            return fail(DEO_ERR_BAD_ARG, "term %d: null operator or boundary condition", t + 1);
         const deo_operator& A = *tm.op;
         const int ax = tm.axis - 1;
         if (ax < 0 || ax >= ndims) return fail(DEO_ERR_BAD_SHAPE, "term %d: axis %d outside 1..%d", t + 1, tm.axis, ndims);
         if (sizes[ax] != A.len)
             return fail(DEO_ERR_BAD_SHAPE, "term %d: size(u, %d) = %lld but the operator has len %d", t + 1, tm.axis,
                         (long long)sizes[ax], A.len);
-        const deo_bc& q = *tm.bc;
-        if (q.kind == DEO_BC_AFFINE && (q.m_l < 0 || q.m_r < 0 || q.m_l > DEO_MAX_BC || q.m_r > DEO_MAX_BC ||
-                                        q.m_l > A.len || q.m_r > A.len))
-            return fail(DEO_ERR_BAD_SHAPE, "term %d: boundary stencil longer than the line", t + 1);
+        auto bad_bc = [&](const deo_bc& b) {
+            if (b.kind != DEO_BC_AFFINE && b.kind != DEO_BC_PERIODIC) return true;
+            return b.kind == DEO_BC_AFFINE && (b.m_l < 0 || b.m_r < 0 || b.m_l > DEO_MAX_BC || b.m_r > DEO_MAX_BC ||
+                                               b.m_l > A.len || b.m_r > A.len);
+        };
+        // one BC per line (MultiDimBC{dim}(BCs::Array)): an array of periodic BCs pads with the edge
+        // planes like PeriodicBC; an array of one affine map is that map on every line; otherwise
+        // every line reads its own ghost map (no fast path)
+        const deo_bc* qp = tm.bc;
+        std::vector<double> lrec;
+        int lmw = 0;
+        if (tm.line_bcs) {
+            const deo_bc* lb = tm.line_bcs;
+            const int64_t nlines = total / A.len;
+            bool all_per = true, all_same = true;
+            auto same_map = [](const deo_bc& a, const deo_bc& b) {
+                if (a.kind != b.kind) return false;
+                if (a.kind == DEO_BC_PERIODIC) return true;
+                if (a.m_l != b.m_l || a.m_r != b.m_r || a.b_l != b.b_l || a.b_r != b.b_r) return false;
+                for (int j = 0; j < a.m_l; ++j) if (a.a_l[j] != b.a_l[j]) return false;
+                for (int j = 0; j < a.m_r; ++j) if (a.a_r[j] != b.a_r[j]) return false;
+                return true;
+            };
+            for (int64_t l = 0; l < nlines; ++l) {
+                if (bad_bc(lb[l]))
+                    return fail(DEO_ERR_BAD_SHAPE, "term %d: line %lld: unknown BC or boundary stencil longer than the line",
+                                t + 1, (long long)l + 1);
+                all_per = all_per && lb[l].kind == DEO_BC_PERIODIC;
+                all_same = all_same && same_map(lb[0], lb[l]);
+                if (lb[l].kind == DEO_BC_AFFINE) lmw = std::max(lmw, std::max(lb[l].m_l, lb[l].m_r));
+            }
+            if (all_per || all_same || ndims == 1) {
+                qp = &lb[0];
+            } else {
+                qp = nullptr;
+                lmw = std::max(lmw, 1);
+                const int rs = 5 + 2 * lmw;
+                lrec.assign((size_t)(nlines * rs), 0.0);
+                for (int64_t l = 0; l < nlines; ++l) {
+                    double* r = lrec.data() + l * rs;
+                    const deo_bc& b = lb[l];
+                    r[0] = b.kind == DEO_BC_PERIODIC ? 1.0 : 0.0;
+                    if (b.kind == DEO_BC_AFFINE) {
+                        r[1] = b.m_l;
+                        r[2] = b.m_r;
+                        r[3] = b.b_l;
+                        r[4] = b.b_r;
+                        for (int j = 0; j < b.m_l; ++j) r[5 + j] = b.a_l[j];
+                        for (int j = 0; j < b.m_r; ++j) r[5 + lmw + j] = b.a_r[j];
+                    }
+                }
+            }
+        }
+        static const deo_bc kNoBC{};
+        const deo_bc& q = qp ? *qp : kNoBC;
+        if (qp && bad_bc(q)) return fail(DEO_ERR_BAD_SHAPE, "term %d: boundary stencil longer than the line", t + 1);
         if (!A.wind && A.len < 2 * A.bpc + 1)
             return fail(DEO_ERR_BAD_SHAPE, "term %d: len %d < 2*boundary_point_count+1", t + 1, A.len);
         if (A.wind && A.len < 2 * A.bpc + A.off)
@@ -1105,6 +1158,15 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         for (int k = 0; k < DEO_MAX_BC; ++k) { T.al[k] = q.a_l[k]; T.ar[k] = q.a_r[k]; }
         T.bl = q.b_l;
         T.br = q.b_r;
+        T.lbc = nullptr;
+        T.lbc_stride = 0;
+        T.lbc_mw = 0;
+        if (!lrec.empty()) {
+            deo_status ls;
+            if ((ls = upload(*P, lrec, reinterpret_cast<const void**>(&T.lbc))) != DEO_OK) return ls;
+            T.lbc_stride = 5 + 2 * lmw;
+            T.lbc_mw = lmw;
+        }
         if (t < 3) {
             deo::ShellTerm& S = P->shell.t[t];
             S.bc_kind = T.bc_kind;
@@ -1135,7 +1197,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         for (int t = 0; t < nterms && ok; ++t) {
             const TermDev& T = D.t[t];
             const RowTabDev& tb = T.tab[0];
-            if (T.has_field || T.nvar != 1 || tb.ilo > tb.ihi || T.axis > 2) {
+            if (T.has_field || T.nvar != 1 || tb.ilo > tb.ihi || T.axis > 2 || T.lbc) {
                 ok = false;
                 break;
             }

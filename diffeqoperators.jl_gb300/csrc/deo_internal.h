@@ -70,6 +70,14 @@ struct TermDev {
     double al[DEO_MAX_BCW];
     double ar[DEO_MAX_BCW];
     double bl, br;
+    // Boundary conditions that differ per line (MultiDimBC{dim}(BCs::Array)):
+    // null, or one record of lbc_stride doubles per line, lines numbered in
+    // the column-major order of the other axes:
+    //   [kind (0 affine, 1 periodic: the line wraps), m_l, m_r, b_l, b_r,
+    //    a_l[0 .. lbc_mw-1], a_r[0 .. lbc_mw-1]]
+    const double* lbc;
+    int lbc_stride;
+    int lbc_mw;
 };
 
 #define DEO_KMAX_TERMS 8

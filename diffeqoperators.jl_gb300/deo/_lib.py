@@ -59,7 +59,7 @@ class BCStruct(C.Structure):
 
 class Term(C.Structure):
     _fields_ = [("op", _vp), ("axis", C.c_int), ("bc", C.POINTER(BCStruct)), ("coeff_field", _vp),
-                ("path", C.c_int)]
+                ("path", C.c_int), ("line_bcs", C.POINTER(BCStruct))]
 
 
 class Instance(C.Structure):

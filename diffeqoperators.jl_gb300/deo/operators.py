@@ -481,13 +481,44 @@ class MultiDimensionalBC:
 
 
 class MultiDimDirectionalBC(MultiDimensionalBC):
-    """One atomic BC extended over every line along `axis` (multi_dim_bc_operators.jl:54-57, 97-101)."""
+    """BCs extending dimension `axis` (multi_dim_bc_operators.jl:54-57): one
+    atomic BC for every line (`s` = the array's size, :97-101), or an array of
+    atomic BCs with one per line, shaped like the array without that axis
+    (MultiDimBC{dim}(BCs::Array), :91-93; its lines get BCs[I, J] * u[I, :, J])."""
 
-    def __init__(self, bc: AtomicBC, axis: int, s: Sequence[int]):
-        self.bc, self.axis, self.shape = bc, int(axis), tuple(int(n) for n in s)
+    def __init__(self, bc, axis: int, s: Sequence[int] | None = None):
+        self.axis = int(axis)
+        if isinstance(bc, AtomicBC):
+            if s is None:
+                raise DeoArgError(2, "an atomic BC needs the array size s")
+            self.bc, self.lines, self.shape = bc, None, tuple(int(n) for n in s)
+            self.ndims = len(self.shape)
+        else:
+            arr = np.asarray(bc, dtype=object)
+            if arr.size == 0 or not all(isinstance(b, AtomicBC) for b in arr.ravel()):
+                raise DeoArgError(2, "MultiDimBC{dim}(BCs): an array of atomic BCs is needed")
+            self.bc, self.lines, self.shape = arr.ravel()[0], arr, None
+            self.ndims = arr.ndim + 1
 
     def __add__(self, other):
         return compose(self, other)
+
+    def check_size(self, shape) -> None:
+        """The reference's assertion at Q*u (multi_dim_bc_operators.jl:211, 237)."""
+        if self.lines is None:
+            if tuple(self.shape) != tuple(shape):
+                raise DeoShapeError(1, f"BC built for size {self.shape}, array has size {tuple(shape)}")
+            return
+        perp = tuple(n for k, n in enumerate(shape) if k != self.axis - 1)
+        if tuple(self.lines.shape) != perp:
+            raise DeoShapeError(1, f"Size of the BCs array in the MultiDimBC is incorrect, needs to be {perp} to "
+                                   f"extend dimension {self.axis}, got {tuple(self.lines.shape)}")
+
+    def line_bcs(self, axis: int):
+        """The per-line BCs in the column-major order of the other axes, or None."""
+        if axis != self.axis:
+            raise DeoShapeError(1, f"operator differentiates along {axis} but the BC extends dimension {self.axis}")
+        return None if self.lines is None else list(self.lines.ravel(order="F"))
 
     def bc_for(self, axis: int, ndims: int) -> AtomicBC:
         if axis != self.axis:
@@ -499,8 +530,17 @@ class ComposedMultiDimBC(MultiDimensionalBC):
     """compose(Qx, Qy, ...) (multi_dim_bc_operators.jl:178-192)."""
 
     def __init__(self, bcs: Sequence[MultiDimDirectionalBC]):
+        self.parts = {b.axis: b for b in bcs}
         self.bcs = {b.axis: b.bc for b in bcs}
-        self.shape = bcs[0].shape
+        self.shape = next((b.shape for b in bcs if b.shape is not None), None)
+        self.ndims = bcs[0].ndims
+
+    def check_size(self, shape) -> None:
+        for b in self.parts.values():
+            b.check_size(shape)
+
+    def line_bcs(self, axis: int):
+        return self.parts[axis].line_bcs(axis)
 
     def bc_for(self, axis: int, ndims: int) -> AtomicBC:
         return self.bcs[axis]
@@ -509,7 +549,7 @@ class ComposedMultiDimBC(MultiDimensionalBC):
 def compose(*bcs):
     if not bcs:
         raise DeoArgError(2, "compose needs at least one BC")
-    n = len(bcs[0].shape)
+    n = bcs[0].ndims
     if len(bcs) != n:
         raise DeoArgError(2, "There must be enough BCs to cover every dimension - check that the number of "
                              "MultiDimBCs == N")
@@ -520,8 +560,14 @@ def compose(*bcs):
     return ComposedMultiDimBC(sorted(bcs, key=lambda b: b.axis))
 
 
-def MultiDimBC(bc: AtomicBC, s: Sequence[int], dim: int | None = None):
-    """MultiDimBC{dim}(BC, s) / MultiDimBC(BC, s) (multi_dim_bc_operators.jl:93-110)."""
+def MultiDimBC(bc, s=None, dim: int | None = None):
+    """MultiDimBC{dim}(BC, s) / MultiDimBC(BC, s) (multi_dim_bc_operators.jl:93-110);
+    MultiDimBC(BCs, dim=dim) with an array of atomic BCs, one per line along
+    `dim` (MultiDimBC{dim}(BCs::Array), :91-93)."""
+    if not isinstance(bc, AtomicBC):
+        if dim is None:
+            raise DeoArgError(2, "MultiDimBC with an array of BCs needs dim")
+        return MultiDimDirectionalBC(bc, dim)
     if dim is not None:
         return MultiDimDirectionalBC(bc, dim, s)
     return tuple(MultiDimDirectionalBC(bc, k + 1, s) for k in range(len(s)))
@@ -610,6 +656,9 @@ class SolvePlan:
                 raise DeoShapeError(1, "an atomic BC on an N-D array extends dimension 1; use MultiDimBC")
             bc = A.Q
         else:
+            A.Q.check_size(self.shape)
+            if A.Q.line_bcs(ax) is not None:
+                raise DeoArgError(2, "A \\ u is built here for one BC per axis, not an array of per-line BCs")
             bc = A.Q.bc_for(ax, nd)
         if ax > nd:
             raise DeoShapeError(1, f"operator axis {ax} but u has {nd} dimensions")
@@ -721,14 +770,20 @@ class Plan:
                                            "(multi_dim_bc_operators.jl:210); use MultiDimBC for other axes")
                 bc = g.Q
             else:
-                if tuple(g.Q.shape) != self.shape:
-                    raise DeoShapeError(1, f"BC built for size {g.Q.shape}, array has size {self.shape}")
+                g.Q.check_size(self.shape)
                 bc = g.Q.bc_for(ax, nd)
             self._keep.append(bc)
             terms[i].op = g.L._h
             terms[i].axis = ax
             terms[i].bc = C.pointer(bc._s)
             terms[i].path = path
+            lines = None if isinstance(g.Q, AtomicBC) else g.Q.line_bcs(ax)
+            if lines is not None:
+                arr = (L.BCStruct * len(lines))(*[b._s for b in lines])
+                self._keep.append(arr)
+                terms[i].line_bcs = C.cast(arr, C.POINTER(L.BCStruct))
+            else:
+                terms[i].line_bcs = None
             if g.field is not None:
                 f = g.field
                 _check_layout(f, "coefficient field")

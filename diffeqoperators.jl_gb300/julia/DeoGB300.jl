@@ -62,6 +62,7 @@ struct DeoTerm
     bc::Ptr{DeoBC}
     coeff_field::Ptr{Cvoid}
     path::Cint
+    line_bcs::Ptr{DeoBC}  # C_NULL, or one BC per line (MultiDimBC{dim}(BCs::Array))
 end
 
 # ---- errors: deo_status -> the reference's exception types ------------------
@@ -105,10 +106,21 @@ deo_bc(Q::AffineBC) = DeoBC(0, length(Q.a_l), length(Q.a_r), _pad(Q.a_l), _pad(Q
 deo_bc(::PeriodicBC) = DeoBC(1, 0, 0, _pad(()), _pad(()), 0.0, 0.0)
 _axis(::DerivativeOperator{T, N}) where {T, N} = N
 
-# BC acting on axis `ax` of an N-D array
+# BCs acting on axis `ax` of an N-D array: the array of per-line BCs
+# (multi_dim_bc_operators.jl:54-61; MultiDimBC{dim}(BC, s) fills it with one
+# BC, MultiDimBC{dim}(BCs::Array) gives one per line), or an atomic BC
+_line_bcs(Q::Union{AffineBC, PeriodicBC}, ax) = nothing
+_line_bcs(Q::MultiDimDirectionalBC, ax) = Q.BCs
+_line_bcs(Q::ComposedMultiDimBC, ax) = Q.BCs[ax]
 _bc_for(Q::Union{AffineBC, PeriodicBC}, ax) = Q
-_bc_for(Q::MultiDimDirectionalBC, ax) = first(Q.BCs)      # one BC per axis (filled)
-_bc_for(Q::ComposedMultiDimBC, ax) = first(Q.BCs[ax])
+_bc_for(Q::Union{MultiDimDirectionalBC, ComposedMultiDimBC}, ax) = first(_line_bcs(Q, ax))
+# libdeo's per-line table (column-major over the other axes, the array's own
+# order); C_NULL-equivalent `nothing` when every line has the same BC
+function _deo_line_bcs(Q, ax)
+    B = _line_bcs(Q, ax)
+    (B === nothing || all(b -> b === first(B) || deo_bc(b) == deo_bc(first(B)), B)) && return nothing
+    return DeoBC[deo_bc(b) for b in vec(B)]
+end
 
 _ghosts(A::GhostDerivativeOperator) = (A,)
 _ghosts(A::DiffEqOperatorCombination) = Tuple(op for op in A.ops)
@@ -145,10 +157,12 @@ function plan_for(A, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
         gs = _ghosts(A)
         ops = [deo_operator(g.L) for g in gs]
         bcs = [deo_bc(_bc_for(g.Q, _axis(g.L))) for g in gs]
-        terms = [DeoTerm(ops[i], _axis(gs[i].L), pointer(bcs, i), C_NULL, 0) for i in eachindex(gs)]
+        lines = [_deo_line_bcs(g.Q, _axis(g.L)) for g in gs]
+        terms = [DeoTerm(ops[i], _axis(gs[i].L), pointer(bcs, i), C_NULL, 0,
+                         lines[i] === nothing ? Ptr{DeoBC}(C_NULL) : pointer(lines[i])) for i in eachindex(gs)]
         sizes = Int64[sz...]
         h = Ref{Ptr{Cvoid}}(C_NULL)
-        GC.@preserve bcs sizes terms check(ccall((:deo_plan_create, libdeo), Cint,
+        GC.@preserve bcs lines sizes terms check(ccall((:deo_plan_create, libdeo), Cint,
                                                  (Cint, Ptr{Int64}, Cint, Cint, Ptr{DeoTerm}, Ref{Ptr{Cvoid}}),
                                                  length(sz), sizes, T === Float64 ? 0 : 1, length(terms), terms, h))
         foreach(op -> ccall((:deo_operator_destroy, libdeo), Cvoid, (Ptr{Cvoid},), op), ops)
@@ -306,6 +320,8 @@ const SOLVES = IdDict{Any, Dict{Any, Ptr{Cvoid}}}()
 function solve_plan_for(A::GhostDerivativeOperator, sz::Dims, ::Type{T}) where {T <: Union{Float32, Float64}}
     cache = get!(() -> Dict{Any, Ptr{Cvoid}}(), SOLVES, A)
     _cached!(cache, (sz, T), _coeff_key(A), :deo_solve_destroy) do
+        _deo_line_bcs(A.Q, _axis(A.L)) === nothing ||
+            throw(ArgumentError("A \\ u is built here for one BC per axis, not an array of per-line BCs"))
         op = deo_operator(A.L)
         bc = Ref(deo_bc(_bc_for(A.Q, _axis(A.L))))
         sizes = Int64[sz...]

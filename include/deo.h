@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define DEO_ABI_VERSION 1
+#define DEO_ABI_VERSION 2
 #define DEO_MAX_BC 16      /* longest ghost stencil a_l / a_r */
 #define DEO_MAX_TERMS 8    /* terms in one plan */
 #define DEO_MAX_DIMS 8
@@ -167,9 +167,15 @@ deo_status deo_bc_array(const deo_bc* bc, int n, double* QL, double* Qb);
 typedef struct {
     const deo_operator* op;
     int axis;                 /* 1-based, Julia's N in CenteredDifference{N} */
-    const deo_bc* bc;         /* applied along `axis` to every line */
+    const deo_bc* bc;         /* applied along `axis` to every line (ignored when line_bcs is set) */
     const void* coeff_field;  /* device pointer or NULL */
     int path;                 /* DEO_PATH_* */
+    /* NULL, or one BC per line along `axis` (host array of prod(sizes)/sizes[axis]
+     * entries, column-major over the other axes): MultiDimBC{dim}(BCs::Array),
+     * multi_dim_bc_operators.jl:91-93, whose lines get BCs[I, J] * u[I, :, J]
+     * (:28-52).  A periodic BC among others wraps around its line; an array
+     * of periodic BCs only pads with the edge planes, as PeriodicBC does. */
+    const deo_bc* line_bcs;
 } deo_term;
 
 deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,

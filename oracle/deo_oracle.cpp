@@ -866,8 +866,40 @@ int orc_abs_scale_nd(int nterms, void* const* ops, const int* axes, const void* 
     return rc;
 }
 
+// MultiDimBC{dim}(BCs::Array) (multi_dim_bc_operators.jl:91-93): line_bcs[t]
+// (may be NULL) holds one BC per line of term t, in the column-major order of
+// the other axes (the BCs array's own order); each line's ghosts are
+// BCs[I, J] * u[I, :, J] (slice_rmul, :28-52), the 1-D ghost fill -- so a
+// periodic BC among others wraps around its line -- except when every BC of
+// the array is periodic, where the array's element type selects the N-D
+// periodic padding with the edge planes (:221-228).
+static int apply_nd_impl(int nterms, void* const* ops, const int* axes, const void* bcs, const double* const* fields,
+                         const void* const* line_bcs, int ndims, const long* sizes, const double* u, double* out,
+                         int overwrite, int nthreads);
+
 int orc_apply_nd(int nterms, void* const* ops, const int* axes, const void* bcs, const double* const* fields,
                  int ndims, const long* sizes, const double* u, double* out, int overwrite, int nthreads) {
+    return apply_nd_impl(nterms, ops, axes, bcs, fields, nullptr, ndims, sizes, u, out, overwrite, nthreads);
+}
+
+int orc_apply_nd_lines(int nterms, void* const* ops, const int* axes, const void* bcs, const double* const* fields,
+                       const void* const* line_bcs, int ndims, const long* sizes, const double* u, double* out,
+                       int overwrite, int nthreads) {
+    return apply_nd_impl(nterms, ops, axes, bcs, fields, line_bcs, ndims, sizes, u, out, overwrite, nthreads);
+}
+
+int orc_abs_scale_nd_lines(int nterms, void* const* ops, const int* axes, const void* bcs,
+                           const double* const* fields, const void* const* line_bcs, int ndims, const long* sizes,
+                           const double* u, double* out) {
+    g_abs = true;
+    const int rc = apply_nd_impl(nterms, ops, axes, bcs, fields, line_bcs, ndims, sizes, u, out, 1, 1);
+    g_abs = false;
+    return rc;
+}
+
+static int apply_nd_impl(int nterms, void* const* ops, const int* axes, const void* bcs, const double* const* fields,
+                         const void* const* line_bcs, int ndims, const long* sizes, const double* u, double* out,
+                         int overwrite, int nthreads) {
     long total = 1;
     for (int k = 0; k < ndims; ++k) total *= sizes[k];
     const BC* bc = static_cast<const BC*>(bcs);
@@ -883,6 +915,9 @@ int orc_apply_nd(int nterms, void* const* ops, const int* axes, const void* bcs,
         const long inner = stride;
         const int mode = (ndims == 1) ? 1 : 0;
         double* dst = (t == 0) ? acc.data() : term.data();
+        const BC* lb = (line_bcs && line_bcs[t]) ? static_cast<const BC*>(line_bcs[t]) : nullptr;
+        bool all_periodic = lb != nullptr;
+        for (long line = 0; lb && line < nlines && all_periodic; ++line) all_periodic = lb[line].kind == 1;
 #if defined(_OPENMP)
 #pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
 #endif
@@ -893,7 +928,9 @@ int orc_apply_nd(int nterms, void* const* ops, const int* axes, const void* bcs,
             L.u = u + base;
             L.stride = stride;
             L.len = n;
-            if (ndims == 1) ghosts_1d(bc[t], L.u, n, stride, L.l, L.r);
+            if (lb && !all_periodic) ghosts_1d(lb[line], L.u, n, stride, L.l, L.r);
+            else if (lb) ghosts_nd(lb[line], L.u, n, stride, L.l, L.r);
+            else if (ndims == 1) ghosts_1d(bc[t], L.u, n, stride, L.l, L.r);
             else ghosts_nd(bc[t], L.u, n, stride, L.l, L.r);
             if (fields && fields[t]) {
                 VecCoeff c{fields[t] + base, stride};

@@ -61,6 +61,12 @@ def lib():
                                    C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, _dp, C.c_int, C.c_int]
         L.orc_abs_scale_nd.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
                                        C.POINTER(_dp), C.c_int, C.POINTER(C.c_long), _dp, _dp]
+        L.orc_apply_nd_lines.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
+                                         C.POINTER(_dp), C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_long), _dp,
+                                         _dp, C.c_int, C.c_int]
+        L.orc_abs_scale_nd_lines.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
+                                             C.POINTER(_dp), C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_long),
+                                             _dp, _dp]
         L.orc_array_op.argtypes = [C.c_void_p, _dp]
         L.orc_array_bc.argtypes = [C.c_void_p, C.c_long, _dp, _dp]
         L.orc_ssprk3.argtypes = [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int), C.c_void_p,
@@ -256,6 +262,9 @@ class _Args:
     """ctypes argument block shared by apply / abs_scale / ssprk3."""
 
     def __init__(self, terms, u: np.ndarray):
+        """terms: (Op, BC[, field[, line_bcs]]); line_bcs (may be None) is a
+        sequence of one BC per line of the term, in the column-major order of
+        the other axes (MultiDimBC{dim}(BCs::Array))."""
         self.u = np.asfortranarray(u, dtype=np.float64)
         self.sizes = (C.c_long * self.u.ndim)(*self.u.shape)
         n = self.n = len(terms)
@@ -271,6 +280,15 @@ class _Args:
                 self.fptrs[i] = f.ctypes.data_as(_dp)
             else:
                 self.fptrs[i] = _dp()
+        self.lines = (C.c_void_p * n)()
+        self.has_lines = False
+        for i, t in enumerate(terms):
+            lb = t[3] if len(t) > 3 else None
+            if lb is not None:
+                arr = (BC * len(lb))(*lb)
+                self.keep.append(arr)
+                self.lines[i] = C.cast(arr, C.c_void_p)
+                self.has_lines = True
 
     def head(self):
         return (self.n, self.ops, self.axes, C.cast(self.bcs, C.c_void_p), self.fptrs, self.u.ndim, self.sizes)
@@ -281,8 +299,13 @@ def apply(terms, u: np.ndarray, out: np.ndarray | None = None, overwrite: bool =
     """sum_t (L_t*Q_t)*u.  terms: list of (Op, BC[, field]); u Fortran-ordered."""
     a = _Args(terms, u)
     o = np.zeros(a.u.shape, order="F") if out is None else out
-    rc = lib().orc_apply_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp), int(overwrite),
-                            int(nthreads))
+    if a.has_lines:
+        h = a.head()
+        rc = lib().orc_apply_nd_lines(*h[:5], a.lines, *h[5:], a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp),
+                                      int(overwrite), int(nthreads))
+    else:
+        rc = lib().orc_apply_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp), int(overwrite),
+                                int(nthreads))
     if rc != 0:
         raise AssertionError("size mismatch between operator and array")
     return o
@@ -292,7 +315,12 @@ def abs_scale(terms, u: np.ndarray) -> np.ndarray:
     """sum_k |c_k * u_k| per point, ghost terms expanded (parity tolerance scale)."""
     a = _Args(terms, u)
     o = np.zeros(a.u.shape, order="F")
-    if lib().orc_abs_scale_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp)) != 0:
+    if a.has_lines:
+        h = a.head()
+        rc = lib().orc_abs_scale_nd_lines(*h[:5], a.lines, *h[5:], a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp))
+    else:
+        rc = lib().orc_abs_scale_nd(*a.head(), a.u.ctypes.data_as(_dp), o.ctypes.data_as(_dp))
+    if rc != 0:
         raise AssertionError("size mismatch between operator and array")
     return o
 

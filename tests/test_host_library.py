@@ -31,7 +31,7 @@ def test_header_symbols_exported():
 
 
 def test_abi_version():
-    assert deo.lib().deo_abi_version() == 1
+    assert deo.lib().deo_abi_version() == 2
 
 
 def _same(a, b):
