@@ -24,6 +24,7 @@ SOURCES = {
     "deo_vector.o": ("nvcc", "deo_vector.cu"),
     "deo_solve.o": ("nvcc", "deo_solve.cu"),
     "deo_host.o": ("cxx", "deo_host.cpp"),
+    "deo_serve.o": ("cxx", "deo_serve.cpp"),
 }
 
 

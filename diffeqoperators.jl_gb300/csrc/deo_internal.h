@@ -255,6 +255,8 @@ extern "C" int deo_k_band_solve(int n, int kl, int ku, const double* ab, const i
 // Launchers implemented in deo_kernels.cu (return cudaError_t as int).
 extern "C" int deo_k_apply(const deo::PlanDev* p, const void* u, void* du, int overwrite, int adjoint,
                            void* stream);
+// x *= f over n points (dtype 0 f64, 1 f32), stream-ordered.
+extern "C" int deo_k_scale(void* x, int64_t n, int dtype, double f, void* stream);
 // Commits k_batch's module image and launch resources on the current device
 // (one empty launch of each instantiation; *counter is bumped, nothing else).
 extern "C" int deo_k_batch_prepare(unsigned int* counter, void* stream);

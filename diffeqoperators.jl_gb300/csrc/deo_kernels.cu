@@ -149,6 +149,23 @@ extern "C" int deo_k_nonlinear_diffusion(const PlanDev* plan, int len, int n, in
 
 extern "C" int deo_k_num_sms(void);
 
+template <typename T>
+__global__ void __launch_bounds__(256) k_scale(T* __restrict__ x, int64_t n, T f) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = f * x[i];
+}
+
+// x *= f over n points of the dtype (the adjoint seed 2 u(T) of ||u(T)||^2).
+extern "C" int deo_k_scale(void* x, int64_t n, int dtype, double f, void* stream) {
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int sms = deo_k_num_sms();
+    const int64_t want = (n + 255) / 256;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * 8));
+    if (dtype == 0) k_scale<double><<<blocks, 256, 0, st>>>((double*)x, n, f);
+    else k_scale<float><<<blocks, 256, 0, st>>>((float*)x, n, (float)f);
+    return (int)cudaGetLastError();
+}
+
 extern "C" int deo_k_stage_batch(const StageDev* st, const WorkItem* items, int64_t n_items, unsigned int* counter,
                                  int dtype, int ctas_per_sm, int threads, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -62,6 +62,16 @@ class Term(C.Structure):
                 ("path", C.c_int), ("line_bcs", C.POINTER(BCStruct))]
 
 
+class Request(C.Structure):
+    _fields_ = [("plan", _vp), ("u0", _vp), ("nsteps", C.c_int), ("dt", C.c_double), ("want_grad", C.c_int)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "admitted", "completed", "rejected", "failed", "cancelled",
+                                          "rounds", "steps", "launches", "rebuilds", "in_use_bytes", "active",
+                                          "pending", "device_us")]
+
+
 class Instance(C.Structure):
     _fields_ = [("plan", _vp), ("u", _vp), ("du", _vp)]
 
@@ -154,6 +164,14 @@ def lib():
     proto("deo_batch_config", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64))
     proto("deo_batch_destroy", None, _vp)
     proto("deo_batch_autotune", st, _vp, C.c_char_p, _vp)
+    proto("deo_serve_create", st, C.c_size_t, C.c_int, C.c_int, C.POINTER(_vp))
+    proto("deo_serve_submit", st, _vp, C.POINTER(Request), C.POINTER(C.c_int64))
+    proto("deo_serve_pump", st, _vp)
+    proto("deo_serve_poll", st, _vp, C.c_int64, _vp, _vp, C.POINTER(C.c_double))
+    proto("deo_serve_cancel", st, _vp, C.c_int64)
+    proto("deo_serve_stats_get", st, _vp, C.POINTER(ServeStats))
+    proto("deo_serve_inject_alloc_failures", st, _vp, C.c_int)
+    proto("deo_serve_destroy", None, _vp)
     _lib = L
     return L
 
@@ -179,6 +197,8 @@ EXPORTED = [
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_nonlinear_diffusion_plan", "deo_nonlinear_diffusion",
     "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
+    "deo_serve_create", "deo_serve_submit", "deo_serve_pump", "deo_serve_poll", "deo_serve_cancel", "deo_serve_stats_get",
+    "deo_serve_inject_alloc_failures", "deo_serve_destroy",
     "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply", "deo_vector_calculus_info",
     "deo_vector_calculus_destroy", "deo_dot_product", "deo_cross_product", "deo_square_norm",
     "deo_solve_plan", "deo_solve_bands", "deo_solve_apply", "deo_solve_destroy",

@@ -1,4 +1,4 @@
-"""Continuous-batching server for method-of-lines solves.
+"""Continuous-batching server for method-of-lines solves (libdeo's deo_serve_*).
 
 Each request is an advection-diffusion solve
     du/dt = nu * Laplacian(u) - c * du/dx,   Dirichlet0 on every face,
@@ -7,32 +7,34 @@ for every axis k, plus UpwindDifference{1}(1, a, h, n, -c)), advanced K
 fixed SSP-RK3 steps (dt from CFL 0.4); optionally the gradient of
 ||u(T)||^2 with respect to u0 is computed by the transposed steps.
 
-The state of every admitted request lives in device memory (three buffers
-per request).  Each server tick advances EVERY active request by one step:
-three batched stage launches (libdeo's persistent work-list kernel) cover all
-requests at once -- forward and adjoint stages mixed -- replayed from a CUDA
-graph while the set of active requests is unchanged.  Requests are admitted
-FIFO whenever their memory fits under the HBM budget, so work that arrives
-while others are on the GPU joins the next tick (continuous batching), and a
-finished request frees its slot immediately.  Every request's arithmetic is
-independent of the others (no cross-request reductions, fixed per-point
-order), so its result is the same alone or in any mix.
+The serving loop is native (csrc/deo_serve.cpp): the state of every admitted
+request lives in device memory; rounds of several steps that advance every
+active request in three batched stage launches per step are enqueued back to
+back without waiting for the device; results are copied out asynchronously;
+requests that arrive while others run are admitted as memory frees up
+(continuous batching) under a device-memory budget.  This module submits the
+requests at their arrival times, drives deo_serve_pump and collects results.
+Every request's arithmetic is independent of the others (no cross-request
+reductions, fixed per-point order), so its result is the same alone or in any
+mix.
 
 No reference counterpart: the reference delegates time stepping to
 OrdinaryDiffEq and has no serving layer.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import List, Optional
 
 import numpy as np
 
-from .batch import StageBatch
+from . import _lib as L
+from ._lib import check
 from .operators import (CenteredDifference, DiffEqOperatorCombination, Dirichlet0BC, MultiDimDirectionalBC, Plan,
-                        UpwindDifference, julia_array)
+                        UpwindDifference)
 
 
 @dataclass
@@ -50,7 +52,6 @@ class Request:
     # filled by the server
     uT: Optional[np.ndarray] = None
     grad: Optional[np.ndarray] = None
-    t_admit: float = float("nan")
     t_done: float = float("nan")
     rejected: str = ""
 
@@ -93,155 +94,152 @@ def advection_diffusion(shape, nu, c, approx_order=2):
     return DiffEqOperatorCombination([P * MultiDimDirectionalBC(bc, P.axis, shape) for P in ops])
 
 
-class _Slot:
-    def __init__(self, req: Request, device):
-        import torch
-        self.req = req
-        A = advection_diffusion(req.shape, req.nu, req.c, req.approx_order)
-        self.A = A
-        self.plan = Plan(A.terms(), req.shape, 0)
-        self.u = julia_array(req.shape, torch.float64, device)
-        self.u.copy_(torch.from_numpy(req.initial()))
-        self.b1 = julia_array(req.shape, torch.float64, device)
-        self.b2 = julia_array(req.shape, torch.float64, device)
-        self.step = 0
-        self.phase = "fwd"          # fwd -> (adj) -> done
-        self.dt = req.dt()
-
-    def stages(self):
-        """(stage1, stage2, stage3) descriptors for this slot's next step."""
-        p, dt = self.plan, self.dt
-        if self.phase == "fwd":
-            return (dict(plan=p, c=self.u, out=self.b1, gamma=1.0, dt=dt),
-                    dict(plan=p, a=self.u, alpha=0.75, c=self.b1, out=self.b2, gamma=0.25, dt=dt),
-                    dict(plan=p, a=self.u, alpha=1.0 / 3.0, c=self.b2, out=self.u, gamma=2.0 / 3.0, dt=dt))
-        # transposed step on ub = self.u, g1 = b1, g2 = b2
-        return (dict(plan=p, c=self.u, out=self.b2, gamma=2.0 / 3.0, dt=dt, adjoint=True),
-                dict(plan=p, c=self.b2, out=self.b1, gamma=0.25, dt=dt, adjoint=True),
-                dict(plan=p, a=self.u, alpha=1.0 / 3.0, b=self.b2, beta=0.75, c=self.b1, out=self.u, gamma=1.0,
-                     dt=dt, adjoint=True))
-
-
 class Server:
-    def __init__(self, hbm_budget_bytes: float = 120e9, use_graph: bool = True, tile: int = 8192,
-                 ctas_per_sm: int = 4, device="cuda", max_active: int = 1 << 30):
+    def __init__(self, hbm_budget_bytes: float = 120e9, max_steps_per_round: int = 64,
+                 inject_alloc_failures: int = 0):
+        h = C.c_void_p()
+        check(L.lib().deo_serve_create(int(hbm_budget_bytes), 0, int(max_steps_per_round), C.byref(h)))
+        self._h = h
         self.budget = float(hbm_budget_bytes)
-        self.use_graph = use_graph
-        self.tile = tile
-        self.ctas = ctas_per_sm
-        self.device = device
-        self.max_active = max_active
-        self.queue: List[Request] = []
-        self.active: List[_Slot] = []
+        if inject_alloc_failures:
+            check(L.lib().deo_serve_inject_alloc_failures(h, int(inject_alloc_failures)))
         self.done: List[Request] = []
-        self.in_use = 0.0
-        self._batches = None
-        self.ticks = 0
-        self.rebuilds = 0
-        self.launches = 0
+        self._out = {}    # native id -> (request, plan, u0 buffer, uT buffer, grad buffer)
+        self._native = {}  # id(request) -> native id
 
-    # -- admission ------------------------------------------------------------
-    def submit(self, req: Request):
-        if req.bytes_needed() > self.budget:
+    def __del__(self):
+        try:
+            if self._h:
+                L.lib().deo_serve_destroy(self._h)
+                self._h = None
+        except Exception:
+            pass
+
+    def submit(self, req: Request, t0: float) -> bool:
+        A = advection_diffusion(req.shape, req.nu, req.c, req.approx_order)
+        plan = Plan(A.terms(), req.shape, 0)
+        u0 = req.initial()
+        q = L.Request(plan.handle, C.c_void_p(u0.ctypes.data), int(req.K), float(req.dt()), int(bool(req.want_grad)))
+        rid = C.c_int64()
+        st = L.lib().deo_serve_submit(self._h, C.byref(q), C.byref(rid))
+        if st == 8:  # DEO_ERR_REJECTED
             req.rejected = "larger than the HBM budget"
+            req.t_done = time.perf_counter() - t0
+            L.lib().deo_serve_poll(self._h, rid.value, None, None, None)  # forget it
             self.done.append(req)
             return False
-        self.queue.append(req)
+        check(st)
+        uT = np.empty(req.shape, order="F")
+        g = np.empty(req.shape, order="F") if req.want_grad else None
+        self._out[rid.value] = (req, plan, u0, uT, g)
+        self._native[id(req)] = rid.value
         return True
 
-    def _admit(self, now: float):
-        changed = False
-        while self.queue and len(self.active) < self.max_active:
-            r = self.queue[0]
-            need = r.bytes_needed()
-            if self.in_use + need > self.budget:
-                break                      # FIFO: wait for memory to free up
-            self.queue.pop(0)
-            try:
-                slot = _Slot(r, self.device)
-            except Exception as e:         # allocation failure is reported, not fatal
-                r.rejected = f"admission failed: {e}"
-                self.done.append(r)
+    def cancel(self, req: Request) -> None:
+        check(L.lib().deo_serve_cancel(self._h, self._native[id(req)]))
+
+    def _collect(self, t0: float) -> int:
+        got = 0
+        lib = L.lib()
+        for rid in list(self._out):
+            req, plan, u0, uT, g = self._out[rid]
+            st = lib.deo_serve_poll(self._h, rid, C.c_void_p(uT.ctypes.data),
+                                    C.c_void_p(g.ctypes.data) if g is not None else None, None)
+            if st == 7:  # DEO_ERR_NOT_READY
                 continue
-            r.t_admit = now
-            self.in_use += need
-            self.active.append(slot)
-            changed = True
-        return changed
-
-    def _rebuild(self):
-        sets = [s.stages() for s in self.active]
-        self._batches = [StageBatch([st[k] for st in sets], tile=self.tile, ctas_per_sm=self.ctas) for k in range(3)]
-        self.rebuilds += 1
-
-    # -- one tick: one SSP-RK3 step (forward or transposed) for every active slot
-    def tick(self):
-        import torch
-        for b in self._batches:
-            b.run(self.use_graph)
-        self.launches += 3
-        self.ticks += 1
-        torch.cuda.current_stream().synchronize()
-        changed = False
-        keep = []
-        for s in self.active:
-            s.step += 1
-            if s.phase == "fwd" and s.step == s.req.K:
-                s.req.uT = s.u.cpu().numpy()
-                if s.req.want_grad:
-                    s.u.mul_(2.0)          # ubar(T) = 2 u(T)
-                    s.phase, s.step = "adj", 0
-                    changed = True
-                else:
-                    s.phase = "done"
-            elif s.phase == "adj" and s.step == s.req.K:
-                s.req.grad = s.u.cpu().numpy()
-                s.phase = "done"
-            if s.phase == "done":
-                changed = True
-                self.in_use -= s.req.bytes_needed()
-                self._finished.append(s.req)
+            req.t_done = time.perf_counter() - t0
+            if st == 0:
+                req.uT, req.grad = uT, g
+            elif st == 6:
+                req.rejected = "admission failed: device memory for the state could not be allocated"
+            elif st == 2:
+                req.rejected = "cancelled"
             else:
-                keep.append(s)
-        self.active = keep
-        return changed
+                check(st)
+            self.done.append(req)
+            del self._out[rid]
+            got += 1
+        return got
 
-    def run(self, requests: List[Request], realtime: bool = True, timeout_s: float = 600.0):
-        """Serve `requests` (arrival times relative to the start).  Returns stats."""
+    def stats(self) -> dict:
+        s = L.ServeStats()
+        check(L.lib().deo_serve_stats_get(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in L.ServeStats._fields_}
+
+    def run(self, requests: List[Request], realtime: bool = True, timeout_s: float = 600.0, on_tick=None):
+        """Serve `requests` (arrival times relative to the start).  on_tick(server,
+        elapsed) is called once per loop iteration (tests cancel from it).
+        Returns stats."""
         import torch
+        lib = L.lib()
         pending = sorted(requests, key=lambda r: r.arrival)
         t0 = time.perf_counter()
-        self._finished = []
         i = 0
-        while (i < len(pending) or self.queue or self.active):
+        while i < len(pending) or self._out:
             now = time.perf_counter() - t0
             if now > timeout_s:
                 raise TimeoutError("serving run exceeded its time limit")
             while i < len(pending) and (pending[i].arrival <= now or not realtime):
-                self.submit(pending[i])
+                self.submit(pending[i], t0)
                 i += 1
-            changed = self._admit(now)
-            if not self.active:
-                if i < len(pending) and realtime:
-                    time.sleep(max(0.0, min(pending[i].arrival - now, 0.001)))
-                continue
-            if changed or self._batches is None:
-                self._rebuild()
-            self._finished = []
-            if self.tick():
-                self._batches = None
-            t = time.perf_counter() - t0
-            for r in self._finished:
-                r.t_done = t
-                self.done.append(r)
+            check(lib.deo_serve_pump(self._h))
+            if on_tick is not None:
+                on_tick(self, now)
+            if not self._collect(t0) and i < len(pending) and not self._out and realtime:
+                time.sleep(max(0.0, min(pending[i].arrival - now, 0.001)))
         torch.cuda.synchronize()
         makespan = time.perf_counter() - t0
-        ok = [r for r in self.done if not r.rejected]
+        done = [r for r in self.done if r in requests]
+        ok = [r for r in done if not r.rejected]
         lat = np.array([r.latency for r in ok]) if ok else np.array([np.nan])
-        return {"requests": len(requests), "completed": len(ok), "rejected": len(self.done) - len(ok),
+        st = self.stats()
+        return {"requests": len(requests), "completed": len(ok), "rejected": len(done) - len(ok),
                 "makespan_s": makespan, "solves_per_s": len(ok) / makespan,
                 "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                "ticks": self.ticks, "launches": self.launches, "rebuilds": self.rebuilds}
+                "ticks": st["steps"], "rounds": st["rounds"], "launches": st["launches"],
+                "rebuilds": st["rebuilds"], "failed": st["failed"], "cancelled": st["cancelled"],
+                "device_s": st["device_us"] * 1e-6}
+
+
+def solve_one_launch_per_instance(requests: List[Request]) -> dict:
+    """The baseline the server is measured against: the same requests, one at a
+    time in arrival order, each SSP-RK3 stage one plain apply of the request's
+    plan (deo_apply) plus its own combination kernels, a host loop of launches
+    per instance; the result of each request is copied to the host when it
+    finishes (the gradient requests take their transposed steps the same way).
+    Returns makespan and solves/s (arrivals ignored: the queue starts full)."""
+    import torch
+    from .operators import julia_array
+    t0 = time.perf_counter()
+    for r in requests:
+        A = advection_diffusion(r.shape, r.nu, r.c, r.approx_order)
+        p = Plan(A.terms(), r.shape, 0)
+        u = julia_array(r.shape)
+        u.copy_(torch.from_numpy(r.initial()))
+        f = julia_array(r.shape)
+        b1, b2 = julia_array(r.shape), julia_array(r.shape)
+        dt = r.dt()
+        for _ in range(r.K):
+            p.apply(u, f)
+            torch.add(u, f, alpha=dt, out=b1)
+            p.apply(b1, f)
+            b2.copy_(0.75 * u + 0.25 * (b1 + dt * f))
+            p.apply(b2, f)
+            u.copy_(u / 3.0 + (2.0 / 3.0) * (b2 + dt * f))
+        r.uT = u.cpu().numpy()
+        if r.want_grad:
+            u.mul_(2.0)
+            for _ in range(r.K):
+                p.adjoint(u, f)
+                b2.copy_((2.0 / 3.0) * (u + dt * f))
+                p.adjoint(b2, f)
+                b1.copy_(0.25 * (b2 + dt * f))
+                p.adjoint(b1, f)
+                u.copy_(u / 3.0 + 0.75 * b2 + (b1 + dt * f))
+            r.grad = u.cpu().numpy()
+    torch.cuda.synchronize()
+    makespan = time.perf_counter() - t0
+    return {"makespan_s": makespan, "solves_per_s": len(requests) / makespan}
 
 
 def poisson_requests(n: int, rate: float, seed: int = 0, grad_frac: float = 0.2, size_scale: float = 1.0,

@@ -393,4 +393,58 @@ function Base.:*(A::CurlOperator{T}, M::CuArray{T, 4}) where {T <: FT}
     _vc_apply!(CuArray{T}(undef, (size(M)[1:3] .- 2)..., 3), A, M, 1)
 end
 
+# ---- serving (deo_serve_*): MOL solves of (L)(du,u,p,t) = mul!(du, L, u) ----
+# Each request: K SSP-RK3 steps of du/dt = A*Q*u from a host array u0 (and,
+# with want_grad, the gradient of ||u(T)||^2 with respect to u0).  The server
+# keeps admitted states on the device under its byte budget; `pump!` never
+# waits for the device.
+struct DeoRequest
+    plan::Ptr{Cvoid}
+    u0::Ptr{Cvoid}
+    nsteps::Cint
+    dt::Cdouble
+    want_grad::Cint
+end
+
+mutable struct DeoServer
+    h::Ptr{Cvoid}
+    T::DataType
+    inputs::Dict{Int64, Any}   # u0 kept alive until the submission has copied it
+end
+
+function DeoServer(budget_bytes::Integer, ::Type{T} = Float64; max_steps_per_round::Integer = 64) where {T <: FT}
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:deo_serve_create, libdeo), Cint, (Csize_t, Cint, Cint, Ref{Ptr{Cvoid}}),
+                budget_bytes, T === Float64 ? 0 : 1, max_steps_per_round, h))
+    s = DeoServer(h[], T, Dict{Int64, Any}())
+    finalizer(x -> ccall((:deo_serve_destroy, libdeo), Cvoid, (Ptr{Cvoid},), x.h), s)
+    return s
+end
+
+"""submit!(s, A, u0, K, dt; want_grad=false) -> request id (an `ErrorException`
+carries DEO_ERR_REJECTED when the state is larger than the budget)."""
+function submit!(s::DeoServer, A::DeoOp, u0::Array{T}, K::Integer, dt::Real; want_grad::Bool = false) where {T <: FT}
+    T === s.T || throw(ArgumentError("the server serves $(s.T)"))
+    p = plan_for(A, size(u0), T)
+    rid = Ref{Int64}(0)
+    q = Ref(DeoRequest(p, pointer(u0), K, dt, want_grad))
+    GC.@preserve u0 check(ccall((:deo_serve_submit, libdeo), Cint, (Ptr{Cvoid}, Ref{DeoRequest}, Ref{Int64}),
+                                s.h, q, rid))
+    return rid[]
+end
+
+pump!(s::DeoServer) = check(ccall((:deo_serve_pump, libdeo), Cint, (Ptr{Cvoid},), s.h))
+
+"""poll!(s, rid, uT[, grad]) -> true once the result is in uT (and grad), false while it runs."""
+function poll!(s::DeoServer, rid::Integer, uT::Array{T}, grad::Union{Nothing, Array{T}} = nothing) where {T <: FT}
+    st = GC.@preserve uT grad ccall((:deo_serve_poll, libdeo), Cint,
+                                     (Ptr{Cvoid}, Int64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cdouble}),
+                                     s.h, rid, pointer(uT), grad === nothing ? C_NULL : pointer(grad), C_NULL)
+    st == 7 && return false   # DEO_ERR_NOT_READY
+    check(st)
+    return true
+end
+
+cancel!(s::DeoServer, rid::Integer) = check(ccall((:deo_serve_cancel, libdeo), Cint, (Ptr{Cvoid}, Int64), s.h, rid))
+
 end # module

@@ -466,6 +466,61 @@ deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int 
 #define DEO_NOALLOC_SCRATCH_BYTES (1 << 20)
 deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, int adjoint, int tile, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Serving: a device-resident loop of method-of-lines solves.  No reference
+ * counterpart (the reference leaves time stepping to OrdinaryDiffEq and has
+ * no serving layer); each solve's right-hand side is a plan, the reference's
+ * (L)(du, u, p, t) = mul!(du, L, u) (DiffEqOperators.jl:67-76).
+ * A request is nsteps fixed SSP-RK3 steps (Shu-Osher) of du/dt = A u from u0,
+ * and with want_grad also the gradient of ||u(T)||^2 with respect to u0 (the
+ * transposed steps from 2 u(T)).  Its state (three device arrays of the
+ * plan's size and dtype) comes from the stream-ordered allocator at
+ * admission; admission is FIFO under the byte budget.  deo_serve_pump never
+ * waits for the device: it collects finished results, admits what fits, and
+ * enqueues rounds (at most two in flight) of S steps, S the fewest steps any
+ * active request has left, in which three batched stage launches per step
+ * advance every active request.  A request's result does not depend on the
+ * others served with it.  All functions are thread-safe on one server.
+ * ---------------------------------------------------------------------- */
+typedef struct deo_server deo_server;
+typedef struct {
+    const deo_plan* plan;  /* right-hand side A; its size and dtype are the state's; kept alive by the caller */
+    const void* u0;        /* host memory, Julia layout, the server's dtype; copied by deo_serve_submit */
+    int nsteps;            /* K >= 1 */
+    double dt;             /* > 0 */
+    int want_grad;         /* also d ||u(T)||^2 / d u0 */
+} deo_request;
+typedef struct {
+    int64_t submitted, admitted, completed, rejected, failed, cancelled;
+    int64_t rounds, steps, launches, rebuilds;
+    int64_t in_use_bytes, active, pending;
+    int64_t device_us;  /* device time of the retired rounds, first launch to last */
+} deo_serve_stats;
+/* budget_bytes: device memory the admitted requests' states may take;
+ * max_steps_per_round caps S (0 = 64). */
+deo_status deo_serve_create(size_t budget_bytes, deo_dtype dtype, int max_steps_per_round, deo_server** out);
+/* *rid receives the request id.  DEO_ERR_REJECTED (with *rid set) if its state
+ * is larger than the whole budget. */
+deo_status deo_serve_submit(deo_server* s, const deo_request* r, int64_t* rid);
+/* One round of bookkeeping (see above); call it in the caller's loop. */
+deo_status deo_serve_pump(deo_server* s);
+/* DEO_ERR_NOT_READY while the request runs; DEO_OK once finished: u(T) (and
+ * with want_grad the gradient) copied to uT / grad (host, may be NULL), the
+ * time from submission to completion to *latency_s (may be NULL), and the
+ * request forgotten.  A rejected, cancelled or failed request reports
+ * DEO_ERR_REJECTED, DEO_ERR_BAD_ARG or DEO_ERR_OOM (device memory for its
+ * state could not be allocated) once, and is forgotten too. */
+deo_status deo_serve_poll(deo_server* s, int64_t rid, void* uT, void* grad, double* latency_s);
+/* Withdraws a pending or running request (its memory returns after the rounds
+ * already enqueued); DEO_ERR_BAD_ARG if it has finished. */
+deo_status deo_serve_cancel(deo_server* s, int64_t rid);
+deo_status deo_serve_stats_get(deo_server* s, deo_serve_stats* out);
+/* Test hook: the next n admissions fail as if the device allocation had
+ * failed (the request reports DEO_ERR_OOM; the server goes on). */
+deo_status deo_serve_inject_alloc_failures(deo_server* s, int n);
+/* Waits for the server's work, frees its memory. */
+void deo_serve_destroy(deo_server* s);
+
 /* Autotuner: times candidate (tile, ctas_per_sm) pairs on this batch and
  * keeps the fastest; results are cached per workload signature in the file
  * `cache_path` (NULL = in-process cache only). */
