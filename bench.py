@@ -196,13 +196,33 @@ def fp64_order_bound(achieved_gbs: float, bytes_per_point: float, fp64_per_point
                      f"{sm_mhz:.0f} MHz"}
 
 
-def shard(n: int, rank: int, ws: int) -> range:
-    """Instances (batched / served workloads) owned by `rank`: a contiguous
-    block, sizes differing by at most one.  Ranks run independent replicas of
-    the path; no collective touches the data."""
-    q, r = divmod(n, ws)
-    lo = rank * q + min(rank, r)
-    return range(lo, lo + q + (1 if rank < r else 0))
+def shard(costs, rank: int, ws: int) -> list:
+    """Indices of the instances (batched / served workloads) that `rank` owns,
+    increasing.  Greedy by cost: instances in decreasing cost (ties by index)
+    go to the least loaded rank (ties to the lower rank), so every rank
+    computes the same partition without communicating.  Ranks run independent
+    replicas of the path on their own instances; no collective touches the
+    data."""
+    n = len(costs)
+    if ws == 1:
+        return list(range(n))
+    load, own = [0] * ws, [[] for _ in range(ws)]
+    for i in sorted(range(n), key=lambda i: (-costs[i], i)):
+        r = min(range(ws), key=lambda k: (load[k], k))
+        load[r] += costs[i]
+        own[r].append(i)
+    return sorted(own[rank])
+
+
+def gather_objects(x, ws: int) -> list:
+    """Every rank's `x`, in rank order (host objects; the ranks' results
+    and latencies, never device data)."""
+    if ws == 1:
+        return [x]
+    import torch.distributed as dist
+    out = [None] * ws
+    dist.all_gather_object(out, x)
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -528,22 +548,27 @@ def batch_instances(count=4096, seed=SEED, scale=1.0):
     return [(spec[0], batch_terms(spec)) for spec in batch_specs(count, seed, scale)]
 
 
-def run_batch(args):
+def run_batch(args, ws=1, rank=0):
+    """Config 4.  Under torchrun each rank takes its share of the instances
+    (shard, balanced by points) and runs the same batched passes on them;
+    the times are the max over ranks and the solves/s count every rank's."""
     import torch
 
     import deo
-    inst = batch_instances(scale=args.size_scale)
+    everything = batch_instances(scale=args.size_scale)
+    mine = shard([int(np.prod(s)) for s, _ in everything], rank, ws)
+    inst = [everything[i] for i in mine]
     plans, us, fw, bw, ones = [], [], [], [], []
-    g = torch.Generator(device="cuda").manual_seed(SEED)
-    total = 0
-    for shape, terms in inst:
+    g = torch.Generator(device="cuda")
+    total = sum(int(np.prod(s)) for s, _ in everything)
+    for i, (shape, terms) in zip(mine, inst):
         p = deo.Plan(terms, shape, 0)
         u = deo.julia_array(shape)
+        g.manual_seed(SEED + i)  # an instance's input does not depend on the sharding
         u.copy_(torch.randn(tuple(reversed(shape)), generator=g, device="cuda", dtype=torch.float64).permute(
             *reversed(range(len(shape)))))
         plans.append(p); us.append(u); fw.append(deo.julia_array(shape)); bw.append(deo.julia_array(shape))
         ones.append(deo.julia_array(shape))
-        total += int(np.prod(shape))
     if args.batch_config:  # fixed tile / CTAs per SM (e.g. for profiling), no autotuning
         tile, ctas = (int(v) for v in args.batch_config.split(","))
         bf = deo.Batch(list(zip(plans, us, fw)), tile=tile, ctas_per_sm=ctas)
@@ -572,22 +597,28 @@ def run_batch(args):
         bf1.run_one_launch_each()
         ba1.run_one_launch_each()
 
-    t_b = _event_time(batched, max(3, args.steps // 50), 2)
-    t_1 = _event_time(one_by_one, max(2, args.steps // 200), 1)
-    t_n = _event_time(one_by_one_native, max(2, args.steps // 100), 1)
+    def timed(fn, steps, warmup):
+        barrier(ws)
+        return max_over_ranks(_event_time(fn, steps, warmup), ws)
+
+    t_b = timed(batched, max(3, args.steps // 50), 2)
+    t_1 = timed(one_by_one, max(2, args.steps // 200), 1)
+    t_n = timed(one_by_one_native, max(2, args.steps // 100), 1)
     # the plain per-instance apply: the generic row-table kernel, one launch per instance
     for p in plans:
         p.set_option(deo.DEO_OPT_FAST_PATH, 0)
-    t_p = _event_time(one_by_one_native, max(2, args.steps // 100), 1)
+    t_p = timed(one_by_one_native, max(2, args.steps // 100), 1)
     for p in plans:
         p.set_option(deo.DEO_OPT_FAST_PATH, 1)
     # results agree bit for bit
     torch.cuda.synchronize()
-    same = max(float(((a - b).abs().max() / b.abs().max().clamp_min(1e-300))) for a, b in zip(fw, ones))
+    same = max([0.0] + [float(((a - b).abs().max() / b.abs().max().clamp_min(1e-300))) for a, b in zip(fw, ones)])
+    same = max(gather_objects(same, ws))
     hbm, _ = peaks()
     byts = 2 * 16 * total
     return {"metric": "solves/s (4096 batched forward+adjoint applies)", "workload": "batched_4096_mixed_f64",
-            "value": len(inst) / t_b, "unit": "solves/s", "dtype": "f64", "total_points": total,
+            "value": len(everything) / t_b, "unit": "solves/s", "dtype": "f64", "total_points": total,
+            "n_gpus": ws, "scaling": "strong", "instances_per_rank": gather_objects(len(inst), ws),
             "ms_per_pass": t_b * 1e3,
             "one_launch_per_instance_plain_ms": t_p * 1e3,
             "speedup_vs_one_launch_per_instance_plain": t_p / t_b,
@@ -597,6 +628,10 @@ def run_batch(args):
             "speedup_vs_one_launch_per_instance_python": t_1 / t_b,
             "GBps": byts / t_b / 1e9, "frac_hbm": byts / t_b / 1e9 / hbm, "max_rel_diff_batched_vs_individual": same,
             "autotune_forward": cfg_f, "autotune_adjoint": cfg_a, "gpu_launches_per_pass": 2}
+
+
+def _serve_cost(r):
+    return r.npts * r.K * (2 if r.want_grad else 1)
 
 
 def run_nld(args):
@@ -621,30 +656,44 @@ def run_nld(args):
             "GBps": byts / t / 1e9, "frac_hbm": byts / t / 1e9 / hbm, "gpu_launches_per_apply": 1}
 
 
-def run_serve(args):
+def run_serve(args, ws=1, rank=0):
     """Poisson arrivals (2000 req/s) of MOL advection-diffusion solves served
     by the native loop (deo_serve_*): solves/s, p50/p99 latency; against the
     same requests solved one at a time with one plain apply launch per stage
-    (deo.serve.solve_one_launch_per_instance), the baseline the task names."""
+    (deo.serve.solve_one_launch_per_instance), the baseline the task names.
+    Under torchrun each rank serves its share of the requests (shard,
+    balanced by point-steps) with its own server; the makespan is the max
+    over ranks and the latencies are pooled."""
     import torch
 
     import deo
     from deo.serve import Server, poisson_requests, solve_one_launch_per_instance
-    reqs = poisson_requests(args.requests, 2000.0, seed=SEED, size_scale=args.size_scale,
-                            k_range=(10, args.kmax))
+    everything = poisson_requests(args.requests, 2000.0, seed=SEED, size_scale=args.size_scale,
+                                  k_range=(10, args.kmax))
+    reqs = [everything[i] for i in shard([_serve_cost(r) for r in everything], rank, ws)]
     srv = Server(hbm_budget_bytes=120e9)
+    barrier(ws)
     st = srv.run(reqs)
-    work = sum(r.npts * r.K * (2 if r.want_grad else 1) for r in reqs)
+    lat = [x for part in gather_objects([r.latency for r in reqs if not r.rejected], ws) for x in part]
+    makespan = max_over_ranks(st["makespan_s"], ws)
+    completed = sum(gather_objects(st["completed"], ws))
+    work = sum(_serve_cost(r) for r in everything)
     out = {"metric": "served solves/s (Poisson 2000 req/s, SSP-RK3 MOL)", "workload": "serve_mol_f64",
-           "value": st["solves_per_s"], "unit": "solves/s", "dtype": "f64", "p50_s": st["p50_s"],
-           "p99_s": st["p99_s"], "requests": st["requests"], "completed": st["completed"],
-           "makespan_s": st["makespan_s"], "point_steps": work, "steps": st["ticks"], "rounds": st["rounds"],
-           "launches": st["launches"], "rebuilds": st["rebuilds"], "device_busy_s": st["device_s"],
-           "size_scale": args.size_scale, "kmax": args.kmax}
+           "value": completed / makespan, "unit": "solves/s", "dtype": "f64",
+           "p50_s": float(np.percentile(lat, 50)) if lat else None,
+           "p99_s": float(np.percentile(lat, 99)) if lat else None, "requests": len(everything),
+           "completed": completed, "makespan_s": makespan, "point_steps": work, "steps": st["ticks"],
+           "rounds": st["rounds"], "launches": st["launches"], "rebuilds": st["rebuilds"],
+           "device_busy_s": st["device_s"], "size_scale": args.size_scale, "kmax": args.kmax,
+           "n_gpus": ws, "scaling": "strong"}
     if args.serve_baseline:
         reqs2 = poisson_requests(args.requests, 2000.0, seed=SEED, size_scale=args.size_scale,
                                  k_range=(10, args.kmax))
+        reqs2 = [reqs2[i] for i in shard([_serve_cost(r) for r in reqs2], rank, ws)]
+        barrier(ws)
         base = solve_one_launch_per_instance(reqs2)
+        base["makespan_s"] = max_over_ranks(base["makespan_s"], ws)
+        base["solves_per_s"] = len(everything) / base["makespan_s"]
         # the baseline rounds each stage's combination separately (torch
         # elementwise ops) where the server fuses it into the apply: compare
         # to the state's scale, not bitwise
@@ -653,8 +702,8 @@ def run_serve(args):
             if a.uT is not None and b.uT is not None:
                 dev = max(dev, float(np.abs(a.uT - b.uT).max() / max(1e-300, np.abs(b.uT).max())))
         out["one_launch_per_instance"] = base
-        out["speedup_vs_one_launch_per_instance"] = st["solves_per_s"] / base["solves_per_s"]
-        out["max_rel_diff_vs_baseline"] = dev
+        out["speedup_vs_one_launch_per_instance"] = out["value"] / base["solves_per_s"]
+        out["max_rel_diff_vs_baseline"] = max(gather_objects(dev, ws))
     return out
 
 
@@ -852,11 +901,19 @@ def main():
                     help="plan option DEO_OPT_EXACT_SUMS for the 3-D workload (default: the library's)")
     ap.add_argument("--serial-shell", action="store_true", help="the boundary shell after the interior kernel")
     args = ap.parse_args()
-    if args.workload in ("line1d", "nonuniform2d", "batch", "serve", "nld", "vector", "solve"):
+    if args.workload in ("batch", "serve"):
+        ws, rank, _ = dist_init()
+        line = (run_batch if args.workload == "batch" else run_serve)(args, ws, rank)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.workload in ("line1d", "nonuniform2d", "nld", "vector", "solve"):
         import torch
         torch.cuda.set_device(0)
-        fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "batch": run_batch,
-              "serve": run_serve, "nld": run_nld, "vector": run_vector,
+        fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "nld": run_nld, "vector": run_vector,
               "solve": run_solve}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
