@@ -279,6 +279,11 @@ def run_ours(args, ws, rank):
         us.append(t)
         dus.append(deo.julia_array((n, n, n), tdt, "cuda"))
     stream = torch.cuda.current_stream()
+    # execution choices (tile shape, shell kernel, shell beside the interior or after it), all
+    # bit-identical: timed on this workload by the library's autotuner before the warm-up
+    tuned = None
+    if not getattr(args, "no_autotune", False) and not getattr(args, "serial_shell", False):
+        tuned = plan.autotune(us[0], dus[0], os.path.join(REPORT_DIR, "plan_autotune.cache") if REPORT_DIR else None)
     for i in range(args.warmup):
         plan.apply(us[i % nbuf], dus[i % nbuf])
     torch.cuda.synchronize()
@@ -362,7 +367,8 @@ def run_ours(args, ws, rank):
                    "operator": "CenteredDifference{1,2,3}(2,4,1/257,256) summed",
                    "bc": "RobinBC((1,.5,0),(1,.5,0),h,1) composed on every face",
                    "l2_policy": f"{nbuf} rotating input/output pairs ({nbuf * 2 * npts * esize / 2**30:.2f} GiB) > L2",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU", "kernel_path": path},
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU", "kernel_path": path,
+                   "autotuned": tuned, "autotune_times_us": plan.autotune_times() if tuned else None},
         "e2e": {"value": ws * npts / e2e_s, "unit": "grid-pts/s", "h2d_bytes_per_step": npts * esize,
                 "d2h_bytes_per_step": npts * esize,
                 "path": "deo_apply_host_async + deo_plan_host_sync (C ABI, pinned host buffers, copies overlapped "
@@ -900,6 +906,7 @@ def main():
     ap.add_argument("--exact-sums", type=int, default=-1,
                     help="plan option DEO_OPT_EXACT_SUMS for the 3-D workload (default: the library's)")
     ap.add_argument("--serial-shell", action="store_true", help="the boundary shell after the interior kernel")
+    ap.add_argument("--no-autotune", action="store_true", help="the plan's default execution choices")
     args = ap.parse_args()
     if args.workload in ("batch", "serve"):
         ws, rank, _ = dist_init()

@@ -19,6 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
     "deo_kernels.o": ("nvcc", "deo_kernels.cu"),
     "deo_tma.o": ("nvcc", "deo_tma.cu"),
+    "deo_vec.o": ("nvcc", "deo_vec.cu"),
     "deo_shell.o": ("nvcc", "deo_shell.cu"),
     "deo_static.o": ("nvcc", "deo_static.cu"),
     "deo_vector.o": ("nvcc", "deo_vector.cu"),
@@ -47,7 +48,7 @@ def _stale(obj: str, src: str) -> bool:
         return True
     deps = [src, os.path.join(CSRC, "deo_internal.h"), os.path.join(CSRC, "deo_eval.cuh"),
             os.path.join(CSRC, "deo_rows.cuh"), os.path.join(CSRC, "deo_ptx.cuh"), os.path.join(CSRC, "deo_fx.cuh"),
-            os.path.join(CSRC, "deo_bfx.cuh"),
+            os.path.join(CSRC, "deo_bfx.cuh"), os.path.join(CSRC, "deo_lap.cuh"),
             os.path.join(HERE, "..", "include", "deo.h"),
             os.path.abspath(__file__)]
     t = os.path.getmtime(obj)

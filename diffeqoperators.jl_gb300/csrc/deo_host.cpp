@@ -792,6 +792,9 @@ struct deo_plan {
     int exact_sums = 1;  // DEO_OPT_EXACT_SUMS
     int timing = 0;      // DEO_OPT_LAUNCH_TIMING
     int concurrent = 1;  // DEO_OPT_CONCURRENT_SHELL
+    // the last deo_plan_autotune: per candidate (f32_vec, vcfg, shell kernel, concurrent) its best ms
+    std::vector<int> tune_cands;
+    std::vector<float> tune_ms;
     PlanDev* d_plan = nullptr;  // device copy (batched kernel)
     deo::ShellPlan* d_shell = nullptr;  // device copy of `shell` when shell.ok
     // concurrent shell: a side stream, fork/join events and the interior kernel's unit counter
@@ -1241,6 +1244,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
                 U.fx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
             if (U.fx) U.fx = fx_weights(U.t[0].w, H, nterms, U.fx_w, U.fx_f);
             U.fx_rows = kFxFp64Rows;
+            U.f32_vec = 1;
             // block fixed point: three axes sharing one band
             U.bfx = U.lap && dtype == DEO_F64 && H <= 3 && nterms == 3;
             for (int t = 0; t < nterms && U.bfx; ++t)
@@ -1257,6 +1261,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         CUDA_TRY(cudaMalloc(&P->d_shell, sizeof(deo::ShellPlan)), "cudaMalloc(shell rows)");
         CUDA_TRY(cudaMemcpy(P->d_shell, &P->shell, sizeof(deo::ShellPlan), cudaMemcpyHostToDevice),
                  "cudaMemcpy(shell rows)");
+
         CUDA_TRY(cudaMalloc(&P->d_sched, kSchedSlots * sizeof(unsigned int)), "cudaMalloc(unit counters)");
         CUDA_TRY(cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking), "cudaStreamCreate");
         CUDA_TRY(cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
@@ -1305,6 +1310,7 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
                              ((p->exact_sums == 1 || p->exact_sums == 4) && p->uni.fx)) &&
                             p->uni.radius <= 3;
             const bool conc = p->concurrent && p->side && p->d_shell && (p->dev.dtype == DEO_F32 || fx);
+            const deo::UniPlan* up = &p->uni;
             const char* k = "";
             const char* k2 = "";
             // a counter of its own for this launch (applies of one plan may run on several streams at once)
@@ -1316,25 +1322,25 @@ static int launch_forward(const deo_plan* p, const void* u, void* du, int overwr
                 cudaError_t c = cudaEventRecord(p->ev_fork, st);
                 if (c == cudaSuccess) c = cudaStreamWaitEvent(p->side, p->ev_fork, 0);
                 if (c != cudaSuccess) return (int)c;
-                int e2 = deo_k_apply_shell(&p->uni, &p->shell, p->d_shell, DEO_SHELL_CONCURRENT, p->d_plan,
+                int e2 = deo_k_apply_shell(up, &p->shell, p->d_shell, DEO_SHELL_CONCURRENT, p->d_plan,
                                            p->dev.dtype, u, du, overwrite, p->side, &k2);
                 if (e2) return e2;
                 c = cudaEventRecord(p->ev_join, p->side);
                 if (c != cudaSuccess) return (int)c;
-                const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
+                const int e = deo_k_apply_tma(up, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
                                               stream, &k, sched);
                 mark(p, 1, stream);
                 c = cudaStreamWaitEvent(st, p->ev_join, 0);
                 if (e) return e;  // (cudaErrorNotSupported cannot occur: the tensor-map rules were checked)
                 if (c != cudaSuccess) return (int)c;
             } else {
-                const int e = deo_k_apply_tma(&p->uni, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
+                const int e = deo_k_apply_tma(up, p->d_plan, p->dev.dtype, u, du, overwrite, p->exact_sums,
                                               stream, &k, sched);
                 if (e) return e;
                 mark(p, 1, stream);
-                const int e2 = deo_k_apply_shell(&p->uni, p->d_shell ? &p->shell : nullptr, p->d_shell,
-                                                 DEO_SHELL_ALONE, p->d_plan, p->dev.dtype, u, du, overwrite, stream,
-                                                 &k2);
+                const int e2 = deo_k_apply_shell(up, p->d_shell ? &p->shell : nullptr, p->d_shell,
+                                                 DEO_SHELL_ALONE, p->d_plan, p->dev.dtype, u, du, overwrite,
+                                                 stream, &k2);
                 if (e2) return e2;
             }
             p->last_kernel = k;
@@ -1368,6 +1374,15 @@ extern "C" deo_status deo_plan_set_option(deo_plan* p, int option, int value) {
             if (value < 0 || value > 8) return fail(DEO_ERR_BAD_ARG, "FP64 rows %d not in 0..8", value);
             p->uni.fx_rows = value;
             return DEO_OK;
+        case DEO_OPT_F32_VECTOR: p->uni.f32_vec = value ? 1 : 0; return DEO_OK;
+        case DEO_OPT_F32_TILE:
+            if (value < 0 || value > 3) return fail(DEO_ERR_BAD_ARG, "tile variant %d not in 0..3", value);
+            p->uni.vcfg = value;
+            return DEO_OK;
+        case DEO_OPT_SHELL_KERNEL:
+            if (value < 0 || value > 3) return fail(DEO_ERR_BAD_ARG, "shell kernel %d not in 0..3", value);
+            p->uni.shell_kernel = value;
+            return DEO_OK;
         case DEO_OPT_TEST_WITHHOLD:
             if (value < 0 || value > 64) return fail(DEO_ERR_BAD_ARG, "withheld plane %d not in 0..64", value);
             p->uni.test_withhold = value;
@@ -1391,6 +1406,10 @@ extern "C" int deo_plan_get_option(const deo_plan* p, int option) {
             return p->exact_sums && p->uni.enabled && p->uni.lap && (p->uni.ens || p->uni.fx || p->uni.bfx);
         case DEO_OPT_LAUNCH_TIMING: return p->timing;
         case DEO_OPT_TEST_WITHHOLD: return p->uni.test_withhold;
+        case DEO_OPT_SHELL_KERNEL: return p->uni.shell_kernel;
+        case DEO_OPT_F32_TILE: return p->uni.vcfg;
+        case DEO_OPT_F32_VECTOR:
+            return p->dev.dtype == DEO_F32 && p->uni.enabled && p->uni.lap && p->uni.f32_vec && p->uni.radius <= 3;
         case DEO_OPT_FX_FP64_ROWS:
             return (p->dev.dtype == DEO_F64 && p->uni.enabled && p->uni.lap &&
                     (p->exact_sums == 1 || p->exact_sums == 4 || (p->exact_sums == 5 && !p->uni.bfx)) &&
@@ -1426,10 +1445,11 @@ extern "C" deo_status deo_plan_launch_times(const deo_plan* p, float* ms, int* n
 extern "C" deo_status deo_device_status(unsigned int* status) {
     if (!status) return fail(DEO_ERR_BAD_ARG, "null argument");
     int e = deo_k_read_status(status);
-    unsigned int s2 = 0;
+    unsigned int s2 = 0, s3 = 0;
     if (!e) e = deo_k_read_shell_status(&s2);
+    if (!e) e = deo_k_read_vec_status(&s3);
     if (e) return cuda_fail((cudaError_t)e, "deo_device_status");
-    *status |= s2;
+    *status |= s2 | s3;
     return *status ? fail(DEO_ERR_TIMEOUT, "a bounded device wait gave up (status 0x%x)", *status) : DEO_OK;
 }
 
@@ -2266,6 +2286,142 @@ static std::string batch_signature(const deo_batch& b) {
 
 static std::mutex g_tune_mu;
 static std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+// ---- plan autotuner: execution choices of the Laplacian-type TMA path --------
+// The candidates are bit-identical to each other (they differ in tiling,
+// which kernel evaluates the boundary shell and whether it runs beside the
+// interior); the numerical variant (DEO_OPT_EXACT_SUMS) is the caller's.
+struct PlanTune {
+    int f32_vec, vcfg, shell, conc;
+};
+static std::map<std::string, PlanTune> g_plan_tune;
+
+static std::string plan_signature(const deo_plan& p) {
+    const deo::UniPlan& U = p.uni;
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "lap/%s/%lldx%lldx%lld/t%d/H%d/es%d/bc%d%d%d", p.dev.dtype == DEO_F64 ? "f64" : "f32",
+                  (long long)U.n[0], (long long)U.n[1], (long long)U.n[2], U.nterms, U.radius, p.exact_sums,
+                  p.shell.t[0].bc_kind, p.shell.t[1].bc_kind, p.shell.t[2].bc_kind);
+    return buf;
+}
+
+static void plan_tune_set(deo_plan* p, const PlanTune& c) {
+    p->uni.f32_vec = c.f32_vec;
+    p->uni.vcfg = c.vcfg;
+    p->uni.shell_kernel = c.shell;
+    p->concurrent = c.conc;
+}
+
+extern "C" deo_status deo_plan_autotune(deo_plan* p, const void* u, void* du, const char* cache_path, void* stream) {
+    deo_status s = check_ptrs(p, u, du);
+    if (s != DEO_OK) return s;
+    if (!(p->uni.enabled && p->uni.lap && p->fast_path && p->use_tma && p->d_shell &&
+          deo_k_tma_ok(&p->uni, p->dev.dtype, u)))
+        return DEO_OK;  // nothing to choose: the plan runs one kernel
+    const std::string key = plan_signature(*p);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (cache_path && g_plan_tune.find(key) == g_plan_tune.end()) {
+            if (FILE* f = fopen(cache_path, "r")) {
+                char k[512];
+                PlanTune c;
+                while (fscanf(f, "%511s %d %d %d %d", k, &c.f32_vec, &c.vcfg, &c.shell, &c.conc) == 5)
+                    if (std::strncmp(k, "lap/", 4) == 0) g_plan_tune[k] = c;
+                fclose(f);
+            }
+        }
+        auto it = g_plan_tune.find(key);
+        if (it != g_plan_tune.end()) {
+            plan_tune_set(p, it->second);
+            return DEO_OK;
+        }
+    }
+    std::vector<PlanTune> cand;
+    const bool f32 = p->dev.dtype == DEO_F32;
+    const int nv = f32 ? (p->uni.nterms == 3 ? (p->uni.radius <= 2 ? 4 : 3) : 1) : 0;
+    for (int shell = 1; shell <= 2; ++shell)
+        for (int conc = 1; conc >= 0; --conc) {
+            for (int v = 0; v < nv; ++v) cand.push_back(PlanTune{1, v, shell, conc});
+            cand.push_back(PlanTune{0, 0, shell, conc});  // Float32: the scalar interior; Float64: the plan's kernel
+        }
+    const PlanTune keep{p->uni.f32_vec, p->uni.vcfg, p->uni.shell_kernel, p->concurrent};
+    cand.insert(cand.begin(), keep);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+    CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+    // The clocks up first: the current choice applied for about 50 ms.  Then three rounds over the
+    // candidates (forward, reverse, forward), each timing about 3 ms of applies; a candidate's time is
+    // its best round, and it replaces the current choice only if faster by more than 2 %.
+    int e = 0;
+    float t_one = 0.0f;
+    {
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 5 && !e; ++r) e = launch_forward(p, u, du, 1, stream);
+        cudaEventRecord(e1, st);
+        if (!e && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&t_one, e0, e1);
+        t_one = std::max(t_one / 5.0f, 1e-3f);
+    }
+    for (int r = 0, nw = (int)std::min(2000.0f, 50.0f / t_one); r < nw && !e; ++r)
+        e = launch_forward(p, u, du, 1, stream);
+    const int reps = std::max(5, std::min(200, (int)(3.0f / t_one)));
+    std::vector<float> t(cand.size(), 1e30f);
+    for (int round = 0; round < 3 && !e && s == DEO_OK; ++round)
+        for (size_t i0 = 0; i0 < cand.size() && !e; ++i0) {
+            const size_t i = round == 1 ? cand.size() - 1 - i0 : i0;
+            plan_tune_set(p, cand[i]);
+            for (int r = 0; r < 2 && !e; ++r) e = launch_forward(p, u, du, 1, stream);  // warm-up
+            cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !e; ++r) e = launch_forward(p, u, du, 1, stream);
+            cudaEventRecord(e1, st);
+            if (e) break;
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                s = fail(DEO_ERR_CUDA, "autotune timing failed");
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            t[i] = std::min(t[i], ms / reps);
+        }
+    if (e && s == DEO_OK) s = cuda_fail((cudaError_t)e, "autotune apply");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    p->tune_cands.clear();
+    p->tune_ms.clear();
+    for (size_t i = 0; i < cand.size(); ++i) {
+        p->tune_cands.insert(p->tune_cands.end(), {cand[i].f32_vec, cand[i].vcfg, cand[i].shell, cand[i].conc});
+        p->tune_ms.push_back(t[i]);
+    }
+    PlanTune pick = keep;
+    float best = t[0] * 0.98f;
+    for (size_t i = 1; i < cand.size(); ++i)
+        if (t[i] < best) {
+            best = t[i];
+            pick = cand[i];
+        }
+    plan_tune_set(p, s == DEO_OK ? pick : keep);
+    if (s != DEO_OK) return s;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_plan_tune[key] = pick;
+    if (cache_path) {
+        if (FILE* f = fopen(cache_path, "a")) {
+            fprintf(f, "%s %d %d %d %d\n", key.c_str(), pick.f32_vec, pick.vcfg, pick.shell, pick.conc);
+            fclose(f);
+        }
+    }
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_plan_autotune_times(const deo_plan* p, int* cands, float* ms, int cap, int* n) {
+    if (!p || !n) return fail(DEO_ERR_BAD_ARG, "null argument");
+    *n = (int)p->tune_ms.size();
+    for (int i = 0; i < *n && i < cap; ++i) {
+        if (ms) ms[i] = p->tune_ms[i];
+        if (cands)
+            for (int k = 0; k < 4; ++k) cands[4 * i + k] = p->tune_cands[4 * i + k];
+    }
+    return DEO_OK;
+}
 
 extern "C" deo_status deo_batch_autotune(deo_batch* b, const char* cache_path, void* stream) {
     if (!b) return fail(DEO_ERR_BAD_ARG, "null batch");

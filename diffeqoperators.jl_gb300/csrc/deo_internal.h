@@ -144,6 +144,14 @@ struct UniPlan {
     // copy the kernels withhold, so that its wait runs out (0: none).
     unsigned int wait_polls;
     int test_withhold;
+    // Float32: 1 the vectorised interior kernel (k_lap_v) where the output
+    // allows 16-byte stores, 0 the scalar one (k_lap_q); vcfg its tile
+    // variant (0..3, deo_vec.cu)
+    int f32_vec;
+    int vcfg;
+    // boundary shell kernel: 0 automatic, 1 faces (k_face), 2 lines
+    // (k_shell_lines), 3 one thread per point (k_shell_generic)
+    int shell_kernel;
 };
 
 // Boundary rows of the terms of a Laplacian-type plan (the rows outside each
@@ -297,6 +305,11 @@ extern "C" int deo_k_read_status(unsigned int* status);
 extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
                                  int bz);
 extern "C" int deo_k_read_shell_status(unsigned int* status);
+// Float32 vectorised interior (deo_vec.cu): cudaErrorNotSupported when the
+// plan or the buffers do not fit it (the caller then runs k_lap_q)
+extern "C" int deo_k_apply_vec(const deo::UniPlan* up, unsigned int* sched, const void* u, void* du, int ow,
+                               void* stream);
+extern "C" int deo_k_read_vec_status(unsigned int* status);
 // 1 if deo_k_apply_tma can run on u (tensor-map alignment rules).
 extern "C" int deo_k_tma_ok(const deo::UniPlan* up, int dtype, const void* u);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,

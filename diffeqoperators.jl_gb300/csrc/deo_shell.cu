@@ -502,7 +502,8 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
     // Float64 alone: the line kernel (FP64-bound, full grid).  Otherwise the face kernel: a shared-memory
     // box per tile; beside a Float64 interior kernel in small CTAs that fit next to its CTAs, so that the
     // shell's FP64 work overlaps the interior's integer work.
-    if (have_lines && sizeof(T) == 8 && mode == DEO_SHELL_ALONE) {
+    const int pick = up->shell_kernel;
+    if (have_lines && (pick == 2 || (pick == 0 && sizeof(T) == 8 && mode == DEO_SHELL_ALONE))) {
         ShellLines SL{};
         const int64_t niz = NT == 3 ? iz : 1;
         SL.l2 = NT == 3 ? nx * ny : 0;
@@ -525,7 +526,7 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         *kernel = "k_shell_lines";
         return (int)cudaGetLastError();
     }
-    if (sp && sp_dev) {
+    if (sp && sp_dev && pick != 3) {
         // Float64 interiors are long: a small persistent shell beside them; Float32 interiors are short: a full grid
         const int e = face_launch<T, NT>(up, sp, sp_dev, u, du, ow, st, mode == DEO_SHELL_CONCURRENT && sizeof(T) == 8);
         if (e != (int)cudaErrorNotSupported) {

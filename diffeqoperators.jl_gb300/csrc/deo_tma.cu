@@ -36,6 +36,7 @@
 
 #include "deo_eval.cuh"
 #include "deo_fx.cuh"
+#include "deo_lap.cuh"
 #include "deo_ptx.cuh"
 
 namespace deo {
@@ -111,28 +112,6 @@ struct TmaCfg {
     static constexpr int P = PMIN <= PBASE ? PBASE : 16;  // power of two >= 2H+2
     static constexpr int SMEM = P * SLOT;
 };
-
-// Work unit u = (tile x, tile y, z chunk); a persistent grid of G CTAs takes
-// units b, b + G, b + 2G, ... (static, so one plan may run on several streams
-// at once).  Planes stream through the ring with a running count, so slot and
-// mbarrier phase carry over from one unit to the next.
-struct LapGrid {
-    int tiles_x, tiles_y, chunks, zc;
-    int units;
-    int perm;  // coprime with units: unit k of the round-robin is (k * perm) % units,
-               // so one CTA's units are spread over tile columns and z chunks
-    unsigned int* sched;  // null: static round-robin; else a zeroed device counter the CTAs claim units from
-};
-
-// The next unit of a CTA: with g.sched claimed from the counter (dynamic, so
-// CTAs that share their SM with other work take fewer units), else k_static.
-// Every thread of the CTA calls it (it contains a barrier).
-__device__ __forceinline__ int claim_unit(const LapGrid& g, int& s_next, int k_static) {
-    if (!g.sched) return k_static;
-    if (threadIdx.x == 0 && threadIdx.y == 0) s_next = (int)atomicAdd(g.sched, 1u);
-    __syncthreads();
-    return s_next;
-}
 
 }  // namespace deo
 
@@ -950,63 +929,6 @@ extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, i
                                                                                           : (int)cudaErrorNotSupported;
 }
 
-// Units and z chunk for a persistent grid of G CTAs (see LapGrid).
-static LapGrid make_grid(const UniPlan* up, int tx, int ty, int H, int nt, int64_t G) {
-    const int64_t nx = up->n[0], ny = up->n[1], nz = up->n[2];
-    LapGrid g;
-    g.tiles_x = (int)((nx + tx - 1) / tx);
-    g.tiles_y = (int)((ny + ty - 1) / ty);
-    const int64_t tiles = (int64_t)g.tiles_x * g.tiles_y;
-    g.zc = (int)nz;
-    if (nt == 3) {
-        double best = -1.0;
-        const int zmin = (int)std::min<int64_t>(nz, 12);
-        for (int zc = zmin; zc <= nz; ++zc) {
-            const int64_t chunks = (nz + zc - 1) / zc;
-            const int64_t units = tiles * chunks;
-            const int64_t rounds = (units + G - 1) / G;
-            const double eff = (double)units / (double)(rounds * G) * (double)zc / (double)(zc + 2 * H) *
-                               ((double)nz / (double)(chunks * zc));
-            if (eff > best + 1e-9) {
-                best = eff;
-                g.zc = zc;
-            }
-        }
-    }
-    g.chunks = (int)((nz + g.zc - 1) / g.zc);
-    g.units = (int)(tiles * g.chunks);
-    g.sched = nullptr;
-    g.perm = 1;
-    for (int cand : {7919, 6007, 4099, 2053, 1031, 521, 263, 131, 67, 37, 17}) {
-        int a = cand, b = g.units;
-        while (b) {
-            const int t = a % b;
-            a = b;
-            b = t;
-        }
-        if (a == 1 && cand < g.units) {
-            g.perm = cand;
-            break;
-        }
-    }
-    return g;
-}
-
-template <typename K>
-static int occupancy_grid(K kernel, int threads, int smem, int64_t& G) {
-    static thread_local int dummy = 0;
-    (void)dummy;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return (int)e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-    G = (int64_t)sms * per_sm;
-    return 0;
-}
-
 template <typename T, int H, int NT, bool ENS>
 static int launch_tma(const UniPlan* up, const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st) {
     using C = TmaCfg<T, H>;
@@ -1199,6 +1121,7 @@ extern "C" int deo_k_apply_tma(const UniPlan* up, const PlanDev* dp, int dtype, 
             DEO_TRY_KERNEL((launch_tma_h<double, true>(up, dp, u, du, overwrite, st)), "k_lap_tma(exact sums v1)");
         DEO_TRY_KERNEL((launch_q_h<double>(up, sched, u, du, overwrite, st)), "k_lap_q");
     } else {
+        if (up->f32_vec) DEO_TRY_KERNEL((deo_k_apply_vec(up, sched, u, du, overwrite, st)), "k_lap_v");
         DEO_TRY_KERNEL((launch_q_h<float>(up, sched, u, du, overwrite, st)), "k_lap_q");
     }
     return (int)cudaErrorNotSupported;

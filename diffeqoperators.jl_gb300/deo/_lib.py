@@ -21,6 +21,9 @@ DEO_PATH_AUTO, DEO_PATH_PADDED, DEO_PATH_GENERIC = 0, 1, 2
 DEO_OPT_FAST_PATH, DEO_OPT_TMA, DEO_OPT_EXACT_SUMS, DEO_OPT_LAUNCH_TIMING, DEO_OPT_CONCURRENT_SHELL = 1, 2, 3, 4, 5
 DEO_OPT_FX_FP64_ROWS = 6
 DEO_OPT_TEST_WITHHOLD = 7
+DEO_OPT_F32_VECTOR = 8
+DEO_OPT_SHELL_KERNEL = 9
+DEO_OPT_F32_TILE = 10
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)
@@ -164,6 +167,9 @@ def lib():
     proto("deo_batch_config", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64))
     proto("deo_batch_destroy", None, _vp)
     proto("deo_batch_autotune", st, _vp, C.c_char_p, _vp)
+    proto("deo_plan_autotune", st, _vp, _vp, _vp, C.c_char_p, _vp)
+    proto("deo_plan_autotune_times", st, _vp, C.POINTER(C.c_int), C.POINTER(C.c_float), C.c_int,
+          C.POINTER(C.c_int))
     proto("deo_serve_create", st, C.c_size_t, C.c_int, C.c_int, C.POINTER(_vp))
     proto("deo_serve_submit", st, _vp, C.POINTER(Request), C.POINTER(C.c_int64))
     proto("deo_serve_pump", st, _vp)
@@ -199,7 +205,7 @@ EXPORTED = [
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_serve_create", "deo_serve_submit", "deo_serve_pump", "deo_serve_poll", "deo_serve_cancel", "deo_serve_stats_get",
     "deo_serve_inject_alloc_failures", "deo_serve_destroy",
-    "deo_batch_autotune", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply", "deo_vector_calculus_info",
+    "deo_batch_autotune", "deo_plan_autotune", "deo_plan_autotune_times", "deo_vector_calculus_plan", "deo_vector_calculus_sizes", "deo_vector_calculus_apply", "deo_vector_calculus_info",
     "deo_vector_calculus_destroy", "deo_dot_product", "deo_cross_product", "deo_square_norm",
     "deo_solve_plan", "deo_solve_bands", "deo_solve_apply", "deo_solve_destroy",
     "deo_padded_plan", "deo_padded_plan_view", "deo_padded_apply", "deo_padded_destroy",

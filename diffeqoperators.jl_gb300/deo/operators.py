@@ -843,6 +843,27 @@ class Plan:
         lib = L.lib()
         return tuple(k.decode() for k in (lib.deo_plan_kernels(self._h, 0), lib.deo_plan_kernels(self._h, 1)) if k)
 
+    def autotune(self, u, du, cache_path: str | None = None) -> dict:
+        """deo_plan_autotune: time the bit-identical execution choices of a
+        Laplacian-type TMA plan on u -> du (du is overwritten) and keep the
+        fastest; returns the chosen options."""
+        self._check(u, du)
+        check(L.lib().deo_plan_autotune(self._h, C.c_void_p(u.data_ptr()), C.c_void_p(du.data_ptr()),
+                                        cache_path.encode() if cache_path else None, _stream_ptr()))
+        return {"f32_vector": self.get_option(L.DEO_OPT_F32_VECTOR), "f32_tile": self.get_option(L.DEO_OPT_F32_TILE),
+                "shell_kernel": self.get_option(L.DEO_OPT_SHELL_KERNEL),
+                "concurrent_shell": self.get_option(L.DEO_OPT_CONCURRENT_SHELL)}
+
+    def autotune_times(self) -> list:
+        """[((f32_vector, f32_tile, shell_kernel, concurrent_shell), us per apply), ...] of the last
+        autotune (empty when it came from the cache)."""
+        n = C.c_int()
+        check(L.lib().deo_plan_autotune_times(self._h, None, None, 0, C.byref(n)))
+        cands = (C.c_int * (4 * n.value))()
+        ms = (C.c_float * n.value)()
+        check(L.lib().deo_plan_autotune_times(self._h, cands, ms, n.value, C.byref(n)))
+        return [(tuple(cands[4 * i:4 * i + 4]), round(ms[i] * 1e3, 2)) for i in range(n.value)]
+
     def launch_times(self) -> list:
         """Device ms of each launch of the last forward apply (needs
         set_option(DEO_OPT_LAUNCH_TIMING, 1) before that apply)."""

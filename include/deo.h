@@ -235,6 +235,18 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
  *     for that copy runs out: the kernel sets its device status bit, waits for
  *     its other copies in flight and returns, leaving its points unwritten.
  *     deo_device_status then reports DEO_ERR_TIMEOUT.  Nothing faults.
+ *   DEO_OPT_F32_VECTOR: Float32 Laplacian-type plans on the TMA path with
+ *     band radius <= 3: 1 (default) evaluates the interior with each thread
+ *     on 4 consecutive x points (16-byte shared-memory loads and stores, when
+ *     du is 16-byte aligned), 0 one point per thread; the two are
+ *     bit-identical to each other and to the generic kernel.
+ *   DEO_OPT_F32_TILE: 0..3, the vectorised kernel's tile (threads along y x
+ *     rows per thread): 0 (default) 16 x 2, 1 8 x 2, 2 16 x 1, 3 8 x 4 (band
+ *     radius <= 2; else as 0); two-axis plans use 0.
+ *   DEO_OPT_SHELL_KERNEL: the boundary-shell kernel of those plans: 0
+ *     (default) automatic, 1 face tiles staged by TMA, 2 one thread per
+ *     (line, end), 3 one thread per point; all in the reference's order
+ *     (bit-identical to the generic kernel).
  * No reference counterpart (execution choices only). */
 #define DEO_OPT_FAST_PATH 1
 #define DEO_OPT_TMA 2
@@ -243,6 +255,9 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
 #define DEO_OPT_CONCURRENT_SHELL 5
 #define DEO_OPT_FX_FP64_ROWS 6
 #define DEO_OPT_TEST_WITHHOLD 7
+#define DEO_OPT_F32_VECTOR 8
+#define DEO_OPT_SHELL_KERNEL 9
+#define DEO_OPT_F32_TILE 10
 deo_status deo_plan_set_option(deo_plan* plan, int option, int value);
 /* 1 if the option is set AND applies to this plan, 0 if not, -1 on error. */
 int deo_plan_get_option(const deo_plan* plan, int option);
@@ -521,6 +536,22 @@ deo_status deo_serve_inject_alloc_failures(deo_server* s, int n);
 /* Waits for the server's work, frees its memory. */
 void deo_serve_destroy(deo_server* s);
 
+/* Plan autotuner for Laplacian-type plans on the TMA path: times the
+ * bit-identical execution choices (Float32: scalar or vectorised interior and
+ * its tile; the boundary-shell kernel; the shell beside the interior or after
+ * it) with overwriting applies u -> du on `stream`, keeps the fastest in the
+ * plan's options (DEO_OPT_F32_VECTOR, DEO_OPT_F32_TILE, DEO_OPT_SHELL_KERNEL,
+ * DEO_OPT_CONCURRENT_SHELL), and caches it per (sizes, dtype, terms, band
+ * radius, exact-sums variant, boundary kinds) in the file `cache_path`
+ * (NULL = in-process only).  Other plans: nothing to choose, DEO_OK.
+ * Writes du.  No reference counterpart. */
+deo_status deo_plan_autotune(deo_plan* plan, const void* u, void* du, const char* cache_path, void* stream);
+/* What the last deo_plan_autotune on this plan timed (nothing when it took
+ * its choice from the cache): *n candidates, the first the plan's choice
+ * before it; candidate i is cands[4i .. 4i+3] = (DEO_OPT_F32_VECTOR,
+ * DEO_OPT_F32_TILE, DEO_OPT_SHELL_KERNEL, DEO_OPT_CONCURRENT_SHELL) and
+ * ms[i] its best time per apply; at most cap are written. */
+deo_status deo_plan_autotune_times(const deo_plan* plan, int* cands, float* ms, int cap, int* n);
 /* Autotuner: times candidate (tile, ctas_per_sm) pairs on this batch and
  * keeps the fastest; results are cached per workload signature in the file
  * `cache_path` (NULL = in-process cache only). */
