@@ -42,10 +42,13 @@ __device__ __noinline__ T ghost_line(const TermDev& t, const T* __restrict__ lin
     return d + T(left ? q[3] : q[4]);
 }
 
-template <typename T>
+// LBC: the plan has per-line boundary conditions (PlanDev::has_lbc); the
+// kernels are instantiated with and without that branch, so that plans
+// without them carry no call to ghost_line.
+template <typename T, bool LBC = false>
 __device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ line, int64_t base) {
     const int64_t s = t.stride;
-    if (t.lbc) return ghost_line<T>(t, line, base, true);
+    if (LBC && t.lbc) return ghost_line<T>(t, line, base, true);
     if (t.bc_kind == 1) return t.periodic_nd ? line[0] : line[(int64_t)(t.len - 1) * s];
     if (t.bc_kind == 2) return line[-s];  // padded input: the ghost is stored before the line
     T d = T(0);
@@ -53,10 +56,10 @@ __device__ __forceinline__ T ghost_left(const TermDev& t, const T* __restrict__ 
     return d + T(t.bl);
 }
 
-template <typename T>
+template <typename T, bool LBC = false>
 __device__ __forceinline__ T ghost_right(const TermDev& t, const T* __restrict__ line, int64_t base) {
     const int64_t s = t.stride;
-    if (t.lbc) return ghost_line<T>(t, line, base, false);
+    if (LBC && t.lbc) return ghost_line<T>(t, line, base, false);
     if (t.bc_kind == 1) return t.periodic_nd ? line[(int64_t)(t.len - 1) * s] : line[0];
     if (t.bc_kind == 2) return line[(int64_t)t.len * s];  // padded input: the ghost is stored after the line
     T d = T(0);
@@ -119,7 +122,7 @@ __device__ __forceinline__ const RowTabDev& row_variant(const TermDev& t, int64_
 }
 
 // One term, one output row: the reference's per-point tap loop.
-template <typename T>
+template <typename T, bool LBC = false>
 __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u, int64_t idx, int i) {
     const int64_t s = t.stride;
     const int64_t base = idx - (int64_t)(i - 1) * s;
@@ -142,8 +145,8 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
         return acc;
     }
     T gl = T(0), gr = T(0);
-    if (r.p0 == 1) gl = ghost_left<T>(t, line, base);
-    if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T>(t, line, base);
+    if (r.p0 == 1) gl = ghost_left<T, LBC>(t, line, base);
+    if (r.p0 + r.nk - 1 == L2) gr = ghost_right<T, LBC>(t, line, base);
     auto tap = [&](int k) {
         const int p = r.p0 + k;
         return (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
@@ -208,12 +211,12 @@ __device__ __forceinline__ T adj_column(const TermDev& t, const T* __restrict__ 
     return acc;
 }
 
-template <typename T>
+template <typename T, bool LBC = false>
 __device__ __forceinline__ T adj_term(const TermDev& t, const T* __restrict__ d, int64_t idx, int j) {
     const int64_t base = idx - (int64_t)(j - 1) * t.stride;
     const int L = t.len;
     T w = adj_column<T>(t, d, base, j + 1);
-    if (t.lbc) {  // this line's own BC
+    if (LBC && t.lbc) {  // this line's own BC
         const double* q = line_bc(t, base);
         if (q[0] != 0.0) {  // periodic line: the left ghost is u[len], the right u[1]
             if (j == L) w += adj_column<T>(t, d, base, 1);
@@ -250,12 +253,12 @@ __device__ __forceinline__ int term_row(const PlanDev& P, const TermDev& t, int6
     return (int)((idx / t.stride) % t.len) + 1;
 }
 
-template <typename T, bool ADJ>
+template <typename T, bool ADJ, bool LBC = false>
 __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ u, int64_t idx) {
     auto term = [&](int tt) {
         const TermDev& t = P.t[tt];
         const int i = term_row(P, t, idx);
-        return ADJ ? adj_term<T>(t, u, idx, i) : eval_term<T>(t, u, idx, i);
+        return ADJ ? adj_term<T, LBC>(t, u, idx, i) : eval_term<T, LBC>(t, u, idx, i);
     };
     T acc = term(0);  // the first term as is, then the others added left to right
     for (int tt = 1; tt < P.nterms; ++tt) acc = acc + term(tt);

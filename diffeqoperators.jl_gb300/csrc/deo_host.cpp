@@ -1169,6 +1169,7 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             if ((ls = upload(*P, lrec, reinterpret_cast<const void**>(&T.lbc))) != DEO_OK) return ls;
             T.lbc_stride = 5 + 2 * lmw;
             T.lbc_mw = lmw;
+            D.has_lbc = 1;
         }
         if (t < 3) {
             deo::ShellTerm& S = P->shell.t[t];
@@ -1277,6 +1278,7 @@ extern "C" void deo_plan_destroy(deo_plan* p) { delete p; }
 extern "C" const PlanDev* deo_plan_device_copy(const deo_plan* p) { return p->d_plan; }
 extern "C" int64_t deo_plan_points(const deo_plan* p) { return p->dev.total; }
 extern "C" int deo_plan_dtype_code(const deo_plan* p) { return p->dev.dtype; }
+extern "C" int deo_plan_has_lbc(const deo_plan* p) { return p->dev.has_lbc; }
 extern "C" deo_status deo_set_error(deo_status s, const char* msg) { return fail(s, "%s", msg); }
 extern "C" size_t deo_plan_table_bytes(const deo_plan* p) { return p ? p->table_bytes : 0; }
 
@@ -2093,6 +2095,7 @@ struct deo_batch {
     std::vector<deo::InstDev> inst;
     std::vector<const deo_plan*> plans;
     int adjoint = 0, dtype = 0;
+    int lbc = 0;  // some plan has per-line boundary conditions
     int tile = 0, ctas = 0;
     int64_t n_items = 0;
     deo::InstDev* d_inst = nullptr;
@@ -2152,6 +2155,7 @@ extern "C" deo_status deo_batch_create(int n, const deo_instance* in, int adjoin
             return fail(DEO_ERR_BAD_ARG, "all instances of a batch must share one dtype");
         b->plans.push_back(in[i].plan);
         b->inst.push_back(deo::InstDev{in[i].plan->d_plan, in[i].u, in[i].du});
+        b->lbc |= in[i].plan->dev.has_lbc;
     }
     b->dtype = n > 0 ? in[0].plan->dev.dtype : 0;
     if (n > 0) {
@@ -2179,8 +2183,10 @@ extern "C" deo_status deo_apply_each(int n, const deo_instance* in, int adjoint,
 
 static deo_status batch_launch(deo_batch& b, cudaStream_t st) {
     const int e = b.kind == 1
-                      ? deo_k_stage_batch(b.d_stages, b.d_items, b.n_items, b.d_counter, b.dtype, b.ctas, 256, st)
-                      : deo_k_batch(b.d_inst, b.d_items, b.n_items, b.d_counter, b.dtype, b.adjoint, b.ctas, 256, st);
+                      ? deo_k_stage_batch(b.d_stages, b.d_items, b.n_items, b.d_counter, b.lbc, b.dtype, b.ctas, 256,
+                                          st)
+                      : deo_k_batch(b.d_inst, b.d_items, b.n_items, b.d_counter, b.dtype, b.adjoint, b.lbc, b.ctas,
+                                    256, st);
     if (e) return cuda_fail((cudaError_t)e, "batched launch");
     return DEO_OK;
 }
@@ -2202,6 +2208,7 @@ extern "C" deo_status deo_stage_batch_create(int n, const deo_stage* in, int til
         b->plans.push_back(s.plan);
         b->stages.push_back(deo::StageDev{s.plan->d_plan, s.a, s.b, s.c, s.out, s.alpha, s.beta, s.gamma, s.dt,
                                           s.adjoint ? 1 : 0, 0});
+        b->lbc |= s.plan->dev.has_lbc;
     }
     b->dtype = n > 0 ? in[0].plan->dev.dtype : 0;
     if (n > 0) {

@@ -86,6 +86,7 @@ struct PlanDev {
     int nterms;
     int dtype;           // 0 f64, 1 f32
     int fastdiv;         // total < 2^31: row indices by FastDiv instead of 64-bit division
+    int has_lbc;         // some term has per-line boundary conditions (TermDev::lbc)
     int64_t sizes[8];
     int64_t total;
     TermDev t[DEO_KMAX_TERMS];
@@ -268,8 +269,10 @@ extern "C" int deo_k_scale(void* x, int64_t n, int dtype, double f, void* stream
 // Commits k_batch's module image and launch resources on the current device
 // (one empty launch of each instantiation; *counter is bumped, nothing else).
 extern "C" int deo_k_batch_prepare(unsigned int* counter, void* stream);
+// lbc: some instance's plan has per-line boundary conditions (the kernel
+// instantiation with that branch)
 extern "C" int deo_k_batch(const deo::InstDev* inst, const deo::WorkItem* items, int64_t n_items,
-                           unsigned int* counter, int dtype, int adjoint, int ctas_per_sm, int threads,
+                           unsigned int* counter, int dtype, int adjoint, int lbc, int ctas_per_sm, int threads,
                            void* stream);
 extern "C" int deo_k_num_sms(void);
 // nonlinear_diffusion! on padded vectors p, q (length len+2): term k-1 of the
@@ -313,4 +316,5 @@ extern "C" int deo_k_read_vec_status(unsigned int* status);
 // 1 if deo_k_apply_tma can run on u (tensor-map alignment rules).
 extern "C" int deo_k_tma_ok(const deo::UniPlan* up, int dtype, const void* u);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,
-                                 unsigned int* counter, int dtype, int ctas_per_sm, int threads, void* stream);
+                                 unsigned int* counter, int lbc, int dtype, int ctas_per_sm, int threads,
+                                 void* stream);

@@ -19,12 +19,12 @@
 
 namespace deo {
 
-template <typename T, bool ADJ>
+template <typename T, bool ADJ, bool LBC>
 __global__ void __launch_bounds__(256) k_apply(const __grid_constant__ PlanDev P, const T* __restrict__ u,
                                                T* __restrict__ du, int overwrite) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= P.total) return;
-    const T r = eval_point<T, ADJ>(P, u, idx);
+    const T r = eval_point<T, ADJ, LBC>(P, u, idx);
     du[idx] = overwrite ? r : r + du[idx];
 }
 
@@ -49,7 +49,7 @@ __device__ __forceinline__ const PlanDev& stage_plan(PlanCache& c, const PlanDev
     return *reinterpret_cast<const PlanDev*>(c.words);
 }
 
-template <typename T, bool ADJ>
+template <typename T, bool ADJ, bool LBC>
 __global__ void __launch_bounds__(256) k_batch(const InstDev* __restrict__ inst, const WorkItem* __restrict__ items,
                                                int64_t n_items, unsigned int* counter) {
     __shared__ int64_t s_item;
@@ -69,14 +69,14 @@ __global__ void __launch_bounds__(256) k_batch(const InstDev* __restrict__ inst,
         T* __restrict__ du = reinterpret_cast<T*>(in.du);
         for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
             const int64_t idx = w.start + q;
-            du[idx] = eval_point<T, ADJ>(P, u, idx);
+            du[idx] = eval_point<T, ADJ, LBC>(P, u, idx);
         }
     }
 }
 
 // Batched Runge-Kutta stage: same work-list scheme; each instance may run
 // the forward operator or its adjoint (uniform per work item).
-template <typename T>
+template <typename T, bool LBC>
 __global__ void __launch_bounds__(256) k_stage(const StageDev* __restrict__ st, const WorkItem* __restrict__ items,
                                                int64_t n_items, unsigned int* counter) {
     __shared__ int64_t s_item;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_stage(const StageDev* __restrict__ st, 
         const T al = T(S.alpha), be = T(S.beta), ga = T(S.gamma), dt = T(S.dt);
         for (int q = threadIdx.x; q < w.count; q += blockDim.x) {
             const int64_t idx = w.start + q;
-            const T f = S.adjoint ? eval_point<T, true>(P, c, idx) : eval_point<T, false>(P, c, idx);
+            const T f = S.adjoint ? eval_point<T, true, LBC>(P, c, idx) : eval_point<T, false, LBC>(P, c, idx);
             const T t = fma(dt, f, c[idx]);
             T acc = a ? al * a[idx] : T(0);
             if (b) acc = fma(be, b[idx], acc);
@@ -167,6 +167,7 @@ extern "C" int deo_k_scale(void* x, int64_t n, int dtype, double f, void* stream
 }
 
 extern "C" int deo_k_stage_batch(const StageDev* st, const WorkItem* items, int64_t n_items, unsigned int* counter,
+                                 int lbc,
                                  int dtype, int ctas_per_sm, int threads, void* stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const int sms = deo_k_num_sms();
@@ -175,8 +176,13 @@ extern "C" int deo_k_stage_batch(const StageDev* st, const WorkItem* items, int6
     if (grid <= 0) return 0;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return (int)e;
-    if (dtype == 0) k_stage<double><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
-    else k_stage<float><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+    if (dtype == 0) {
+        if (lbc) k_stage<double, true><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+        else k_stage<double, false><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+    } else {
+        if (lbc) k_stage<float, true><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+        else k_stage<float, false><<<(unsigned)grid, threads, 0, s>>>(st, items, n_items, counter);
+    }
     return (int)cudaGetLastError();
 }
 
@@ -185,16 +191,17 @@ extern "C" int deo_k_apply(const PlanDev* p, const void* u, void* du, int overwr
     const int64_t blocks = (p->total + threads - 1) / threads;
     if (blocks == 0) return 0;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto go = [&](auto kernel, const auto* in, auto* out) {
+        kernel<<<(unsigned)blocks, threads, 0, st>>>(*p, in, out, overwrite);
+    };
+    const double* ud = (const double*)u;
+    const float* uf = (const float*)u;
     if (p->dtype == 0) {
-        if (adjoint)
-            k_apply<double, true><<<(unsigned)blocks, threads, 0, st>>>(*p, (const double*)u, (double*)du, overwrite);
-        else
-            k_apply<double, false><<<(unsigned)blocks, threads, 0, st>>>(*p, (const double*)u, (double*)du, overwrite);
+        if (p->has_lbc) adjoint ? go(k_apply<double, true, true>, ud, (double*)du) : go(k_apply<double, false, true>, ud, (double*)du);
+        else adjoint ? go(k_apply<double, true, false>, ud, (double*)du) : go(k_apply<double, false, false>, ud, (double*)du);
     } else {
-        if (adjoint)
-            k_apply<float, true><<<(unsigned)blocks, threads, 0, st>>>(*p, (const float*)u, (float*)du, overwrite);
-        else
-            k_apply<float, false><<<(unsigned)blocks, threads, 0, st>>>(*p, (const float*)u, (float*)du, overwrite);
+        if (p->has_lbc) adjoint ? go(k_apply<float, true, true>, uf, (float*)du) : go(k_apply<float, false, true>, uf, (float*)du);
+        else adjoint ? go(k_apply<float, true, false>, uf, (float*)du) : go(k_apply<float, false, false>, uf, (float*)du);
     }
     return (int)cudaGetLastError();
 }
@@ -206,7 +213,7 @@ extern "C" int deo_k_num_sms(void) {
     return n;
 }
 
-// Loads the four k_batch instantiations onto the current device and runs each
+// Loads the k_batch instantiations onto the current device and runs each
 // once over an empty work-list (one CTA; it only bumps *counter), so that the
 // module image and the resources a launch of them takes are committed now:
 // with lazy module loading (the CUDA default) that would otherwise happen at
@@ -214,20 +221,25 @@ extern "C" int deo_k_num_sms(void) {
 extern "C" int deo_k_batch_prepare(unsigned int* counter, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaFuncAttributes a;
-    cudaError_t e = cudaFuncGetAttributes(&a, k_batch<double, false>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<double, true>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<float, false>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_batch<float, true>);
+    cudaError_t e = cudaSuccess;
+    auto prep = [&](auto kernel) {
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, kernel);
+        if (e == cudaSuccess) kernel<<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
+    };
+    prep(k_batch<double, false, false>);
+    prep(k_batch<double, true, false>);
+    prep(k_batch<float, false, false>);
+    prep(k_batch<float, true, false>);
+    prep(k_batch<double, false, true>);
+    prep(k_batch<double, true, true>);
+    prep(k_batch<float, false, true>);
+    prep(k_batch<float, true, true>);
     if (e != cudaSuccess) return (int)e;
-    k_batch<double, false><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
-    k_batch<double, true><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
-    k_batch<float, false><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
-    k_batch<float, true><<<1, 256, 0, st>>>(nullptr, nullptr, 0, counter);
     return (int)cudaGetLastError();
 }
 
 extern "C" int deo_k_batch(const InstDev* inst, const WorkItem* items, int64_t n_items, unsigned int* counter,
-                           int dtype, int adjoint, int ctas_per_sm, int threads, void* stream) {
+                           int dtype, int adjoint, int lbc, int ctas_per_sm, int threads, void* stream) {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int sms = deo_k_num_sms();
     int64_t grid = (int64_t)sms * (ctas_per_sm > 0 ? ctas_per_sm : 4);
@@ -235,12 +247,13 @@ extern "C" int deo_k_batch(const InstDev* inst, const WorkItem* items, int64_t n
     if (grid <= 0) return 0;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return (int)e;
+    auto go = [&](auto kernel) { kernel<<<(unsigned)grid, threads, 0, st>>>(inst, items, n_items, counter); };
     if (dtype == 0) {
-        if (adjoint) k_batch<double, true><<<(unsigned)grid, threads, 0, st>>>(inst, items, n_items, counter);
-        else k_batch<double, false><<<(unsigned)grid, threads, 0, st>>>(inst, items, n_items, counter);
+        if (lbc) adjoint ? go(k_batch<double, true, true>) : go(k_batch<double, false, true>);
+        else adjoint ? go(k_batch<double, true, false>) : go(k_batch<double, false, false>);
     } else {
-        if (adjoint) k_batch<float, true><<<(unsigned)grid, threads, 0, st>>>(inst, items, n_items, counter);
-        else k_batch<float, false><<<(unsigned)grid, threads, 0, st>>>(inst, items, n_items, counter);
+        if (lbc) adjoint ? go(k_batch<float, true, true>) : go(k_batch<float, false, true>);
+        else adjoint ? go(k_batch<float, true, false>) : go(k_batch<float, false, false>);
     }
     return (int)cudaGetLastError();
 }

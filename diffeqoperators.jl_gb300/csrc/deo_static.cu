@@ -28,6 +28,7 @@
 extern "C" const deo::PlanDev* deo_plan_device_copy(const deo_plan* p);
 extern "C" int64_t deo_plan_points(const deo_plan* p);
 extern "C" int deo_plan_dtype_code(const deo_plan* p);
+extern "C" int deo_plan_has_lbc(const deo_plan* p);
 extern "C" deo_status deo_set_error(deo_status s, const char* msg);
 
 namespace {
@@ -102,7 +103,7 @@ deo_status prepare(int dev, cudaStream_t st, unsigned char** base) {
 extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, int adjoint, int tile, void* stream) {
     if (n < 0 || (n > 0 && !inst)) return deo_set_error(DEO_ERR_BAD_ARG, "null or negative instance list");
     const int64_t t = tile > 0 ? tile : 8192;
-    int dtype = -1;
+    int dtype = -1, lbc = 0;
     int64_t items = 0;
     for (int i = 0; i < n; ++i) {
         if (!inst[i].plan || !inst[i].u || !inst[i].du)
@@ -111,6 +112,7 @@ extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, i
         const int dt = deo_plan_dtype_code(inst[i].plan);
         if (dtype >= 0 && dt != dtype) return deo_set_error(DEO_ERR_BAD_ARG, "all instances must share one dtype");
         dtype = dt;
+        lbc |= deo_plan_has_lbc(inst[i].plan);
         items += (deo_plan_points(inst[i].plan) + t - 1) / t;
     }
     const size_t inst_off = kCounterBytes;
@@ -145,7 +147,7 @@ extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, i
     if (e != cudaSuccess) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString(e));
     const int r = deo_k_batch(reinterpret_cast<const deo::InstDev*>(base + inst_off),
                               reinterpret_cast<const deo::WorkItem*>(base + item_off), m,
-                              reinterpret_cast<unsigned int*>(base), dtype, adjoint ? 1 : 0, 4, 256, st);
+                              reinterpret_cast<unsigned int*>(base), dtype, adjoint ? 1 : 0, lbc, 4, 256, st);
     if (r) return deo_set_error(DEO_ERR_CUDA, cudaGetErrorString((cudaError_t)r));
     return DEO_OK;
 }
