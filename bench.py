@@ -503,6 +503,14 @@ def run_nonuniform2d(args):
     res["fused_ms"] = t * 1e3
     res["fused_GBps"] = 24 * n * n / t / 1e9
     res["fused_frac_hbm"] = res["fused_GBps"] / hbm
+    # DEO_PLAN_MERGE_TERMS: D1x + D2x and D1y + D2y each evaluated as one term (5 terms -> 3)
+    pm = deo.plan_for(ops, (n, n), 0, merge_terms=True)
+    om = deo.julia_array((n, n))
+    tm = _event_time(lambda: pm.apply(ud, om), args.steps, args.warmup)
+    torch.cuda.synchronize()
+    res["fused_merged_ms"] = tm * 1e3
+    res["fused_merged_terms"] = pm.evaluated_terms
+    res["fused_merged_max_rel_diff"] = float((om - outs[1]).abs().max() / outs[1].abs().max())
     return res
 
 

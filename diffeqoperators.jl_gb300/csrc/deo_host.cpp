@@ -710,14 +710,14 @@ struct HostTab {
     std::vector<double> W;  // [nw][nexp]
 };
 
-static deo_status compile_table(const deo_operator& A, int mode, bool scaled, double sgn, HostTab& T,
-                                std::vector<int>& rlo, std::vector<int>& rhi) {
-    const long len = A.len;
+// The table of rows i = 1..len given by `row(i)`.
+template <typename Row>
+static deo_status compile_rows(long len, Row row, HostTab& T, std::vector<int>& rlo, std::vector<int>& rhi) {
     // pass 1: longest run of identical rows -> band
     long best_lo = 1, best_len = 0, run_lo = 1;
-    RowSpec prev = build_row(A, mode, scaled, sgn, 1);
+    RowSpec prev = row(1);
     for (long i = 1; i <= len; ++i) {
-        RowSpec cur = (i == 1) ? prev : build_row(A, mode, scaled, sgn, i);
+        RowSpec cur = (i == 1) ? prev : row(i);
         if (cur.p0 < 1 || cur.p0 + cur.nk - 1 > len + 2 || cur.nk < 1)
             return fail(DEO_ERR_BAD_SHAPE, "row %ld of the operator reads outside the padded line (len %ld too short)",
                         i, len);
@@ -736,7 +736,7 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
     if (best_len >= 2) {
         d.ilo = (int)best_lo;
         d.ihi = (int)(best_lo + best_len - 1);
-        RowSpec b = build_row(A, mode, scaled, sgn, best_lo);
+        RowSpec b = row(best_lo);
         d.band_p0_off = (int)(b.p0 - best_lo);
         d.band_cidx_off = (int)(b.cidx - best_lo);
         d.band_nk = b.nk;
@@ -750,7 +750,7 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
     std::vector<RowSpec> ex;
     for (long i = 1; i <= len; ++i) {
         if (i >= d.ilo && i <= d.ihi) continue;
-        ex.push_back(build_row(A, mode, scaled, sgn, i));
+        ex.push_back(row(i));
         nw = std::max(nw, ex.back().nk);
     }
     d.nexp = (int)ex.size();
@@ -762,6 +762,33 @@ static deo_status compile_table(const deo_operator& A, int mode, bool scaled, do
         for (int k = 0; k < ex[e].nk; ++k) T.W[(size_t)k * ex.size() + e] = ex[e].w[k];
     }
     return DEO_OK;
+}
+
+static deo_status compile_table(const deo_operator& A, int mode, bool scaled, double sgn, HostTab& T,
+                                std::vector<int>& rlo, std::vector<int>& rhi) {
+    return compile_rows(A.len, [&](long i) { return build_row(A, mode, scaled, sgn, i); }, T, rlo, rhi);
+}
+
+// Row i of a sum of terms on one axis with one boundary condition: the
+// union of their windows, the weights of each padded position added in the
+// terms' order (a position a term does not read contributes nothing).
+// nk = 0 when the union is wider than DEO_MAX_NW.
+static RowSpec merge_row(const RowSpec& a, const RowSpec& b) {
+    RowSpec r;
+    r.p0 = std::min(a.p0, b.p0);
+    const int end = std::max(a.p0 + a.nk, b.p0 + b.nk);
+    r.nk = end - r.p0;
+    r.cidx = a.cidx;
+    if (r.nk > DEO_MAX_NW) {
+        r.nk = 0;
+        return r;
+    }
+    for (int k = 0; k < r.nk; ++k) {
+        const int p = r.p0 + k;
+        const bool ia = p >= a.p0 && p < a.p0 + a.nk, ib = p >= b.p0 && p < b.p0 + b.nk;
+        r.w[k] = ia && ib ? a.w[p - a.p0] + b.w[p - b.p0] : (ia ? a.w[p - a.p0] : b.w[p - b.p0]);
+    }
+    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -1035,8 +1062,24 @@ static bool bfx_weights(const double* w, int H, deo::UniPlan& U) {
     return true;
 }
 
+static bool same_bc(const deo_bc& a, const deo_bc& b) {
+    if (a.kind != b.kind) return false;
+    if (a.kind == DEO_BC_PERIODIC) return true;
+    if (a.m_l != b.m_l || a.m_r != b.m_r || a.b_l != b.b_l || a.b_r != b.b_r) return false;
+    for (int j = 0; j < a.m_l; ++j)
+        if (a.a_l[j] != b.a_l[j]) return false;
+    for (int j = 0; j < a.m_r; ++j)
+        if (a.a_r[j] != b.a_r[j]) return false;
+    return true;
+}
+
 extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms,
                                       const deo_term* terms, deo_plan** out) {
+    return deo_plan_create_opts(ndims, sizes, dtype, nterms, terms, 0, out);
+}
+
+extern "C" deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms,
+                                           const deo_term* terms, int flags, deo_plan** out) {
     if (!out || !sizes || !terms) return fail(DEO_ERR_BAD_ARG, "null argument");
     *out = nullptr;
     if (ndims < 1 || ndims > DEO_MAX_DIMS) return fail(DEO_ERR_BAD_SHAPE, "ndims must be 1..%d", DEO_MAX_DIMS);
@@ -1055,6 +1098,40 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
     }
     D.total = total;
     D.fastdiv = total < (1LL << 31) ? 1 : 0;
+    // DEO_PLAN_MERGE_TERMS: a term on the same axis as an earlier one, with the same boundary condition
+    // and path, no coefficient field and no per-line BCs, joins it (lead[t] = that term) when every
+    // row's union window fits DEO_MAX_NW taps; the plan then has fewer terms
+    std::vector<int> lead(nterms, -1), eff(nterms, 0);
+    if (flags & DEO_PLAN_MERGE_TERMS) {
+        auto joinable = [&](const deo_term& a, const deo_term& b) {
+            if (!a.op || !b.op || !a.bc || !b.bc || a.line_bcs || b.line_bcs || a.coeff_field || b.coeff_field)
+                return false;
+            if (a.axis != b.axis || a.path != b.path || a.op->len != b.op->len || !same_bc(*a.bc, *b.bc)) return false;
+            const int md = a.path == DEO_PATH_PADDED ? 1 : a.path == DEO_PATH_GENERIC ? 0 : (ndims == 1 ? 1 : 0);
+            for (long i = 1; i <= a.op->len; ++i) {
+                const RowSpec ra = build_row(*a.op, md, true, 1.0, i), rb = build_row(*b.op, md, true, 1.0, i);
+                if (ra.nk < 1 || rb.nk < 1 || merge_row(ra, rb).nk < 1) return false;
+            }
+            return true;
+        };
+        for (int t = 1; t < nterms; ++t)
+            for (int s = 0; s < t; ++s) {
+                if (lead[s] >= 0) continue;
+                // the union of every member so far must stay within DEO_MAX_NW: check against each
+                bool ok = joinable(terms[s], terms[t]);
+                for (int m = s + 1; m < t && ok; ++m)
+                    if (lead[m] == s) ok = joinable(terms[m], terms[t]);
+                if (ok) {
+                    lead[t] = s;
+                    break;
+                }
+            }
+    }
+    {
+        int ne = 0;
+        for (int t = 0; t < nterms; ++t) eff[t] = lead[t] < 0 ? ne++ : eff[lead[t]];
+        D.nterms = ne;
+    }
     for (int t = 0; t < nterms; ++t) {
         const deo_term& tm = terms[t];
         if (tm.path < DEO_PATH_AUTO || tm.path > DEO_PATH_GENERIC)
@@ -1128,7 +1205,8 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             return fail(DEO_ERR_BAD_SHAPE, "term %d: len %d < 2*boundary_point_count+1", t + 1, A.len);
         if (A.wind && A.len < 2 * A.bpc + A.off)
             return fail(DEO_ERR_BAD_SHAPE, "term %d: len %d too short for the upwind boundary rows", t + 1, A.len);
-        TermDev& T = D.t[t];
+        if (lead[t] >= 0) continue;  // joined an earlier term (its rows are in that term's table)
+        TermDev& T = D.t[eff[t]];
         T.axis = ax;
         T.len = A.len;
         int64_t stride = 1;
@@ -1142,11 +1220,23 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         T.field = tm.coeff_field;
         T.nvar = (T.has_field && A.wind) ? 2 : 1;
         std::vector<int> rlo(A.len + 2, A.len + 1), rhi(A.len + 2, 0);
+        std::vector<const deo_operator*> members{&A};
+        for (int m = t + 1; m < nterms; ++m)
+            if (lead[m] == t) members.push_back(terms[m].op);
         for (int v = 0; v < T.nvar; ++v) {
             HostTab H;
-            deo_status s = compile_table(A, mode, !T.has_field, v == 0 ? 1.0 : -1.0, H, rlo, rhi);
+            deo_status s;
+            if (members.size() == 1) {
+                s = compile_table(A, mode, !T.has_field, v == 0 ? 1.0 : -1.0, H, rlo, rhi);
+            } else {
+                s = compile_rows(A.len, [&](long i) {
+                    RowSpec r = build_row(*members[0], mode, true, 1.0, i);
+                    for (size_t m = 1; m < members.size(); ++m) r = merge_row(r, build_row(*members[m], mode, true, 1.0, i));
+                    return r;
+                }, H, rlo, rhi);
+            }
             if (s != DEO_OK) return s;
-            if (v == 0) shell_rows(H, A.len, dtype, t, P->shell);
+            if (v == 0) shell_rows(H, A.len, dtype, eff[t], P->shell);
             if ((s = upload_tab(*P, H, dtype, T.tab[v])) != DEO_OK) return s;
         }
         for (int p = 0; p < A.len + 2; ++p)
@@ -1171,8 +1261,8 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             T.lbc_mw = lmw;
             D.has_lbc = 1;
         }
-        if (t < 3) {
-            deo::ShellTerm& S = P->shell.t[t];
+        if (eff[t] < 3) {
+            deo::ShellTerm& S = P->shell.t[eff[t]];
             S.bc_kind = T.bc_kind;
             S.periodic_nd = T.periodic_nd;
             S.ml = T.ml;
@@ -1191,14 +1281,14 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
             }
         }
     }
-    P->shell.ok = P->shell.ok >= 0 && nterms <= 3 ? 1 : 0;
+    P->shell.ok = P->shell.ok >= 0 && D.nterms <= 3 ? 1 : 0;
     // fast path for 2-D/3-D plans whose terms all have constant interior rows
     {
         deo::UniPlan& U = P->uni;
         bool ok = (ndims == 2 || ndims == 3) && sizes[0] < (1LL << 30) && sizes[1] < (1LL << 30) &&
                   (ndims < 3 || sizes[2] < (1LL << 30));
         int H = 0;
-        for (int t = 0; t < nterms && ok; ++t) {
+        for (int t = 0; t < D.nterms && ok; ++t) {
             const TermDev& T = D.t[t];
             const RowTabDev& tb = T.tab[0];
             if (T.has_field || T.nvar != 1 || tb.ilo > tb.ihi || T.axis > 2 || T.lbc) {
@@ -1218,14 +1308,14 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
         if (ok && H >= 1 && H <= 4) {
             U.enabled = 1;
             U.radius = H;
-            U.nterms = nterms;
+            U.nterms = D.nterms;
             // centred-band specialisation: term t on axis t, 2H+1 taps from -H
-            U.lap = (nterms == ndims);
-            for (int t = 0; t < nterms && U.lap; ++t)
+            U.lap = (D.nterms == ndims);
+            for (int t = 0; t < D.nterms && U.lap; ++t)
                 U.lap = U.t[t].axis == t && U.t[t].nk == 2 * H + 1 && U.t[t].off0 == -H;
             // exact neighbour sums: Float64, one band shared by every term
             U.ens = U.lap && dtype == DEO_F64;
-            for (int t = 0; t < nterms && U.ens; ++t)
+            for (int t = 0; t < D.nterms && U.ens; ++t)
                 U.ens = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
             for (int k = 0; k < 2 * H + 1 && U.ens; ++k)
                 U.ens = k == H || std::fpclassify(U.t[0].w[k]) == FP_NORMAL;  // scaled through their exponents
@@ -1240,15 +1330,15 @@ extern "C" deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype
                 for (int k = 0; k < 2 * H + 1; ++k) U.ens_w[k] = U.t[0].w[k];  // weight at offset k - H
             }
             // fixed-point evaluation: the same shared band, as exact integers on one exponent
-            U.fx = U.lap && dtype == DEO_F64 && H <= 3 && (nterms == 2 || nterms == 3);
-            for (int t = 0; t < nterms && U.fx; ++t)
+            U.fx = U.lap && dtype == DEO_F64 && H <= 3 && (D.nterms == 2 || D.nterms == 3);
+            for (int t = 0; t < D.nterms && U.fx; ++t)
                 U.fx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
-            if (U.fx) U.fx = fx_weights(U.t[0].w, H, nterms, U.fx_w, U.fx_f);
+            if (U.fx) U.fx = fx_weights(U.t[0].w, H, D.nterms, U.fx_w, U.fx_f);
             U.fx_rows = kFxFp64Rows;
             U.f32_vec = 1;
             // block fixed point: three axes sharing one band
-            U.bfx = U.lap && dtype == DEO_F64 && H <= 3 && nterms == 3;
-            for (int t = 0; t < nterms && U.bfx; ++t)
+            U.bfx = U.lap && dtype == DEO_F64 && H <= 3 && D.nterms == 3;
+            for (int t = 0; t < D.nterms && U.bfx; ++t)
                 U.bfx = std::memcmp(U.t[t].w, U.t[0].w, sizeof(double) * (2 * H + 1)) == 0;
             if (U.bfx) U.bfx = bfx_weights(U.t[0].w, H, U);
             for (int k = 0; k < 3; ++k) U.n[k] = k < ndims ? sizes[k] : 1;
@@ -1279,6 +1369,7 @@ extern "C" const PlanDev* deo_plan_device_copy(const deo_plan* p) { return p->d_
 extern "C" int64_t deo_plan_points(const deo_plan* p) { return p->dev.total; }
 extern "C" int deo_plan_dtype_code(const deo_plan* p) { return p->dev.dtype; }
 extern "C" int deo_plan_has_lbc(const deo_plan* p) { return p->dev.has_lbc; }
+extern "C" int deo_plan_terms(const deo_plan* p) { return p ? p->dev.nterms : -1; }
 extern "C" deo_status deo_set_error(deo_status s, const char* msg) { return fail(s, "%s", msg); }
 extern "C" size_t deo_plan_table_bytes(const deo_plan* p) { return p ? p->table_bytes : 0; }
 

@@ -755,7 +755,7 @@ class Plan:
     """A compiled deo_plan for (terms, Julia size, dtype)."""
 
     def __init__(self, ghosts: Sequence[GhostDerivativeOperator], shape: Sequence[int], dtype_code: int,
-                 path: int = L.DEO_PATH_AUTO):
+                 path: int = L.DEO_PATH_AUTO, merge_terms: bool = False):
         nd = len(shape)
         terms = (Term * len(ghosts))()
         self._keep = []
@@ -795,7 +795,8 @@ class Plan:
                 terms[i].coeff_field = None
         sizes = (C.c_int64 * nd)(*self.shape)
         h = C.c_void_p()
-        check(L.lib().deo_plan_create(nd, sizes, dtype_code, len(ghosts), terms, C.byref(h)))
+        check(L.lib().deo_plan_create_opts(nd, sizes, dtype_code, len(ghosts), terms,
+                                           L.DEO_PLAN_MERGE_TERMS if merge_terms else 0, C.byref(h)))
         self._h = h
         self._ops = [g.L for g in ghosts]  # keep operators alive
 
@@ -810,6 +811,11 @@ class Plan:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def evaluated_terms(self) -> int:
+        """Terms evaluated per point (after DEO_PLAN_MERGE_TERMS)."""
+        return int(L.lib().deo_plan_terms(self._h))
 
     def table_bytes(self) -> int:
         return int(L.lib().deo_plan_table_bytes(self._h))
@@ -926,13 +932,13 @@ class Plan:
 _plan_cache: dict = {}
 
 
-def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO) -> Plan:
+def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO, merge_terms: bool = False) -> Plan:
     key = (tuple(id(g) for g in ghosts), tuple(shape), dtype_code, path,
-           tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts))
+           tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts), merge_terms)
     versions = tuple(g.L._version for g in ghosts)
     p = _plan_cache.get(key)
     if p is None or p._versions != versions:  # a plan of earlier coefficient values is replaced
-        p = Plan(ghosts, shape, dtype_code, path)
+        p = Plan(ghosts, shape, dtype_code, path, merge_terms)
         p._versions = versions
         # keep the ghosts alive with the plan so ids stay unique
         p._ghosts = list(ghosts)

@@ -180,10 +180,26 @@ typedef struct {
 
 deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
                            deo_plan** out);
+/* deo_plan_create with flags:
+ *   DEO_PLAN_MERGE_TERMS: terms on one axis with the same boundary condition
+ *     and path, without coefficient fields or per-line BCs, are evaluated as
+ *     one term whose row i has the union of their windows and, at each padded
+ *     position, the sum of their weights (added in the terms' order, rounded
+ *     once; row widths up to 16).  Each merged row then takes one tap per
+ *     position instead of one per term and position, and the result differs
+ *     from the reference's term-by-term sums by rounding only: within the
+ *     same 4 ulp of sum |c_k u_k| (the weights' rounding adds at most half an
+ *     ulp of each merged weight times its value).  No reference counterpart. */
+#define DEO_PLAN_MERGE_TERMS 1
+deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
+                                int flags, deo_plan** out);
 /* Frees the plan's device tables, streams and events (cudaFree waits for the device). */
 void deo_plan_destroy(deo_plan* plan);
 /* Device bytes held by the plan's tables. */
 size_t deo_plan_table_bytes(const deo_plan* plan);
+/* Terms the plan evaluates per point (fewer than it was given when
+ * DEO_PLAN_MERGE_TERMS joined some); -1 for a null plan. */
+int deo_plan_terms(const deo_plan* plan);
 /* Plan options (defaults 1 unless stated):
  *   DEO_OPT_FAST_PATH: Laplacian-type 2-D/3-D plans (term t a centred band on
  *     axis t) use the tiled TMA kernels below for interior points; 0 forces

@@ -66,6 +66,12 @@ def test_nonuniform_2048_fused_and_per_operator_against_oracle(cuda):
     p.apply(ud, out)
     ref = O.apply(oterms, u, nthreads=NTHREADS)
     worst["fused"] = _ulps(to_host(out), ref, O.abs_scale(oterms, u))
+    # the same terms with D1 + D2 merged per axis (DEO_PLAN_MERGE_TERMS): against the oracle's
+    # term-by-term sums, same bar
+    pm = deo.plan_for(ops, (n, n), 0, merge_terms=True)
+    assert pm.evaluated_terms == 3
+    pm.apply(ud, out)
+    worst["fused_merged"] = _ulps(to_host(out), ref, O.abs_scale(oterms, u))
     assert deo.device_status() == 0
     _report("parity_nonuniform2d_2048", {"max_ulp_of_scale": worst})
     assert max(worst.values()) <= 4.0, worst
