@@ -864,6 +864,33 @@ def run_solve(args):
             "cpu_baseline": cpu, "gpu_launches_per_solve": 1}
 
 
+def run_adjoint(args):
+    """The transposed apply (deo_apply_adjoint, the rrule's pullback) of the
+    256^3 Float64 Robin Laplacian, rotating buffers larger than L2."""
+    import torch
+
+    import deo
+    n = args.n
+    AQ, plan, tdt = lap3d_setup(n, "f64")
+    g = torch.Generator(device="cuda").manual_seed(SEED)
+    pairs = []
+    for _ in range(3):
+        v = deo.julia_array((n, n, n), tdt)
+        v.copy_(torch.randn((n, n, n), generator=g, device="cuda", dtype=tdt))
+        pairs.append((v, deo.julia_array((n, n, n), tdt)))
+    k = [0]
+
+    def step():
+        v, ub = pairs[k[0] % 3]
+        k[0] += 1
+        plan.adjoint(v, ub)
+    t = _event_time(step, args.steps, args.warmup)
+    hbm, _ = peaks()
+    return {"metric": "grid-pts/s (adjoint of the 256^3 Laplacian apply)", "workload": "adjoint_lap3d_256_f64",
+            "value": n ** 3 / t, "unit": "grid-pts/s", "dtype": "f64", "ms": t * 1e3,
+            "GBps": 16 * n ** 3 / t / 1e9, "frac_hbm": 16 * n ** 3 / t / 1e9 / hbm, "kernel": "k_apply (adjoint)"}
+
+
 def run_secondary(args):
     """The other benchmark configurations, run after the headline and attached
     to its line (each bounded to a few seconds of timed work):
@@ -888,6 +915,7 @@ def run_secondary(args):
 
     sub("lap3d_f32", lambda a: run_ours(a, 1, 0), workload="lap3d_f32", steps=300, warmup=10, no_cpu=True)
     sub("line1d", run_line1d, steps=2000, warmup=50)
+    sub("adjoint", run_adjoint, steps=30, warmup=3)
     sub("nonuniform2d", run_nonuniform2d, steps=50, warmup=5)
     sub("batch", run_batch, steps=150, warmup=3, size_scale=1.0, batch_config="")
     sub("serve", run_serve, requests=args.requests, size_scale=args.size_scale, kmax=args.kmax,
@@ -902,7 +930,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="lap3d",
-                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld", "vector", "solve"])
+                    choices=["lap3d", "lap3d_f32", "line1d", "nonuniform2d", "batch", "serve", "nld", "vector", "solve",
+                             "adjoint"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--requests", type=int, default=64)
@@ -925,11 +954,11 @@ def main():
             import torch.distributed as dist
             dist.destroy_process_group()
         return
-    if args.workload in ("line1d", "nonuniform2d", "nld", "vector", "solve"):
+    if args.workload in ("line1d", "nonuniform2d", "nld", "vector", "solve", "adjoint"):
         import torch
         torch.cuda.set_device(0)
         fn = {"line1d": run_line1d, "nonuniform2d": run_nonuniform2d, "nld": run_nld, "vector": run_vector,
-              "solve": run_solve}[args.workload]
+              "solve": run_solve, "adjoint": run_adjoint}[args.workload]
         print(json.dumps(fn(args)), flush=True)
         return
     if args.warmup < 3:

@@ -20,6 +20,7 @@ SOURCES = {
     "deo_kernels.o": ("nvcc", "deo_kernels.cu"),
     "deo_tma.o": ("nvcc", "deo_tma.cu"),
     "deo_vec.o": ("nvcc", "deo_vec.cu"),
+    "deo_concretize.o": ("nvcc", "deo_concretize.cu"),
     "deo_shell.o": ("nvcc", "deo_shell.cu"),
     "deo_static.o": ("nvcc", "deo_static.cu"),
     "deo_vector.o": ("nvcc", "deo_vector.cu"),

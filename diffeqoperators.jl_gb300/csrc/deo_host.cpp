@@ -2123,57 +2123,82 @@ extern "C" deo_status deo_solve_apply(const deo_solve* s, const void* u, void* x
 
 extern "C" void deo_solve_destroy(deo_solve* s) { delete s; }
 
+extern "C" deo_status deo_plan_concretize_device(const deo_plan* p, double* Al, double* Ab, void* stream) {
+    if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");
+    const int64_t n = p->dev.total;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CUDA_TRY(cudaMemsetAsync(Al, 0, (size_t)n * (size_t)n * sizeof(double), st), "cudaMemsetAsync");
+    const int e = deo_k_concretize(&p->dev, 0, Al, Ab, 0, 0, nullptr, nullptr, stream);
+    if (e == (int)cudaErrorNotSupported) return fail(DEO_ERR_UNSUPPORTED, "plan reads ghosts stored around its lines");
+    if (e) return cuda_fail((cudaError_t)e, "concretize");
+    return DEO_OK;
+}
+
 extern "C" deo_status deo_plan_concretize(const deo_plan* p, double* Al, double* Ab) {
     if (!p || !Al || !Ab) return fail(DEO_ERR_BAD_ARG, "null argument");
     const int64_t n = p->dev.total;
-    if (n > 8192) return fail(DEO_ERR_UNSUPPORTED, "concretisation is for checking operators with <= 8192 points");
-    if (p->dev.dtype != DEO_F64) return fail(DEO_ERR_UNSUPPORTED, "concretisation needs a Float64 plan");
-    const int64_t B = std::min<int64_t>(n + 1, 256);
-    double *dU = nullptr, *dD = nullptr;
-    CUDA_TRY(cudaMalloc(&dU, (size_t)(n * B) * 8), "cudaMalloc");
-    if (cudaMalloc(&dD, (size_t)(n * B) * 8) != cudaSuccess) {
-        cudaFree(dU);
-        return fail(DEO_ERR_OOM, "cudaMalloc");
+    if (n > (1LL << 31) / 8) return fail(DEO_ERR_UNSUPPORTED, "n x n too large for a dense matrix; use the banded form");
+    const size_t bytes = (size_t)n * (size_t)n * sizeof(double);
+    size_t fr = 0, tot = 0;
+    CUDA_TRY(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    if (bytes + (size_t)n * 8 > fr / 10 * 9) return fail(DEO_ERR_OOM, "dense A_l needs %zu bytes of device memory", bytes);
+    cudaStream_t st = nullptr;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    double *dA = nullptr, *dB = nullptr;
+    deo_status s = DEO_OK;
+    if (cudaMallocAsync(&dA, bytes, st) != cudaSuccess || cudaMallocAsync(&dB, (size_t)n * 8, st) != cudaSuccess) {
+        s = fail(DEO_ERR_OOM, "cudaMallocAsync");
+    } else {
+        s = deo_plan_concretize_device(p, dA, dB, st);
+        if (s == DEO_OK && (cudaMemcpyAsync(Al, dA, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                            cudaMemcpyAsync(Ab, dB, (size_t)n * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess))
+            s = fail(DEO_ERR_CUDA, "D2H");
     }
-    std::vector<double> hU((size_t)(n * B)), hD((size_t)(n * B));
-    std::vector<double> col0(n);
-    deo_status st = DEO_OK;
-    // column j = -1 is the zero vector (gives A_b); columns 0..n-1 unit vectors
-    for (int64_t j0 = -1; j0 < n && st == DEO_OK; j0 += B) {
-        const int64_t nb = std::min<int64_t>(B, n - j0);
-        std::fill(hU.begin(), hU.end(), 0.0);
-        for (int64_t b = 0; b < nb; ++b)
-            if (j0 + b >= 0) hU[(size_t)(b * n + j0 + b)] = 1.0;
-        if (cudaMemcpy(dU, hU.data(), (size_t)(n * nb) * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
-            st = fail(DEO_ERR_CUDA, "H2D");
-            break;
-        }
-        for (int64_t b = 0; b < nb; ++b) {
-            const int e = deo_k_apply(&p->dev, dU + b * n, dD + b * n, 1, 0, nullptr);
-            if (e) {
-                st = cuda_fail((cudaError_t)e, "concretize launch");
-                break;
-            }
-        }
-        if (st != DEO_OK) break;
-        if (cudaMemcpy(hD.data(), dD, (size_t)(n * nb) * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
-            st = fail(DEO_ERR_CUDA, "D2H");
-            break;
-        }
-        for (int64_t b = 0; b < nb; ++b) {
-            const int64_t j = j0 + b;
-            const double* c = &hD[(size_t)(b * n)];
-            if (j < 0) {
-                std::copy(c, c + n, col0.begin());
-                std::copy(c, c + n, Ab);
-            } else {
-                for (int64_t i = 0; i < n; ++i) Al[(size_t)(j * n + i)] = c[i] - col0[i];
-            }
-        }
-    }
-    cudaFree(dU);
-    cudaFree(dD);
-    return st;
+    if (dA) cudaFreeAsync(dA, st);
+    if (dB) cudaFreeAsync(dB, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (s == DEO_OK && e != cudaSuccess) s = cuda_fail(e, "concretize");
+    return s;
+}
+
+extern "C" deo_status deo_plan_bandwidths(const deo_plan* p, int64_t* l, int64_t* u, void* stream) {
+    if (!p || !l || !u) return fail(DEO_ERR_BAD_ARG, "null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned long long* d = nullptr;
+    CUDA_TRY(cudaMallocAsync(&d, 2 * sizeof(unsigned long long), st), "cudaMallocAsync");
+    unsigned long long h[2] = {0, 0};
+    cudaError_t c = cudaMemsetAsync(d, 0, sizeof h, st);
+    int e = c == cudaSuccess ? deo_k_concretize(&p->dev, 2, nullptr, nullptr, 0, 0, d, nullptr, stream) : (int)c;
+    if (!e) e = (int)cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (!e) e = (int)cudaStreamSynchronize(st);
+    if (e == (int)cudaErrorNotSupported) return fail(DEO_ERR_UNSUPPORTED, "plan reads ghosts stored around its lines");
+    if (e) return cuda_fail((cudaError_t)e, "bandwidths");
+    *l = (int64_t)h[0];
+    *u = (int64_t)h[1];
+    return DEO_OK;
+}
+
+extern "C" deo_status deo_plan_concretize_banded(const deo_plan* p, int64_t l, int64_t u, double* data, double* Ab,
+                                                 void* stream) {
+    if (!p || !data || !Ab || l < 0 || u < 0) return fail(DEO_ERR_BAD_ARG, "null argument or negative bandwidth");
+    const int64_t n = p->dev.total;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int* flag = nullptr;
+    CUDA_TRY(cudaMallocAsync(&flag, sizeof(int), st), "cudaMallocAsync");
+    cudaError_t c = cudaMemsetAsync(flag, 0, sizeof(int), st);
+    if (c == cudaSuccess) c = cudaMemsetAsync(data, 0, (size_t)(l + u + 1) * (size_t)n * sizeof(double), st);
+    int e = c == cudaSuccess ? deo_k_concretize(&p->dev, 1, data, Ab, l, u, nullptr, flag, stream) : (int)c;
+    int hf = 0;
+    if (!e) e = (int)cudaMemcpyAsync(&hf, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(flag, st);
+    if (!e) e = (int)cudaStreamSynchronize(st);
+    if (e == (int)cudaErrorNotSupported) return fail(DEO_ERR_UNSUPPORTED, "plan reads ghosts stored around its lines");
+    if (e) return cuda_fail((cudaError_t)e, "concretize (banded)");
+    if (hf) return fail(DEO_ERR_BAD_SHAPE, "an entry of A_l lies outside the bands (%lld, %lld)", (long long)l,
+                        (long long)u);
+    return DEO_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -313,6 +313,10 @@ extern "C" int deo_k_read_shell_status(unsigned int* status);
 extern "C" int deo_k_apply_vec(const deo::UniPlan* up, unsigned int* sched, const void* u, void* du, int ow,
                                void* stream);
 extern "C" int deo_k_read_vec_status(unsigned int* status);
+// Device concretisation from the plan's tables (deo_concretize.cu): mode 0
+// dense, 1 banded (l, u; *flag set for an entry outside), 2 bandwidths into lu
+extern "C" int deo_k_concretize(const deo::PlanDev* p, int mode, double* A, double* Ab, int64_t l, int64_t u,
+                                unsigned long long* lu, int* flag, void* stream);
 // 1 if deo_k_apply_tma can run on u (tensor-map alignment rules).
 extern "C" int deo_k_tma_ok(const deo::UniPlan* up, int dtype, const void* u);
 extern "C" int deo_k_stage_batch(const deo::StageDev* st, const deo::WorkItem* items, int64_t n_items,

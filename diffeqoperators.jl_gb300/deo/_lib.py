@@ -162,6 +162,9 @@ def lib():
     proto("deo_plan_host_sync", st, _vp)
     proto("deo_apply_adjoint", st, _vp, _vp, _vp, C.c_int, _vp)
     proto("deo_plan_concretize", st, _vp, _dp, _dp)
+    proto("deo_plan_concretize_device", st, _vp, _vp, _vp, _vp)
+    proto("deo_plan_bandwidths", st, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _vp)
+    proto("deo_plan_concretize_banded", st, _vp, C.c_int64, C.c_int64, _vp, _vp, _vp)
     proto("deo_batch_create", st, C.c_int, C.POINTER(Instance), C.c_int, C.c_int, C.c_int, C.POINTER(_vp))
     proto("deo_stage_batch_create", st, C.c_int, C.POINTER(Stage), C.c_int, C.c_int, C.POINTER(_vp))
     proto("deo_batch_run", st, _vp, C.c_int, _vp)
@@ -205,7 +208,8 @@ EXPORTED = [
     "deo_operator_destroy", "deo_operator_array", "deo_operator_banded", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
     "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_create_opts", "deo_plan_terms", "deo_plan_destroy",
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_nonlinear_diffusion_plan", "deo_nonlinear_diffusion",
-    "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize",
+    "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize", "deo_plan_concretize_device", "deo_plan_bandwidths",
+    "deo_plan_concretize_banded",
     "deo_batch_create", "deo_stage_batch_create", "deo_batch_run", "deo_apply_each", "deo_batch_apply_noalloc", "deo_batch_set_buffers", "deo_batch_config", "deo_batch_destroy",
     "deo_serve_create", "deo_serve_submit", "deo_serve_pump", "deo_serve_poll", "deo_serve_cancel", "deo_serve_stats_get",
     "deo_serve_inject_alloc_failures", "deo_serve_destroy",

@@ -922,11 +922,29 @@ class Plan:
         check(L.lib().deo_plan_host_sync(self._h))
 
     def concretize(self):
+        """(A_l, A_b) of du = A_l u + A_b, dense, built on the device from the plan's tables."""
         n = int(np.prod(self.shape))
         Al = np.zeros((n, n), order="F")
         Ab = np.zeros(n)
         check(L.lib().deo_plan_concretize(self._h, Al.ctypes.data_as(_dp), _ptr(Ab)))
         return Al, Ab
+
+    def bandwidths(self) -> tuple:
+        lo, up = C.c_int64(), C.c_int64()
+        check(L.lib().deo_plan_bandwidths(self._h, C.byref(lo), C.byref(up), _stream_ptr()))
+        return lo.value, up.value
+
+    def concretize_banded(self):
+        """BandedMatrix(L*Q) on the device: (l, u, data, A_b) with data the (l+u+1) x n band storage
+        (entry (i, j) at row u+i-j of column j) and A_b, both device tensors."""
+        torch = _torch()
+        lo, up = self.bandwidths()
+        n = int(np.prod(self.shape))
+        data = torch.empty((n, lo + up + 1), dtype=torch.float64, device="cuda").t()  # column-major
+        ab = torch.empty(n, dtype=torch.float64, device="cuda")
+        check(L.lib().deo_plan_concretize_banded(self._h, lo, up, C.c_void_p(data.data_ptr()),
+                                                 C.c_void_p(ab.data_ptr()), _stream_ptr()))
+        return lo, up, data, ab
 
 
 _plan_cache: dict = {}

@@ -96,7 +96,11 @@ def advection_diffusion(shape, nu, c, approx_order=2):
 
 class Server:
     def __init__(self, hbm_budget_bytes: float = 120e9, max_steps_per_round: int = 64,
-                 inject_alloc_failures: int = 0):
+                 inject_alloc_failures: int = 0, merge_terms: bool = True):
+        """merge_terms: build each request's plan with DEO_PLAN_MERGE_TERMS
+        (the diffusion and advection terms along axis 1 share the boundary
+        condition, so they are evaluated as one tap set)."""
+        self.merge_terms = merge_terms
         h = C.c_void_p()
         check(L.lib().deo_serve_create(int(hbm_budget_bytes), 0, int(max_steps_per_round), C.byref(h)))
         self._h = h
@@ -117,7 +121,7 @@ class Server:
 
     def submit(self, req: Request, t0: float) -> bool:
         A = advection_diffusion(req.shape, req.nu, req.c, req.approx_order)
-        plan = Plan(A.terms(), req.shape, 0)
+        plan = Plan(A.terms(), req.shape, 0, merge_terms=self.merge_terms)
         u0 = req.initial()
         q = L.Request(plan.handle, C.c_void_p(u0.ctypes.data), int(req.K), float(req.dt()), int(bool(req.want_grad)))
         rid = C.c_int64()

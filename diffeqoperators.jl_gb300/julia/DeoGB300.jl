@@ -393,6 +393,25 @@ function Base.:*(A::CurlOperator{T}, M::CuArray{T, 4}) where {T <: FT}
     _vc_apply!(CuArray{T}(undef, (size(M)[1:3] .- 2)..., 3), A, M, 1)
 end
 
+# ---- BandedMatrix(A*Q) from the device (concretization.jl:926-936) ----------
+using BandedMatrices: _BandedMatrix
+
+"""device_banded(A, sz, T) -> (BandedMatrix A_l, A_b): the affine map of the
+GhostDerivativeOperator (or combination) A on arrays of size sz, built on the
+device from the plan's row tables (deo_plan_concretize_banded)."""
+function device_banded(A::DeoOp, sz::Dims, ::Type{T} = Float64) where {T <: FT}
+    p = plan_for(A, sz, T)
+    l, u = Ref{Int64}(0), Ref{Int64}(0)
+    check(ccall((:deo_plan_bandwidths, libdeo), Cint, (Ptr{Cvoid}, Ref{Int64}, Ref{Int64}, Ptr{Cvoid}),
+                p, l, u, _stream()))
+    n = prod(sz)
+    data = CuArray{Float64}(undef, l[] + u[] + 1, n)
+    Ab = CuArray{Float64}(undef, n)
+    check(ccall((:deo_plan_concretize_banded, libdeo), Cint,
+                (Ptr{Cvoid}, Int64, Int64, CuPtr{Float64}, CuPtr{Float64}, Ptr{Cvoid}), p, l[], u[], data, Ab, _stream()))
+    return _BandedMatrix(Array(data), n, l[], u[]), Array(Ab)
+end
+
 # ---- serving (deo_serve_*): MOL solves of (L)(du,u,p,t) = mul!(du, L, u) ----
 # Each request: K SSP-RK3 steps of du/dt = A*Q*u from a host array u0 (and,
 # with want_grad, the gradient of ||u(T)||^2 with respect to u0).  The server

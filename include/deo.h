@@ -425,10 +425,29 @@ deo_status deo_dot_product(deo_dtype dtype, int64_t npts, int ncomp, const void*
 deo_status deo_cross_product(deo_dtype dtype, int64_t npts, const void* A, const void* B, void* u, void* stream);
 deo_status deo_square_norm(deo_dtype dtype, int64_t npts, int ncomp, const void* A, void* u, void* stream);
 
-/* Concretisation on the device: A_l (n x n, column-major, n = prod(sizes)) and
- * A_b (n) of the affine map, by applying the plan to unit vectors in batches.
- * For checking small operators (n <= 8192).  Allocates device scratch. */
+/* Concretisation: the affine map du = A_l u + A_b of the plan, built on the
+ * device from its row tables (Array(L*Q) = (Array(L) * Q_l, Array(L) * Q_b),
+ * concretization.jl:914-958, summed over the terms of a combination): one
+ * thread per row, each entry the sum of its contributions in the order of
+ * the product L * Q_l, in Float64 (Float32 plans: their weights widened).
+ * n = prod(sizes).  Plans of padded inputs are DEO_ERR_UNSUPPORTED.
+ *   deo_plan_concretize: dense A_l (n x n, column-major) and A_b (n) into
+ *     host memory; device scratch from the stream-ordered allocator on a
+ *     private stream; DEO_ERR_OOM when n x n does not fit the device.
+ *   deo_plan_concretize_device: the same into device buffers, on `stream`,
+ *     without waiting (A_l is zeroed first).
+ *   deo_plan_bandwidths: the lower / upper bandwidths l, u of A_l (largest
+ *     i - j and j - i over its structural entries); waits for `stream`.
+ *   deo_plan_concretize_banded: BandedMatrix(L*Q): A_l in band storage,
+ *     (l + u + 1) x n column-major with entry (i, j) at row u + i - j of
+ *     column j (BandedMatrices' bandeddata layout), and A_b, device buffers,
+ *     on `stream`; DEO_ERR_BAD_SHAPE if an entry lies outside (l, u).  Waits
+ *     for `stream` (to read that check). */
 deo_status deo_plan_concretize(const deo_plan* plan, double* A_l_host, double* A_b_host);
+deo_status deo_plan_concretize_device(const deo_plan* plan, double* A_l_dev, double* A_b_dev, void* stream);
+deo_status deo_plan_bandwidths(const deo_plan* plan, int64_t* l, int64_t* u, void* stream);
+deo_status deo_plan_concretize_banded(const deo_plan* plan, int64_t l, int64_t u, double* data_dev, double* A_b_dev,
+                                      void* stream);
 
 /* ------------------------------------------------------------------------
  * Batched applies: many independent (plan, u, du) instances in ONE launch of

@@ -66,7 +66,7 @@ def test_gradient_matches_single_solve_adjoint(cuda):
     import deo
     from deo.serve import advection_diffusion
     r = Request(shape=(24, 20), nu=0.03, c=-0.7, K=15, want_grad=True, seed=5)
-    s = Server()
+    s = Server(merge_terms=False)  # the plans of the single-solve path below
     s.run([r])
     A = advection_diffusion(r.shape, r.nu, r.c)
     u0 = deo.julia_array(r.shape)
