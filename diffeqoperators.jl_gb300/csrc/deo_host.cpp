@@ -844,6 +844,10 @@ struct deo_plan {
     } pipe;
     std::mutex pipe_mu;
     // kernels launched by the last forward apply (diagnostics; last writer wins)
+    // transposed applies on the TMA path: the box of columns read only by band rows of every axis
+    // (1-based, per term), where the transpose is the band itself (symmetric bands)
+    int adj_ok = 0;
+    int adj_lo[3] = {0, 0, 0}, adj_hi[3] = {0, 0, 0};  // (the transpose there: the band, taps reversed)
     mutable std::atomic<const char*> last_kernel{""};
     mutable std::atomic<const char*> last_kernel2{""};
     // launch timing: events around each launch of the last forward apply
@@ -1355,6 +1359,25 @@ extern "C" deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_
 
         CUDA_TRY(cudaMalloc(&P->d_sched, kSchedSlots * sizeof(unsigned int)), "cudaMalloc(unit counters)");
         CUDA_TRY(cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking), "cudaStreamCreate");
+        // the transposed fast path: the box of columns along each axis read only by band rows:
+        // [flo + H, fhi - H], clear of the points the boundary rows and the ghost maps read
+        // (ShellTerm::wlo, whi; a boundary row may be wider than the band)
+        {
+            const deo::UniPlan& U = P->uni;
+            const int H = U.radius;
+            bool ok = U.nterms >= 2 && U.nterms <= 3;
+            for (int a = 0; a < U.nterms && ok; ++a) {
+                const deo::UniTerm& t = U.t[a];
+                ok = t.nk == 2 * H + 1 && t.off0 == -H && t.axis == a;
+                const TermDev& T = D.t[a];
+                const deo::ShellTerm& S = P->shell.t[a];
+                const int lo = std::max(t.flo + H, S.wlo + 1), hi = std::min(t.fhi - H, S.len - S.whi);
+                ok = ok && lo <= hi && !T.lbc && S.len == T.len;
+                P->adj_lo[a] = lo;
+                P->adj_hi[a] = hi;
+            }
+            P->adj_ok = ok ? 1 : 0;
+        }
         CUDA_TRY(cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming), "cudaEventCreate");
         CUDA_TRY(cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming), "cudaEventCreate");
     }
@@ -1554,10 +1577,55 @@ extern "C" deo_status deo_apply(const deo_plan* p, const void* u, void* du, int 
     return DEO_OK;
 }
 
+// Transposed applies.  Laplacian-type plans on the TMA path: the interior
+// kernel of the forward apply, with every band's taps reversed, on the box
+// of columns read only by band rows (there column j of the transpose is
+// sum_k w[2H - k] d[j + k - H], the order in which the generic column
+// evaluator adds the rows), then the generic column evaluator on the rest
+// (k_shell_adj, a full grid; beside the interior, in the one CTA per SM that
+// fits there, it took longer than the interior: 0.52 against 0.37 ms at
+// 256^3).  Other plans: the generic transposed kernel.
+template <typename E>
+static void reverse_taps(E* w, int n) {
+    for (int k = 0; k < n / 2; ++k) std::swap(w[k], w[n - 1 - k]);
+}
+
+static int launch_adjoint(const deo_plan* p, const void* d, void* ub, int overwrite, void* stream) {
+    if (p->adj_ok && p->uni.enabled && p->uni.lap && p->fast_path && p->use_tma &&
+        deo_k_tma_ok(&p->uni, p->dev.dtype, d)) {
+        deo::UniPlan ua = p->uni;
+        const int K = 2 * ua.radius + 1;
+        for (int a = 0; a < ua.nterms; ++a) {
+            ua.t[a].flo = p->adj_lo[a];
+            ua.t[a].fhi = p->adj_hi[a];
+            if (p->dev.dtype == DEO_F64) reverse_taps(ua.t[a].w, K);
+            else reverse_taps(reinterpret_cast<float*>(ua.t[a].w), K);
+        }
+        // the same reversal of the integer and exact-sum images of the shared band (their centre
+        // weight and scale are unchanged)
+        reverse_taps(ua.ens_w, K);
+        reverse_taps(ua.fx_w, K);
+        reverse_taps(ua.bfx_w, K);
+        unsigned int* sched = p->d_sched ? p->d_sched + (p->sched_slot.fetch_add(1) % kSchedSlots) : nullptr;
+        const char* k = "";
+        const int e = deo_k_apply_tma(&ua, p->d_plan, p->dev.dtype, d, ub, overwrite, p->exact_sums, stream, &k,
+                                      sched);
+        if (e) return e;
+        const int e2 = deo_k_apply_shell_adj(&ua, p->d_plan, p->dev.dtype, d, ub, overwrite, 0, stream);
+        if (e2) return e2;
+        p->last_kernel = k;
+        p->last_kernel2 = "k_shell_adj";
+        return 0;
+    }
+    p->last_kernel = "k_apply";
+    p->last_kernel2 = "";
+    return deo_k_apply(&p->dev, d, ub, overwrite, 1, stream);
+}
+
 extern "C" deo_status deo_apply_adjoint(const deo_plan* p, const void* d, void* ub, int overwrite, void* stream) {
     deo_status s = check_ptrs(p, d, ub);
     if (s != DEO_OK) return s;
-    const int e = deo_k_apply(&p->dev, d, ub, overwrite, 1, stream);
+    const int e = launch_adjoint(p, d, ub, overwrite, stream);
     if (e) return cuda_fail((cudaError_t)e, "deo_apply_adjoint launch");
     return DEO_OK;
 }

@@ -308,6 +308,10 @@ extern "C" int deo_k_read_status(unsigned int* status);
 extern "C" int deo_k_encode_map3(void* map, const void* u, int es, int64_t nx, int64_t ny, int64_t nz, int bx, int by,
                                  int bz);
 extern "C" int deo_k_read_shell_status(unsigned int* status);
+// The transposed operator outside the box of up's [flo, fhi] (the generic
+// column evaluator, one thread per point); concurrent: one CTA per SM
+extern "C" int deo_k_apply_shell_adj(const deo::UniPlan* up, const deo::PlanDev* dp, int dtype, const void* d,
+                                     void* ub, int overwrite, int concurrent, void* stream);
 // Float32 vectorised interior (deo_vec.cu): cudaErrorNotSupported when the
 // plan or the buffers do not fit it (the caller then runs k_lap_q)
 extern "C" int deo_k_apply_vec(const deo::UniPlan* up, unsigned int* sched, const void* u, void* du, int ow,

@@ -48,6 +48,7 @@
 
 extern "C" int64_t deo_plan_points(const deo_plan* p);
 extern "C" int deo_plan_dtype_code(const deo_plan* p);
+extern "C" size_t deo_plan_table_bytes(const deo_plan* p);
 extern "C" deo_status deo_set_error(deo_status s, const char* msg);
 
 namespace {
@@ -412,7 +413,10 @@ extern "C" deo_status deo_serve_submit(deo_server* s, const deo_request* q, int6
     r.grad = q->want_grad != 0;
     r.npts = deo_plan_points(q->plan);
     r.vec_bytes = (size_t)r.npts * (s->dtype == DEO_F64 ? 8 : 4);
-    r.state_bytes = 3 * r.vec_bytes;
+    // counted against the budget: the three state buffers, the plan's device tables, and the
+    // request's entries in the three stage batches (work items of at least 1024 points)
+    r.state_bytes = 3 * r.vec_bytes + deo_plan_table_bytes(q->plan) +
+                    3 * (sizeof(deo::StageDev) + ((size_t)r.npts / 1024 + 1) * sizeof(deo::WorkItem));
     r.t_submit = now_s();
     *rid = r.rid;
     ++s->stats.submitted;

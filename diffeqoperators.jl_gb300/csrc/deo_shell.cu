@@ -354,6 +354,26 @@ __global__ void __launch_bounds__(256) k_shell_generic(const __grid_constant__ S
     }
 }
 
+// The transposed operator on the points outside the box of the interior
+// kernels' adjoint (the box's columns are read only by band rows of every
+// axis, so there the transpose is the forward band with its taps reversed --
+// the band itself, for the symmetric bands this path takes): the generic
+// column evaluator (adj_term: every row touching the column, the ghost
+// columns folded back through the BC map), one thread per point.
+template <typename T>
+__global__ void __launch_bounds__(256) k_shell_adj(const __grid_constant__ ShellBox B, const PlanDev* __restrict__ P,
+                                                   const T* __restrict__ d, T* __restrict__ ub, int overwrite) {
+    const int64_t nx = B.n[0], ny = B.n[1];
+    const int64_t total = B.cz + B.cy + B.cx;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t x, y, z;
+        shell_coords(B, t, x, y, z);
+        const int64_t idx = (z * ny + y) * nx + x;
+        const T r = eval_point<T, true>(*P, d, idx);
+        ub[idx] = overwrite ? r : r + ub[idx];
+    }
+}
+
 }  // namespace deo
 
 using namespace deo;
@@ -464,9 +484,9 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
     return (int)cudaGetLastError();
 }
 
-template <typename T, int NT>
-static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPlan* sp_dev, int mode,
-                          const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st, const char** kernel) {
+// The shell's index space: the points of the array outside the box
+// [flo, fhi] of every term's axis (UniTerm; 0-based below).
+static ShellBox shell_box(const UniPlan* up) {
     ShellBox B{};
     for (int k = 0; k < 3; ++k) {
         B.n[k] = up->n[k];
@@ -488,7 +508,6 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
     B.cy = iz * (ny - iy) * nx;
     B.cx = iz * iy * (nx - ix);
     const int64_t total = B.cz + B.cy + B.cx;
-    if (total == 0) return 0;
     B.small = total < (1LL << 31) && nx * ny < (1LL << 31);
     if (B.small) {
         auto fd = [](int64_t d) { return make_fastdiv((uint32_t)std::max<int64_t>(d, 1)); };
@@ -498,6 +517,18 @@ static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPla
         B.d_niy = fd(iy);
         B.d_nxo = fd(nx - ix);
     }
+    return B;
+}
+
+template <typename T, int NT>
+static int launch_shell_t(const UniPlan* up, const ShellPlan* sp, const ShellPlan* sp_dev, int mode,
+                          const PlanDev* dp, const void* u, void* du, int ow, cudaStream_t st, const char** kernel) {
+    ShellBox B = shell_box(up);
+    const int64_t ix = B.hi[0] - B.lo[0] + 1, iy = B.hi[1] - B.lo[1] + 1, iz = B.hi[2] - B.lo[2] + 1;
+    const int64_t nx = B.n[0], ny = B.n[1];
+    (void)ny;
+    const int64_t total = B.cz + B.cy + B.cx;
+    if (total == 0) return 0;
     const bool have_lines = sp && sp_dev && B.lo[0] <= B.hi[0] && B.lo[1] <= B.hi[1] && B.lo[2] <= B.hi[2];
     // Float64 alone: the line kernel (FP64-bound, full grid).  Otherwise the face kernel: a shared-memory
     // box per tile; beside a Float64 interior kernel in small CTAs that fit next to its CTAs, so that the
@@ -559,6 +590,25 @@ extern "C" int deo_k_apply_shell(const UniPlan* up, const ShellPlan* sp, const S
     if (!kernel) kernel = &none;
     return dtype == 0 ? launch_shell<double>(up, sp, sp_dev, mode, dp, u, du, overwrite, st, kernel)
                       : launch_shell<float>(up, sp, sp_dev, mode, dp, u, du, overwrite, st, kernel);
+}
+
+extern "C" int deo_k_apply_shell_adj(const UniPlan* up, const PlanDev* dp, int dtype, const void* d, void* ub,
+                                     int overwrite, int concurrent, void* stream) {
+    if (up->nterms < 2 || up->nterms > 3) return (int)cudaErrorNotSupported;
+    const ShellBox B = shell_box(up);
+    const int64_t total = B.cz + B.cy + B.cx;
+    if (total == 0) return 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto go = [&](auto kernel, const auto* in, auto* out) {
+        static int64_t g = 0;
+        if (!g) g = shell_grid(kernel, 1LL << 40);
+        // beside the interior kernel: one CTA per SM (fits next to its CTAs); alone: a full grid
+        const int64_t grid = std::min<int64_t>(concurrent ? deo_k_num_sms() : g, (total + 255) / 256);
+        kernel<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(B, dp, in, out, overwrite);
+    };
+    if (dtype == 0) go(k_shell_adj<double>, (const double*)d, (double*)ub);
+    else go(k_shell_adj<float>, (const float*)d, (float*)ub);
+    return (int)cudaGetLastError();
 }
 
 extern "C" int deo_k_read_shell_status(unsigned int* status) {

@@ -64,6 +64,8 @@ class Request:
         return self.t_done - self.arrival
 
     def bytes_needed(self, esize: int = 8) -> int:
+        """The three state buffers (the server also counts the plan's device
+        tables and the request's stage work-list entries)."""
         return 3 * self.npts * esize
 
     def dt(self) -> float:

@@ -546,7 +546,9 @@ typedef struct {
     int64_t in_use_bytes, active, pending;
     int64_t device_us;  /* device time of the retired rounds, first launch to last */
 } deo_serve_stats;
-/* budget_bytes: device memory the admitted requests' states may take;
+/* budget_bytes: device memory the admitted requests may take: each one's
+ * three state buffers, its plan's device tables and its stage work-list
+ * entries;
  * max_steps_per_round caps S (0 = 64). */
 deo_status deo_serve_create(size_t budget_bytes, deo_dtype dtype, int max_steps_per_round, deo_server** out);
 /* *rid receives the request id.  DEO_ERR_REJECTED (with *rid set) if its state

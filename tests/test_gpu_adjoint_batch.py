@@ -477,3 +477,50 @@ def test_default_path_accumulate_equals_overwrite_plus_base(cuda, dtype):
     p.apply(ud, acc, overwrite=False)
     assert torch.equal(acc, base + ow)
     assert deo.device_status() == 0
+
+
+@pytest.mark.parametrize("dtype,sums", [("f64", 0), ("f64", 1), ("f32", 0)])
+@pytest.mark.parametrize("case", [dict(ND[0], shape=(72, 45, 33)), ND[1], dict(ND[2], shape=(24, 20, 18)),
+                                  LAP_CASES[2],
+                                  dict(shape=(64, 40, 30), terms=[T("centered", 2, 6, axis=k, h=0.02,
+                                                                    bc=("neumann", 0.3, -0.2, 1)) for k in (1, 2, 3)],
+                                       seed=12)],
+                         ids=["a4-robin", "a2-dirichlet0", "a4-periodic", "2d-a4-robin", "a6-neumann"])
+def test_transposed_fast_path(cuda, case, dtype, sums):
+    """deo_apply_adjoint on the TMA path (the interior kernel on the columns
+    read only by band rows, k_shell_adj on the rest) against the generic
+    transposed kernel: bit for bit in the reference's order (EXACT_SUMS=0;
+    Float32), within the 4-ulp bar for the fixed-point interior; overwrite and
+    accumulate (the shell runs after the interior whatever
+    DEO_OPT_CONCURRENT_SHELL says)."""
+    import torch
+    A, oterms, u = build(case, dtype=dtype)
+    shape = tuple(case["shape"])
+    p = deo.Plan(A.terms(), shape, 0 if dtype == "f64" else 1)
+    p.set_option(deo.DEO_OPT_EXACT_SUMS, sums)
+    v = to_device(np.asfortranarray(np.random.default_rng(8).standard_normal(shape)), dtype)
+    base = to_device(np.asfortranarray(np.random.default_rng(9).standard_normal(shape)), dtype)
+    tdt = v.dtype
+    p.set_option(deo.DEO_OPT_FAST_PATH, 0)
+    ref, ref_acc = deo.julia_array(shape, tdt), base.clone()
+    p.adjoint(v, ref)
+    p.adjoint(v, ref_acc, overwrite=False)
+    assert p.kernels == ("k_apply",)
+    p.set_option(deo.DEO_OPT_FAST_PATH, 1)
+    for conc in (1, 0):
+        p.set_option(deo.DEO_OPT_CONCURRENT_SHELL, conc)
+        o = deo.julia_array(shape, tdt, fill=np.nan)
+        p.adjoint(v, o)
+        assert p.kernels[1] == "k_shell_adj" and p.kernels[0].startswith("k_lap_"), p.kernels
+        a = base.clone()
+        p.adjoint(v, a, overwrite=False)
+        if dtype == "f32" or sums == 0:
+            assert torch.equal(o, ref), conc
+            assert torch.equal(a, ref_acc), conc
+        else:
+            r, g = to_host(ref), to_host(o)
+            vh = to_host(v)
+            # the transposed sum's scale: sum_i |A[i, j] v_i|, from the forward operator's abs scale of |v|
+            scale = O.abs_scale(oterms, np.abs(vh))
+            assert (np.abs(g - r) <= 4 * np.spacing(np.maximum(scale, np.abs(r))) + 1e-300).all()
+    assert deo.device_status() == 0
