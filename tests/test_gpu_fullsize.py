@@ -122,10 +122,14 @@ def test_batched_forward_adjoint_and_fd_gradient_full_range(cuda):
         worst = max(worst, w)
     _report("parity_batched", {"instances": len(specs), "points": int(sum(np.prod(sp[0]) for sp in specs)),
                                "forward_max_ulp_of_scale": worst})
-    # the batched adjoint equals the per-instance adjoint kernel bit for bit
+    # the batched adjoint equals the per-instance transposed apply in the reference's tap order bit for
+    # bit (the batched kernel keeps that order; a Laplacian-type instance's own adjoint may take the
+    # TMA path with the fixed-point interior, within the bar instead)
     for p, v, ub in zip(plans, vs, ubars):
         one = deo.julia_array(tuple(v.shape))
+        p.set_option(deo.DEO_OPT_EXACT_SUMS, 0)
         p.adjoint(v, one)
+        p.set_option(deo.DEO_OPT_EXACT_SUMS, 1)
         assert torch.equal(one, ub)
     # finite-difference gradient of f(u) = <v, A u> (A affine: the BC offsets cancel) on a random
     # direction w, through the batched forward pass, against <A^T v, w> from the batched adjoint
