@@ -109,34 +109,42 @@ struct FaceGrid {
     int box_bytes[3];
 };
 
-template <typename T, int NT>
-__device__ __forceinline__ T face_point(const ShellTerm* S, const UniPlan& U, const T* __restrict__ pc,
-                                        const int (&c)[3], const int (&org)[3], const int (&bd)[3],
-                                        const int64_t (&sb)[3], const T* __restrict__ u, int64_t gidx,
-                                        const int64_t (&gst)[3]) {
+// The terms of a face point other than the face's own axis A, added into
+// acc in axis order around the A term `va` (the generic evaluator's order):
+// a band from the box, or (at edges and corners of the shell) the other
+// axis's boundary row, from the box when its points lie in it.
+template <typename T, int NT, int MAXW>
+__device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, const T* __restrict__ pc, int A, T va,
+                                      const int (&c)[3], const int (&org)[3], const int (&bd)[3],
+                                      const int64_t (&sb)[3], const T* __restrict__ u, int64_t gidx,
+                                      const int64_t (&gst)[3]) {
     T acc = T(0);
 #pragma unroll
     for (int b = 0; b < NT; ++b) {
-        const int ib = c[b] + 1;
         T v;
-        if (ib >= U.t[b].flo && ib <= U.t[b].fhi) {
-            v = shell_band<T>(U.t[b], U.radius, pc, 0, sb[b]);
+        if (b == A) {
+            v = va;
         } else {
-            const ShellTerm& SB = S[b];
-            const bool low = ib <= SB.nlo;
-            const int w0 = low ? 0 : SB.len - SB.whi;
-            const int w1 = low ? SB.wlo : SB.len;
-            if (w0 >= org[b] && w1 <= org[b] + bd[b])  // the row's points are in the box
-                v = shell_row_cold<T>(SB, pc - c[b] * sb[b], sb[b], ib);
-            else
-                v = shell_row_cold<T>(SB, u + gidx - c[b] * gst[b], gst[b], ib);
+            const int ib = c[b] + 1;
+            if (ib >= U.t[b].flo && ib <= U.t[b].fhi) {
+                v = shell_band<T>(U.t[b], U.radius, pc, 0, sb[b]);
+            } else {
+                const ShellTerm& SB = S[b];
+                const bool low = ib <= SB.nlo;
+                const int w0 = low ? 0 : SB.len - SB.whi;
+                const int w1 = low ? SB.wlo : SB.len;
+                if (w0 >= org[b] && w1 <= org[b] + bd[b])
+                    v = shell_row_cold<T, MAXW>(SB, pc - c[b] * sb[b], sb[b], ib);
+                else
+                    v = shell_row_cold<T, MAXW>(SB, u + gidx - c[b] * gst[b], gst[b], ib);
+            }
         }
         acc = (b == 0) ? v : acc + v;
     }
     return zero_fix(acc);
 }
 
-template <typename T, int NT>
+template <typename T, int NT, int MAXW>
 __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMap m0,
                                               const __grid_constant__ CUtensorMap m1,
                                               const __grid_constant__ CUtensorMap m2,
@@ -209,20 +217,39 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
         const int nrows = e ? SA.nhi : SA.nlo;
         const int cA0 = e ? SA.len - SA.nhi : 0;
         const int tw1 = G.tw1[A], tw2 = G.tw2[A];
-        const int npts = nrows * tw1 * tw2;
-        for (int q = threadIdx.x; q < npts; q += blockDim.x) {
-            const int r = q / (tw1 * tw2);
-            const int q2 = q - r * tw1 * tw2;
-            const int p2 = q2 / tw1, p1 = q2 - p2 * tw1;
+        const int L2 = SA.len + 2;
+        // one thread per line of the tile along A: the line's ghosts once (the boundary condition's
+        // map of its end points, from the box), then its nrows boundary rows, each with the other
+        // axes' terms
+        bool need_l = false, need_r = false;
+        for (int r = 0; r < nrows; ++r) {
+            const ShellRow& R = SA.row[(e ? SA.nlo : 0) + r];
+            need_l |= R.p0 == 1;
+            need_r |= R.p0 + R.nk - 1 == L2;
+        }
+        const bool line_in_box = (e ? SA.len - SA.whi : 0) >= org[A] && (e ? SA.len : SA.wlo) <= org[A] + bd[A];
+        for (int q = threadIdx.x; q < tw1 * tw2; q += blockDim.x) {
+            const int p2 = q / tw1, p1 = q - p2 * tw1;
             int c[3];
-            c[A] = cA0 + r;
+            c[A] = 0;
             c[b1] = c1 + p1;
             c[b2] = c2 + p2;
             if (c[b1] >= G.e1[A] || c[b2] >= G.e2[A]) continue;
-            const int64_t gidx = c[0] + c[1] * nx + (int64_t)c[2] * sxy;
-            const T* pc = box + (int64_t)(c[2] - org[2]) * sb[2] + (int64_t)(c[1] - org[1]) * sb[1] + (c[0] - org[0]);
-            const T tot = face_point<T, NT>(S, U, pc, c, org, bd, sb, u, gidx, gst);
-            du[gidx] = ow ? tot : tot + du[gidx];
+            const int64_t g0 = c[0] + c[1] * nx + (int64_t)c[2] * sxy;  // the line's first point
+            const T* box0 = box + (int64_t)(c[2] - org[2]) * sb[2] + (int64_t)(c[1] - org[1]) * sb[1] + (c[0] - org[0]);
+            const T* line = line_in_box ? box0 : u + g0;  // position 0 of the line along A
+            const int64_t ls = line_in_box ? sb[A] : gst[A];
+            const T gl = need_l ? shell_ghost<T, MAXW>(SA, line, ls, true) : T(0);
+            const T gr = need_r ? shell_ghost<T, MAXW>(SA, line, ls, false) : T(0);
+            for (int r = 0; r < nrows; ++r) {
+                c[A] = cA0 + r;
+                const ShellRow& R = SA.row[(e ? SA.nlo : 0) + r];
+                const T va = row_eval<T, MAXW>(R, line, ls, L2, gl, gr);
+                const int64_t gidx = g0 + (int64_t)c[A] * gst[A];
+                const T* pc = box0 + (int64_t)c[A] * sb[A];
+                const T tot = face_sum<T, NT, MAXW>(S, U, pc, A, va, c, org, bd, sb, u, gidx, gst);
+                du[gidx] = ow ? tot : tot + du[gidx];
+            }
         }
         __syncthreads();  // every thread is done with the box before the next copy overwrites it
     }
@@ -470,17 +497,27 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
     if (NT < 3) maps[2] = maps[0];
     static size_t smem_set = 0;
     if (smem_max > smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_face<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        cudaError_t e = cudaFuncSetAttribute(k_face<T, NT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_face<T, NT, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
         // the interior kernels run with the largest shared-memory carveout; asking for the same lets this
         // kernel's CTAs share their SMs
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_face<T, NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            e = cudaFuncSetAttribute(k_face<T, NT, 8>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     (int)cudaSharedmemCarveoutMaxShared);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_face<T, NT, 16>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return (int)e;
         smem_set = smem_max;
     }
-    k_face<T, NT><<<(unsigned)(small ? std::min(cta, deo_k_num_sms()) : cta), small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u,
-                                                          (T*)du, ow);
+    const unsigned grid = (unsigned)(small ? std::min(cta, deo_k_num_sms()) : cta);
+    if (sp->maxw <= 8)
+        k_face<T, NT, 8><<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev,
+                                                                    (const T*)u, (T*)du, ow);
+    else
+        k_face<T, NT, 16><<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev,
+                                                                     (const T*)u, (T*)du, ow);
     return (int)cudaGetLastError();
 }
 
