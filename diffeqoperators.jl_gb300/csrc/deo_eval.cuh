@@ -265,6 +265,13 @@ __device__ __forceinline__ T eval_point(const PlanDev& P, const T* __restrict__ 
     return ADJ ? acc : zero_fix(acc);
 }
 
+// Out-of-line copy of the generic column evaluator (the transposed shell's
+// boundary columns).
+template <typename T>
+__device__ __noinline__ T adj_term_cold(const TermDev& t, const T* __restrict__ d, int64_t idx, int j) {
+    return adj_term<T>(t, d, idx, j);
+}
+
 // Out-of-line copy for a kernel that evaluates a few boundary points with
 // the generic evaluator (the shell fallback).
 template <typename T>

@@ -382,22 +382,33 @@ __global__ void __launch_bounds__(256) k_shell_generic(const __grid_constant__ S
 }
 
 // The transposed operator on the points outside the box of the interior
-// kernels' adjoint (the box's columns are read only by band rows of every
-// axis, so there the transpose is the forward band with its taps reversed --
-// the band itself, for the symmetric bands this path takes): the generic
-// column evaluator (adj_term: every row touching the column, the ghost
-// columns folded back through the BC map), one thread per point.
-template <typename T>
-__global__ void __launch_bounds__(256) k_shell_adj(const __grid_constant__ ShellBox B, const PlanDev* __restrict__ P,
-                                                   const T* __restrict__ d, T* __restrict__ ub, int overwrite) {
+// kernels' transposed applies, one thread per point.  Along an axis where the
+// point's column is read only by band rows (inside that axis's [flo, fhi] of
+// U, whose bands carry their taps reversed) the term is the reversed band,
+// summed as the generic column evaluator sums its rows; along the others the
+// generic column evaluator (adj_term: every row touching the column, the
+// ghost columns folded back through the BC map).  Terms added in axis order.
+template <typename T, int NT>
+__global__ void __launch_bounds__(256) k_shell_adj(const __grid_constant__ ShellBox B, const __grid_constant__ UniPlan U,
+                                                   const PlanDev* __restrict__ P, const T* __restrict__ d,
+                                                   T* __restrict__ ub, int overwrite) {
     const int64_t nx = B.n[0], ny = B.n[1];
     const int64_t total = B.cz + B.cy + B.cx;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t x, y, z;
         shell_coords(B, t, x, y, z);
         const int64_t idx = (z * ny + y) * nx + x;
-        const T r = eval_point<T, true>(*P, d, idx);
-        ub[idx] = overwrite ? r : r + ub[idx];
+        const int64_t crd[3] = {x, y, z};
+        const int64_t st[3] = {1, nx, nx * ny};
+        T acc = T(0);
+#pragma unroll
+        for (int a = 0; a < NT; ++a) {
+            const int j = (int)crd[a] + 1;
+            const T r = (j >= U.t[a].flo && j <= U.t[a].fhi) ? shell_band<T>(U.t[a], U.radius, d, idx, st[a])
+                                                             : adj_term_cold<T>(P->t[a], d, idx, j);
+            acc = (a == 0) ? r : acc + r;
+        }
+        ub[idx] = overwrite ? acc : acc + ub[idx];
     }
 }
 
@@ -641,10 +652,15 @@ extern "C" int deo_k_apply_shell_adj(const UniPlan* up, const PlanDev* dp, int d
         if (!g) g = shell_grid(kernel, 1LL << 40);
         // beside the interior kernel: one CTA per SM (fits next to its CTAs); alone: a full grid
         const int64_t grid = std::min<int64_t>(concurrent ? deo_k_num_sms() : g, (total + 255) / 256);
-        kernel<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(B, dp, in, out, overwrite);
+        kernel<<<(unsigned)std::max<int64_t>(grid, 1), 256, 0, st>>>(B, *up, dp, in, out, overwrite);
     };
-    if (dtype == 0) go(k_shell_adj<double>, (const double*)d, (double*)ub);
-    else go(k_shell_adj<float>, (const float*)d, (float*)ub);
+    if (up->nterms == 3) {
+        if (dtype == 0) go(k_shell_adj<double, 3>, (const double*)d, (double*)ub);
+        else go(k_shell_adj<float, 3>, (const float*)d, (float*)ub);
+    } else {
+        if (dtype == 0) go(k_shell_adj<double, 2>, (const double*)d, (double*)ub);
+        else go(k_shell_adj<float, 2>, (const float*)d, (float*)ub);
+    }
     return (int)cudaGetLastError();
 }
 
