@@ -1286,6 +1286,48 @@ extern "C" deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_
         }
     }
     P->shell.ok = P->shell.ok >= 0 && D.nterms <= 3 ? 1 : 0;
+    // DEO_PLAN_STAR: every term a constant band (no coefficient field, no per-line BCs): one star of
+    // taps for the points whose rows read no ghost along any axis, the centre taps merged (added in
+    // the terms' order in Float64, rounded once to the plan's dtype)
+    if (flags & DEO_PLAN_STAR) {
+        deo::StarDev S{};
+        bool ok = true;
+        double centre = 0.0;
+        bool have_centre = false;
+        std::vector<std::pair<int64_t, double>> taps;
+        for (int t = 0; t < D.nterms && ok; ++t) {
+            const TermDev& T = D.t[t];
+            const RowTabDev& tb = T.tab[0];
+            ok = !T.has_field && T.nvar == 1 && !T.lbc && tb.ilo <= tb.ihi;
+            if (!ok) break;
+            const int flo = std::max(tb.ilo, 2 - tb.band_p0_off);
+            const int fhi = std::min(tb.ihi, T.len + 2 - tb.band_nk - tb.band_p0_off);
+            ok = flo <= fhi;
+            S.lo[t] = flo;
+            S.hi[t] = fhi;
+            for (int k = 0; k < tb.band_nk && ok; ++k) {
+                const double w = dtype == DEO_F64 ? tb.wband[k] : (double)reinterpret_cast<const float*>(tb.wband)[k];
+                const int rel = tb.band_p0_off + k - 1;  // line position of tap k minus the point's
+                if (rel == 0) {
+                    centre = have_centre ? centre + w : w;
+                    have_centre = true;
+                } else {
+                    taps.emplace_back((int64_t)rel * T.stride, w);
+                }
+            }
+        }
+        if (ok && (int)taps.size() + (have_centre ? 1 : 0) <= DEO_STAR_MAX) {
+            if (have_centre) {
+                S.off[S.n] = 0;
+                S.w[S.n++] = dtype == DEO_F64 ? centre : (double)(float)centre;
+            }
+            for (const auto& tw : taps) {
+                S.off[S.n] = tw.first;
+                S.w[S.n++] = tw.second;
+            }
+            D.star = S;
+        }
+    }
     // fast path for 2-D/3-D plans whose terms all have constant interior rows
     {
         deo::UniPlan& U = P->uni;
@@ -1393,6 +1435,7 @@ extern "C" int64_t deo_plan_points(const deo_plan* p) { return p->dev.total; }
 extern "C" int deo_plan_dtype_code(const deo_plan* p) { return p->dev.dtype; }
 extern "C" int deo_plan_has_lbc(const deo_plan* p) { return p->dev.has_lbc; }
 extern "C" int deo_plan_terms(const deo_plan* p) { return p ? p->dev.nterms : -1; }
+extern "C" int deo_plan_star_taps(const deo_plan* p) { return p ? p->dev.star.n : -1; }
 extern "C" deo_status deo_set_error(deo_status s, const char* msg) { return fail(s, "%s", msg); }
 extern "C" size_t deo_plan_table_bytes(const deo_plan* p) { return p ? p->table_bytes : 0; }
 

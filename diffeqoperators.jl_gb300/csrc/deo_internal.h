@@ -81,6 +81,19 @@ struct TermDev {
 };
 
 #define DEO_KMAX_TERMS 8
+#define DEO_STAR_MAX 32
+// A plan built with DEO_PLAN_STAR whose terms are all constant bands: at a
+// point whose row along every term's axis is in [lo, hi] of that term (band
+// rows that read no ghost), the forward apply is one sum over n taps at flat
+// offsets `off` with weights `w` -- every term's taps, the centre taps of the
+// terms merged into one (weights of the plan's dtype, held as doubles).
+struct StarDev {
+    int n;
+    int lo[DEO_KMAX_TERMS], hi[DEO_KMAX_TERMS];
+    int64_t off[DEO_STAR_MAX];
+    double w[DEO_STAR_MAX];
+};
+
 struct PlanDev {
     int ndims;
     int nterms;
@@ -90,6 +103,7 @@ struct PlanDev {
     int64_t sizes[8];
     int64_t total;
     TermDev t[DEO_KMAX_TERMS];
+    StarDev star;
 };
 
 // The band rows of a plan whose terms all have constant interior rows (uniform

@@ -127,6 +127,12 @@ extern "C" deo_status deo_batch_apply_noalloc(int n, const deo_instance* inst, i
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return deo_set_error(DEO_ERR_CUDA, "cudaGetDevice failed");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // its copy from the (pageable, reused) host image cannot be captured into a graph
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess)
+        return deo_set_error(DEO_ERR_CUDA, "cudaStreamIsCapturing failed");
+    if (cap != cudaStreamCaptureStatusNone)
+        return deo_set_error(DEO_ERR_UNSUPPORTED, "deo_batch_apply_noalloc cannot run under stream capture");
     std::lock_guard<std::mutex> lk(g_mu);
     unsigned char* base = nullptr;
     const deo_status ps = prepare(dev, st, &base);

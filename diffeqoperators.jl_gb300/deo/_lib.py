@@ -25,6 +25,7 @@ DEO_OPT_F32_VECTOR = 8
 DEO_OPT_SHELL_KERNEL = 9
 DEO_OPT_F32_TILE = 10
 DEO_PLAN_MERGE_TERMS = 1
+DEO_PLAN_STAR = 2
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)
@@ -125,6 +126,7 @@ def lib():
     proto("deo_bc_array", st, C.POINTER(BCStruct), C.c_int, _dp, _dp)
     proto("deo_plan_create", st, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(Term), C.POINTER(_vp))
     proto("deo_plan_terms", C.c_int, _vp)
+    proto("deo_plan_star_taps", C.c_int, _vp)
     proto("deo_plan_create_opts", st, C.c_int, C.POINTER(C.c_int64), C.c_int, C.c_int, C.POINTER(Term), C.c_int,
           C.POINTER(_vp))
     proto("deo_plan_destroy", None, _vp)
@@ -206,7 +208,7 @@ EXPORTED = [
     "deo_upwind_difference", "deo_operator_from_tables", "deo_operator_describe",
     "deo_operator_set_coefficients", "deo_operator_scale_coefficients", "deo_operator_clone",
     "deo_operator_destroy", "deo_operator_array", "deo_operator_banded", "deo_robin_bc", "deo_general_bc", "deo_dirichlet_bc",
-    "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_create_opts", "deo_plan_terms", "deo_plan_destroy",
+    "deo_neumann_bc", "deo_periodic_bc", "deo_bc_array", "deo_plan_create", "deo_plan_create_opts", "deo_plan_terms", "deo_plan_star_taps", "deo_plan_destroy",
     "deo_plan_table_bytes", "deo_plan_set_option", "deo_plan_get_option", "deo_plan_kernels", "deo_plan_launch_times", "deo_device_status", "deo_apply", "deo_apply_host", "deo_nonlinear_diffusion_plan", "deo_nonlinear_diffusion",
     "deo_nonlinear_diffusion_destroy", "deo_apply_host_async", "deo_plan_host_sync", "deo_apply_adjoint", "deo_plan_concretize", "deo_plan_concretize_device", "deo_plan_bandwidths",
     "deo_plan_concretize_banded",

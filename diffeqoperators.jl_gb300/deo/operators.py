@@ -755,7 +755,7 @@ class Plan:
     """A compiled deo_plan for (terms, Julia size, dtype)."""
 
     def __init__(self, ghosts: Sequence[GhostDerivativeOperator], shape: Sequence[int], dtype_code: int,
-                 path: int = L.DEO_PATH_AUTO, merge_terms: bool = False):
+                 path: int = L.DEO_PATH_AUTO, merge_terms: bool = False, star: bool = False):
         nd = len(shape)
         terms = (Term * len(ghosts))()
         self._keep = []
@@ -795,8 +795,8 @@ class Plan:
                 terms[i].coeff_field = None
         sizes = (C.c_int64 * nd)(*self.shape)
         h = C.c_void_p()
-        check(L.lib().deo_plan_create_opts(nd, sizes, dtype_code, len(ghosts), terms,
-                                           L.DEO_PLAN_MERGE_TERMS if merge_terms else 0, C.byref(h)))
+        flags = (L.DEO_PLAN_MERGE_TERMS if merge_terms else 0) | (L.DEO_PLAN_STAR if star else 0)
+        check(L.lib().deo_plan_create_opts(nd, sizes, dtype_code, len(ghosts), terms, flags, C.byref(h)))
         self._h = h
         self._ops = [g.L for g in ghosts]  # keep operators alive
 
@@ -811,6 +811,11 @@ class Plan:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def star_taps(self) -> int:
+        """Taps of the merged star (DEO_PLAN_STAR), 0 without one."""
+        return int(L.lib().deo_plan_star_taps(self._h))
 
     @property
     def evaluated_terms(self) -> int:

@@ -101,7 +101,9 @@ class Server:
                  inject_alloc_failures: int = 0, merge_terms: bool = True):
         """merge_terms: build each request's plan with DEO_PLAN_MERGE_TERMS
         (the diffusion and advection terms along axis 1 share the boundary
-        condition, so they are evaluated as one tap set)."""
+        condition, so they are evaluated as one tap set).  DEO_PLAN_STAR is
+        not used: on the served mix it saved no time (3.11 against 3.04 s of
+        device time)."""
         self.merge_terms = merge_terms
         h = C.c_void_p()
         check(L.lib().deo_serve_create(int(hbm_budget_bytes), 0, int(max_steps_per_round), C.byref(h)))

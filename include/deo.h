@@ -191,6 +191,15 @@ deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int
  *     same 4 ulp of sum |c_k u_k| (the weights' rounding adds at most half an
  *     ulp of each merged weight times its value).  No reference counterpart. */
 #define DEO_PLAN_MERGE_TERMS 1
+/*   DEO_PLAN_STAR: when every term is a constant band (no coefficient field,
+ *     no per-line BCs), points whose rows read no ghost along any axis are
+ *     evaluated as one sum over all the terms' taps, the terms' centre
+ *     weights added into one (in Float64, rounded once): one FP64 (Float32)
+ *     instruction per tap instead of per tap and per term sum, for the
+ *     generic, batched and Runge-Kutta stage kernels (Laplacian-type plans on
+ *     the TMA path keep their interior kernels).  Rounding differs from the
+ *     reference's term-by-term sums, within the same bar. */
+#define DEO_PLAN_STAR 2
 deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
                                 int flags, deo_plan** out);
 /* Frees the plan's device tables, streams and events (cudaFree waits for the device). */
@@ -200,6 +209,8 @@ size_t deo_plan_table_bytes(const deo_plan* plan);
 /* Terms the plan evaluates per point (fewer than it was given when
  * DEO_PLAN_MERGE_TERMS joined some); -1 for a null plan. */
 int deo_plan_terms(const deo_plan* plan);
+/* Taps of the plan's merged star (DEO_PLAN_STAR; 0 when it has none); -1 for a null plan. */
+int deo_plan_star_taps(const deo_plan* plan);
 /* Plan options (defaults 1 unless stated):
  *   DEO_OPT_FAST_PATH: Laplacian-type 2-D/3-D plans (term t a centred band on
  *     axis t) use the tiled TMA kernels below for interior points; 0 forces
@@ -506,7 +517,9 @@ deo_status deo_stage_batch_create(int n, const deo_stage* stages, int tile, int 
  * address with cudaGetSymbolAddress and launches the kernel once over an empty
  * work-list), not when the library is loaded; they stay until the process
  * exits.  A call with n = 0 does only this set-up: make it where the footprint
- * may still grow (before admitting requests), and before any stream capture.
+ * may still grow (before admitting requests).  No call may be made under
+ * stream capture (its copy from a reused host image cannot be captured):
+ * on a capturing stream it returns DEO_ERR_UNSUPPORTED and enqueues nothing.
  * After a device reset the next call repeats the set-up.
  * Each call copies its work-list from host memory on `stream`; calls on one
  * stream are ordered by that stream.  Every call reuses the same array (the

@@ -87,3 +87,52 @@ def test_merged_plan_against_oracle(cuda, case, nterms):
     torch.cuda.synchronize()
     assert torch.equal(b_out, out)
     assert deo.device_status() == 0
+
+
+
+STAR_CASES = [
+    (dict(shape=(300,), terms=[T("centered", 2, 4, bc=ROBIN)], seed=11), 5),
+    (dict(shape=(96, 80), terms=[T("centered", 2, 4, axis=1, bc=ROBIN), T("centered", 2, 4, axis=2, bc=ROBIN)],
+          seed=12), 9),
+    (dict(shape=(40, 36, 30), terms=[T("centered", 2, 2, axis=k, bc=("dirichlet0",)) for k in (1, 2, 3)]
+          + [T("upwind", 1, 2, axis=1, coeff=-0.6, bc=("dirichlet0",))], seed=13), 8),
+    (dict(shape=(50, 44), terms=[T("centered", 1, 4, axis=1, bc=("periodic",)), T("centered", 2, 2, axis=2,
+                                                                                 bc=GEN)], seed=14), 7),
+    (dict(shape=(60, 50), terms=[T("centered", 2, 2, axis=1, coeff="vector", bc=ROBIN)], seed=15), 0),  # no band
+]
+
+
+@pytest.mark.parametrize("case,ntaps", STAR_CASES, ids=["1d", "2d", "3d-advection", "2d-periodic-general",
+                                                        "coefficient-vector"])
+def test_star_plan_against_oracle_and_kernels(cuda, case, ntaps):
+    """DEO_PLAN_STAR (with DEO_PLAN_MERGE_TERMS): the points whose rows read no
+    ghost as one sum over every term's taps, the centre weights merged; against
+    the oracle at the 4-ulp bar; the batched and Runge-Kutta stage kernels give
+    the plan's apply bit for bit.  A term without a constant band (a coefficient
+    vector) leaves the plan without a star."""
+    import torch
+    A, oterms, u = build(case)
+    shape = tuple(case["shape"])
+    p = deo.Plan(A.terms(), shape, 0, merge_terms=True, star=True)
+    assert p.star_taps == ntaps
+    p.set_option(deo.DEO_OPT_FAST_PATH, 0)  # the generic kernels (Laplacian-type plans would take the TMA path)
+    ud = to_device(u)
+    out = deo.julia_array(shape, fill=np.nan)
+    p.apply(ud, out)
+    ref = O.apply(oterms, u)
+    assert _ulps(to_host(out), ref, O.abs_scale(oterms, u)) <= 4.0
+    b_out = deo.julia_array(shape, fill=np.nan)
+    deo.Batch([(p, ud, b_out)]).run(use_graph=False)
+    torch.cuda.synchronize()
+    assert torch.equal(b_out, out)
+    # one Runge-Kutta stage c + dt * A c with gamma = 1: the stage kernel's RHS is the same star
+    dt = 1e-3
+    s_out = deo.julia_array(shape, fill=np.nan)
+    deo.StageBatch([dict(plan=p, c=ud, out=s_out, gamma=1.0, dt=dt)]).run(use_graph=False)
+    torch.cuda.synchronize()
+    # out = gamma * fma(dt, f, c) with gamma = 1: compare with fma(dt, f, c) from the plan's f (bit for bit)
+    f = to_host(out)
+    c = to_host(ud)
+    got = to_host(s_out)
+    assert np.allclose(got, c + dt * f, rtol=0, atol=4 * np.spacing(np.abs(c) + dt * np.abs(f)).max())
+    assert deo.device_status() == 0

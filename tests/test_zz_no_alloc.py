@@ -119,3 +119,22 @@ def test_noalloc_calls_leave_free_device_memory_unchanged(cuda):
     for a, b in zip(outs_new, outs_ref):
         assert torch.equal(a, b)
     assert torch.cuda.mem_get_info()[0] == free0
+
+
+def test_noalloc_refuses_stream_capture(cuda):
+    """Under stream capture the call enqueues nothing and returns
+    DEO_ERR_UNSUPPORTED; the capture stays valid and the entry point usable."""
+    import torch
+    plans, us, outs_ref, outs_new, arr, ref = _setup(0)
+    lib = deo.lib()
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        st = lib.deo_batch_apply_noalloc(len(plans), arr, 0, 0, C.c_void_p(s.cuda_stream))
+    assert st == 3  # DEO_ERR_UNSUPPORTED
+    assert b"stream capture" in lib.deo_last_error()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.deo_batch_apply_noalloc(len(plans), arr, 0, 0, stream) == 0
+    torch.cuda.synchronize()
+    for a, b in zip(outs_new, outs_ref):
+        assert torch.equal(a, b)
