@@ -142,4 +142,14 @@ __device__ __forceinline__ T shell_band(const UniTerm& ut, int H, const T* __res
     return r;
 }
 
+// The same with the radius known at compile time: exactly 2H + 1 taps.
+template <typename T, int H>
+__device__ __forceinline__ T shell_band_h(const UniTerm& ut, const T* __restrict__ p, int64_t s) {
+    const T* q = p - H * s;
+    T r = T(0);
+#pragma unroll
+    for (int k = 0; k <= 2 * H; ++k) r = fma(uni_w<T>(ut, k), ldv(q + k * s), r);
+    return r;
+}
+
 }  // namespace deo

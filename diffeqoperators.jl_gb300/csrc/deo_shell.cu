@@ -6,6 +6,8 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "deo_ptx.cuh"
 #include "deo_rows.cuh"
@@ -112,8 +114,9 @@ struct FaceGrid {
 // The terms of a face point other than the face's own axis A, added into
 // acc in axis order around the A term `va` (the generic evaluator's order):
 // a band from the box, or (at edges and corners of the shell) the other
-// axis's boundary row, from the box when its points lie in it.
-template <typename T, int NT, int MAXW>
+// axis's boundary row, from the box when its points lie in it.  HB: the
+// band radius when known at compile time (0: U.radius).
+template <typename T, int NT, int MAXW, int HB>
 __device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, const T* __restrict__ pc, int A, T va,
                                       const int (&c)[3], const int (&org)[3], const int (&bd)[3],
                                       const int64_t (&sb)[3], const T* __restrict__ u, int64_t gidx,
@@ -127,7 +130,8 @@ __device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, cons
         } else {
             const int ib = c[b] + 1;
             if (ib >= U.t[b].flo && ib <= U.t[b].fhi) {
-                v = shell_band<T>(U.t[b], U.radius, pc, 0, sb[b]);
+                if constexpr (HB > 0) v = shell_band_h<T, HB>(U.t[b], pc, sb[b]);
+                else v = shell_band<T>(U.t[b], U.radius, pc, 0, sb[b]);
             } else {
                 const ShellTerm& SB = S[b];
                 const bool low = ib <= SB.nlo;
@@ -144,7 +148,7 @@ __device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, cons
     return zero_fix(acc);
 }
 
-template <typename T, int NT, int MAXW>
+template <typename T, int NT, int MAXW, int HB>
 __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMap m0,
                                               const __grid_constant__ CUtensorMap m1,
                                               const __grid_constant__ CUtensorMap m2,
@@ -247,7 +251,7 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
                 const T va = row_eval<T, MAXW>(R, line, ls, L2, gl, gr);
                 const int64_t gidx = g0 + (int64_t)c[A] * gst[A];
                 const T* pc = box0 + (int64_t)c[A] * sb[A];
-                const T tot = face_sum<T, NT, MAXW>(S, U, pc, A, va, c, org, bd, sb, u, gidx, gst);
+                const T tot = face_sum<T, NT, MAXW, HB>(S, U, pc, A, va, c, org, bd, sb, u, gidx, gst);
                 du[gidx] = ow ? tot : tot + du[gidx];
             }
         }
@@ -506,30 +510,38 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
         if (e) return e;
     }
     if (NT < 3) maps[2] = maps[0];
-    static size_t smem_set = 0;
-    if (smem_max > smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_face<T, NT, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_face<T, NT, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-        // the interior kernels run with the largest shared-memory carveout; asking for the same lets this
-        // kernel's CTAs share their SMs
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_face<T, NT, 8>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_face<T, NT, 16>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                     (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return (int)e;
-        smem_set = smem_max;
-    }
     const unsigned grid = (unsigned)(small ? std::min(cta, deo_k_num_sms()) : cta);
-    if (sp->maxw <= 8)
-        k_face<T, NT, 8><<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev,
-                                                                    (const T*)u, (T*)du, ow);
-    else
-        k_face<T, NT, 16><<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev,
-                                                                     (const T*)u, (T*)du, ow);
-    return (int)cudaGetLastError();
+    auto go = [&](auto kernel) -> int {
+        // the dynamic shared memory each instantiation was last allowed (the instantiations share one
+        // function type, so they are told apart by address)
+        static std::mutex mu;
+        static std::map<const void*, size_t> smem_set;
+        std::lock_guard<std::mutex> lk(mu);
+        size_t& set = smem_set[reinterpret_cast<const void*>(kernel)];
+        if (smem_max > set) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+            // the interior kernels run with the largest shared-memory carveout; asking for the same lets
+            // this kernel's CTAs share their SMs
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+            if (e != cudaSuccess) return (int)e;
+            set = smem_max;
+        }
+        kernel<<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u,
+                                                          (T*)du, ow);
+        return (int)cudaGetLastError();
+    };
+    // rows and ghost maps of at most 8 points with the band radius known at compile time; else general
+    if (sp->maxw <= 8) {
+        switch (up->radius) {
+            case 1: return go(k_face<T, NT, 8, 1>);
+            case 2: return go(k_face<T, NT, 8, 2>);
+            case 3: return go(k_face<T, NT, 8, 3>);
+            case 4: return go(k_face<T, NT, 8, 4>);
+        }
+    }
+    return go(k_face<T, NT, 16, 0>);
 }
 
 // The shell's index space: the points of the array outside the box
