@@ -109,15 +109,44 @@ struct FaceGrid {
     int orgA[3][2];            // box origin along A for the low / high end
     int box[3][3];             // box dims (x, y, z) of face A
     int box_bytes[3];
+    int nbuf;                  // box buffers: 2 = the next tile's copy in flight while a tile is computed
+    int slot;                  // bytes per buffer (a multiple of 128)
 };
+
+// Tile blk of the face grid: face axis A, end e, its first coordinates
+// (c1, c2) along the two other axes b1 < b2, and its box's origin.
+struct FaceTile {
+    int A, e, c1, c2, o0, o1, o2;
+};
+__device__ __forceinline__ FaceTile face_tile_at(const FaceGrid& G, int blk) {
+    FaceTile f;
+    const int A = blk < G.cta0[1] ? 2 : (blk < G.cta0[2] ? 1 : 0);
+    const int local = blk - G.cta0[2 - A];
+    const int per_end = G.tiles1[A] * G.tiles2[A];
+    const int e = local / per_end;
+    const int rem = local - e * per_end;
+    const int tt2 = rem / G.tiles1[A], tt1 = rem - tt2 * G.tiles1[A];
+    f.A = A;
+    f.e = e;
+    f.c1 = G.r1[A] + tt1 * G.tw1[A];
+    f.c2 = G.r2[A] + tt2 * G.tw2[A];
+    // box origin: along A the end's origin; along b1 < b2 the tile less the halo
+    const int oA = G.orgA[A][e];
+    f.o0 = A == 0 ? oA : f.c1 - G.halo[0];
+    f.o1 = A == 1 ? oA : (A == 0 ? f.c1 - G.halo[1] : f.c2 - G.halo[1]);
+    f.o2 = A == 2 ? oA : f.c2 - G.halo[2];
+    return f;
+}
 
 // The terms of a face point other than the face's own axis A, added into
 // acc in axis order around the A term `va` (the generic evaluator's order):
 // a band from the box, or (at edges and corners of the shell) the other
 // axis's boundary row, from the box when its points lie in it.  HB: the
-// band radius when known at compile time (0: U.radius).
-template <typename T, int NT, int MAXW, int HB>
-__device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, const T* __restrict__ pc, int A, T va,
+// band radius when known at compile time (0: U.radius).  A is a template
+// parameter so that every coordinate array is indexed by constants and
+// stays in registers.
+template <typename T, int NT, int MAXW, int HB, int A>
+__device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, const T* __restrict__ pc, T va,
                                       const int (&c)[3], const int (&org)[3], const int (&bd)[3],
                                       const int64_t (&sb)[3], const T* __restrict__ u, int64_t gidx,
                                       const int64_t (&gst)[3]) {
@@ -148,86 +177,32 @@ __device__ __forceinline__ T face_sum(const ShellTerm* S, const UniPlan& U, cons
     return zero_fix(acc);
 }
 
-template <typename T, int NT, int MAXW, int HB>
-__global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMap m0,
-                                              const __grid_constant__ CUtensorMap m1,
-                                              const __grid_constant__ CUtensorMap m2,
-                                              const __grid_constant__ FaceGrid G, const __grid_constant__ UniPlan U,
-                                              const ShellPlan* __restrict__ SPg, const T* __restrict__ u,
-                                              T* __restrict__ du, int ow) {
-    static_assert(sizeof(ShellTerm) % 8 == 0, "ShellTerm copied in 8-byte words");
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(16) ShellTerm S[NT];
-    __shared__ __align__(8) uint64_t mbar;
-    if (threadIdx.x == 0) {
-        mbar_init(&mbar, 1);
-        fence_mbar_init();
-    }
-    {
-        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(SPg->t);
-        unsigned long long* dst = reinterpret_cast<unsigned long long*>(S);
-        for (int q = threadIdx.x; q < (int)(NT * sizeof(ShellTerm) / 8); q += blockDim.x) dst[q] = __ldg(src + q);
-    }
-    __syncthreads();
-    const T* box = reinterpret_cast<const T*>(smem);
-    const int64_t nx = G.n[0], sxy = (int64_t)G.n[0] * G.n[1];
-    const int64_t gst[3] = {1, nx, sxy};
-    // tiles blockIdx.x, + gridDim.x, ...: one box each; the mbarrier's phase flips per tile
-    uint32_t phase = 0;
-    for (int blk = blockIdx.x; blk < G.cta0[3]; blk += gridDim.x, phase ^= 1u) {
-        const int A = blk < G.cta0[1] ? 2 : (blk < G.cta0[2] ? 1 : 0);
-        const int b1 = A == 0 ? 1 : 0, b2 = A == 2 ? 1 : 2;
-        const int local = blk - G.cta0[2 - A];
-        const int per_end = G.tiles1[A] * G.tiles2[A];
-        const int e = local / per_end;
-        const int rem = local - e * per_end;
-        const int tt2 = rem / G.tiles1[A], tt1 = rem - tt2 * G.tiles1[A];
-        const int c1 = G.r1[A] + tt1 * G.tw1[A], c2 = G.r2[A] + tt2 * G.tw2[A];
-        int org[3], bd[3];
-        org[A] = G.orgA[A][e];
-        org[b1] = c1 - G.halo[b1];
-        org[b2] = c2 - G.halo[b2];
-        bd[0] = G.box[A][0];
-        bd[1] = G.box[A][1];
-        bd[2] = G.box[A][2];
-        // test hook: each CTA's first box copy withheld, so that its wait runs out
-        const bool withheld = U.test_withhold > 0 && blk == (int)blockIdx.x;
-        if (threadIdx.x == 0 && !withheld) {
-            mbar_expect_tx(&mbar, (uint32_t)G.box_bytes[A]);
-            tma_load_3d(smem, A == 0 ? &m0 : (A == 1 ? &m1 : &m2), &mbar, org[0], org[1], org[2]);
-        }
-        bool timeout = false;
-        {
-            const unsigned int polls = U.wait_polls ? U.wait_polls : (1u << 22);
-            uint32_t it = 0;
-            while (!mbar_try_wait(&mbar, phase)) {
-                if (++it > polls) {
-                    timeout = true;
-                    break;
-                }
-            }
-        }
-        if (__syncthreads_or(timeout)) {
-            if (threadIdx.x == 0) {
-                atomicOr(&g_deo_shell_status, 1u);
-                if (!withheld)
-                    for (uint32_t it = 0; it < (1u << 22); ++it)  // the copy may still be in flight
-                        if (mbar_try_wait(&mbar, phase)) break;
-            }
-            return;
-        }
+// One face tile from its landed box: one thread per line of the tile along
+// A, the line's ghosts once (the boundary condition's map of its end points,
+// from the box), then its boundary rows at end e, each with the other axes'
+// terms.  (c1, c2): the tile's first coordinates along b1 < b2; org: the
+// box's origin.
+template <typename T, int NT, int MAXW, int HB, int A>
+__device__ __forceinline__ void face_tile(const ShellTerm* S, const UniPlan& U, const FaceGrid& G,
+                                          const T* __restrict__ box, const T* __restrict__ u, T* __restrict__ du,
+                                          int ow, int e, int c1, int c2, int o0, int o1, int o2) {
+    if constexpr (A < NT) {
+        constexpr int b1 = A == 0 ? 1 : 0, b2 = A == 2 ? 1 : 2;
+        const int org[3] = {o0, o1, o2};
+        const int bd[3] = {G.box[A][0], G.box[A][1], G.box[A][2]};
+        const int64_t nx = G.n[0], sxy = (int64_t)G.n[0] * G.n[1];
+        const int64_t gst[3] = {1, nx, sxy};
         const int64_t sb[3] = {1, bd[0], (int64_t)bd[0] * bd[1]};
         const ShellTerm& SA = S[A];
         const int nrows = e ? SA.nhi : SA.nlo;
         const int cA0 = e ? SA.len - SA.nhi : 0;
         const int tw1 = G.tw1[A], tw2 = G.tw2[A];
+        const int e1 = G.e1[A], e2 = G.e2[A];
         const int L2 = SA.len + 2;
-        // one thread per line of the tile along A: the line's ghosts once (the boundary condition's
-        // map of its end points, from the box), then its nrows boundary rows, each with the other
-        // axes' terms
+        const int row0 = e ? SA.nlo : 0;
         bool need_l = false, need_r = false;
         for (int r = 0; r < nrows; ++r) {
-            const ShellRow& R = SA.row[(e ? SA.nlo : 0) + r];
+            const ShellRow& R = SA.row[row0 + r];
             need_l |= R.p0 == 1;
             need_r |= R.p0 + R.nk - 1 == L2;
         }
@@ -238,7 +213,7 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
             c[A] = 0;
             c[b1] = c1 + p1;
             c[b2] = c2 + p2;
-            if (c[b1] >= G.e1[A] || c[b2] >= G.e2[A]) continue;
+            if (c[b1] >= e1 || c[b2] >= e2) continue;
             const int64_t g0 = c[0] + c[1] * nx + (int64_t)c[2] * sxy;  // the line's first point
             const T* box0 = box + (int64_t)(c[2] - org[2]) * sb[2] + (int64_t)(c[1] - org[1]) * sb[1] + (c[0] - org[0]);
             const T* line = line_in_box ? box0 : u + g0;  // position 0 of the line along A
@@ -247,15 +222,95 @@ __global__ void __launch_bounds__(256) k_face(const __grid_constant__ CUtensorMa
             const T gr = need_r ? shell_ghost<T, MAXW>(SA, line, ls, false) : T(0);
             for (int r = 0; r < nrows; ++r) {
                 c[A] = cA0 + r;
-                const ShellRow& R = SA.row[(e ? SA.nlo : 0) + r];
+                const ShellRow& R = SA.row[row0 + r];
                 const T va = row_eval<T, MAXW>(R, line, ls, L2, gl, gr);
                 const int64_t gidx = g0 + (int64_t)c[A] * gst[A];
                 const T* pc = box0 + (int64_t)c[A] * sb[A];
-                const T tot = face_sum<T, NT, MAXW, HB>(S, U, pc, A, va, c, org, bd, sb, u, gidx, gst);
+                const T tot = face_sum<T, NT, MAXW, HB, A>(S, U, pc, va, c, org, bd, sb, u, gidx, gst);
                 du[gidx] = ow ? tot : tot + du[gidx];
             }
         }
-        __syncthreads();  // every thread is done with the box before the next copy overwrites it
+    }
+}
+
+// A persistent grid over the face tiles (tiles blockIdx.x, + gridDim.x, ...),
+// 128 threads per CTA.  With two buffers the next tile's box copy is issued
+// before the current tile is computed; buffer b's mbarrier completes once per
+// use, so its phase is the parity of its use count.
+template <typename T, int NT, int MAXW, int HB>
+__global__ void __launch_bounds__(128, 4) k_face(const __grid_constant__ CUtensorMap m0,
+                                                 const __grid_constant__ CUtensorMap m1,
+                                                 const __grid_constant__ CUtensorMap m2,
+                                                 const __grid_constant__ FaceGrid G, const __grid_constant__ UniPlan U,
+                                                 const ShellPlan* __restrict__ SPg, const T* __restrict__ u,
+                                                 T* __restrict__ du, int ow) {
+    static_assert(sizeof(ShellTerm) % 8 == 0, "ShellTerm copied in 8-byte words");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(16) ShellTerm S[NT];
+    __shared__ __align__(8) uint64_t mbar[2];
+    const int nb = G.nbuf, total = G.cta0[3], stride = (int)gridDim.x;
+    auto issue = [&](int blk, int buf) {
+        const FaceTile f = face_tile_at(G, blk);
+        mbar_expect_tx(&mbar[buf], (uint32_t)G.box_bytes[f.A]);
+        tma_load_3d(smem + buf * G.slot, f.A == 0 ? &m0 : (f.A == 1 ? &m1 : &m2), &mbar[buf], f.o0, f.o1, f.o2);
+    };
+    // test hook: each CTA's first box copy withheld, so that its wait runs out
+    const bool hold0 = U.test_withhold > 0;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+        if ((int)blockIdx.x < total && !hold0) issue(blockIdx.x, 0);  // in flight while the terms are staged
+    }
+    {
+        const unsigned long long* src = reinterpret_cast<const unsigned long long*>(SPg->t);
+        unsigned long long* dst = reinterpret_cast<unsigned long long*>(S);
+        for (int q = threadIdx.x; q < (int)(NT * sizeof(ShellTerm) / 8); q += blockDim.x) dst[q] = __ldg(src + q);
+    }
+    __syncthreads();
+    int i = 0;
+    for (int blk = blockIdx.x; blk < total; blk += stride, ++i) {
+        const int buf = nb == 2 ? (i & 1) : 0;
+        const uint32_t ph = nb == 2 ? ((uint32_t)(i >> 1) & 1u) : ((uint32_t)i & 1u);
+        const int nxt = blk + stride;
+        // the other buffer's last reader (tile i - 1) finished at the barrier closing its iteration
+        if (threadIdx.x == 0) {
+            if (nb == 2) {
+                if (nxt < total) issue(nxt, buf ^ 1);
+            } else if (i > 0) {
+                issue(blk, 0);
+            }
+        }
+        bool timeout = false;
+        {
+            const unsigned int polls = U.wait_polls ? U.wait_polls : (1u << 22);
+            uint32_t it = 0;
+            while (!mbar_try_wait(&mbar[buf], ph)) {
+                if (++it > polls) {
+                    timeout = true;
+                    break;
+                }
+            }
+        }
+        if (__syncthreads_or(timeout)) {
+            if (threadIdx.x == 0) {
+                atomicOr(&g_deo_shell_status, 1u);
+                // the copies that may still be in flight: this tile's (unless withheld), the next tile's
+                if (!(hold0 && i == 0))
+                    for (uint32_t it = 0; it < (1u << 22); ++it)
+                        if (mbar_try_wait(&mbar[buf], ph)) break;
+                if (nb == 2 && nxt < total)
+                    for (uint32_t it = 0; it < (1u << 22); ++it)
+                        if (mbar_try_wait(&mbar[buf ^ 1], (uint32_t)((i + 1) >> 1) & 1u)) break;
+            }
+            return;
+        }
+        const FaceTile f = face_tile_at(G, blk);
+        const T* box = reinterpret_cast<const T*>(smem + buf * G.slot);
+        if (f.A == 0) face_tile<T, NT, MAXW, HB, 0>(S, U, G, box, u, du, ow, f.e, f.c1, f.c2, f.o0, f.o1, f.o2);
+        else if (f.A == 1) face_tile<T, NT, MAXW, HB, 1>(S, U, G, box, u, du, ow, f.e, f.c1, f.c2, f.o0, f.o1, f.o2);
+        else face_tile<T, NT, MAXW, HB, 2>(S, U, G, box, u, du, ow, f.e, f.c1, f.c2, f.o0, f.o1, f.o2);
+        __syncthreads();  // every thread is done with the box before a later copy overwrites it
     }
 }
 
@@ -430,10 +485,10 @@ static int64_t shell_grid(K kernel, int64_t total) {
 
 // Face grid and the three tensor maps; returns cudaErrorNotSupported when a
 // box would exceed the TMA / shared-memory limits (the caller falls back).
-// small: one persistent 128-thread CTA per SM over 32 x 8 tiles (16 x 8 on the
-// x faces), launched before the Float64 interior kernel so that it holds its
-// place on every SM beside the interior's CTAs; else 256 threads, one CTA per
-// 32 x 32 tile.
+// small: one persistent CTA per SM over 32 x 8 tiles (16 x 8 on the x faces),
+// one box buffer, small enough to run beside the Float64 interior kernel's
+// CTAs; else 32 x 8 tiles, two box buffers and as many persistent CTAs as fit
+// on the device.  128 threads per CTA either way.
 template <typename T, int NT>
 static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* sp_dev, const void* u, void* du, int ow,
                        cudaStream_t st, bool small) {
@@ -468,7 +523,7 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
         range(b1, G.r1[A], G.e1[A]);
         range(b2, G.r2[A], G.e2[A]);
         G.tw1[A] = std::min(small && b1 == 1 ? 16 : 32, G.e1[A] - G.r1[A]);
-        G.tw2[A] = (b2 < NT) ? std::min(small ? 8 : 32, G.e2[A] - G.r2[A]) : 1;
+        G.tw2[A] = (b2 < NT) ? std::min(8, G.e2[A] - G.r2[A]) : 1;
         G.tiles1[A] = (G.e1[A] - G.r1[A] + G.tw1[A] - 1) / G.tw1[A];
         G.tiles2[A] = (G.e2[A] - G.r2[A] + G.tw2[A] - 1) / G.tw2[A];
         // box along A: the points both ends' rows read
@@ -498,7 +553,10 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
     }
     G.cta0[3] = cta;
     if (cta == 0) return 0;
-    if (smem_max > 200 * 1024) return (int)cudaErrorNotSupported;
+    G.nbuf = small ? 1 : 2;
+    G.slot = (int)((smem_max + 127) / 128 * 128);
+    const size_t dyn = (size_t)G.nbuf * G.slot;
+    if (dyn > 200 * 1024) return (int)cudaErrorNotSupported;
     alignas(64) CUtensorMap maps[3];
     for (int A = 0; A < 3; ++A) {
         if (A >= NT) {
@@ -510,26 +568,32 @@ static int face_launch(const UniPlan* up, const ShellPlan* sp, const ShellPlan* 
         if (e) return e;
     }
     if (NT < 3) maps[2] = maps[0];
-    const unsigned grid = (unsigned)(small ? std::min(cta, deo_k_num_sms()) : cta);
     auto go = [&](auto kernel) -> int {
-        // the dynamic shared memory each instantiation was last allowed (the instantiations share one
-        // function type, so they are told apart by address)
+        // per instantiation (told apart by address: they share one function type) the dynamic shared
+        // memory it was last allowed, and its resident CTAs per SM for a given dynamic size
         static std::mutex mu;
         static std::map<const void*, size_t> smem_set;
+        static std::map<std::pair<const void*, size_t>, int> per_sm;
         std::lock_guard<std::mutex> lk(mu);
-        size_t& set = smem_set[reinterpret_cast<const void*>(kernel)];
-        if (smem_max > set) {
-            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        const void* key = reinterpret_cast<const void*>(kernel);
+        size_t& set = smem_set[key];
+        if (dyn > set) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
             // the interior kernels run with the largest shared-memory carveout; asking for the same lets
             // this kernel's CTAs share their SMs
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                          (int)cudaSharedmemCarveoutMaxShared);
             if (e != cudaSuccess) return (int)e;
-            set = smem_max;
+            set = dyn;
         }
-        kernel<<<grid, small ? 128 : 256, smem_max, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u,
-                                                          (T*)du, ow);
+        int& occ = per_sm[{key, dyn}];
+        if (occ == 0) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 128, dyn) != cudaSuccess || occ < 1)
+                occ = 1;
+        }
+        const unsigned grid = (unsigned)std::min(cta, (small ? 1 : occ) * deo_k_num_sms());
+        kernel<<<grid, 128, dyn, st>>>(maps[0], maps[1], maps[2], G, *up, sp_dev, (const T*)u, (T*)du, ow);
         return (int)cudaGetLastError();
     };
     // rows and ghost maps of at most 8 points with the band radius known at compile time; else general
