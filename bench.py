@@ -164,6 +164,34 @@ def barrier(ws):
         dist.barrier()
 
 
+def host_link_gbs(h_in, h_out, reps: int = 6) -> float:
+    """GB/s each way of the host link with a host->device and a
+    device->host copy of these pinned buffers in flight at once (two streams,
+    the copy engines), as the pipelined host applies move them: the bound on
+    the end-to-end throughput."""
+    import torch
+    d_in = torch.empty_like(h_in, device="cuda")
+    d_out = torch.empty_like(h_out, device="cuda")
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def both():
+        with torch.cuda.stream(s1):
+            d_in.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+
+    for _ in range(2):
+        both()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        both()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / reps
+    del d_in, d_out
+    return h_in.numel() * h_in.element_size() / dt / 1e9
+
+
 def max_over_ranks(x: float, ws: int) -> float:
     if ws == 1:
         return x
@@ -326,6 +354,7 @@ def run_ours(args, ws, rank):
     dev_out = dus[(args.steps - 1) % nbuf].permute(2, 1, 0).contiguous().view(-1).cpu()
     if not torch.equal(dev_out, dh):
         raise RuntimeError("host-buffer path disagrees with the device path")
+    link = host_link_gbs(uh, dh)  # the copies alone, both directions at once (overwrites dh)
 
     hbm, peak_kind = peaks()
     alg_bytes = 2 * esize * npts
@@ -372,7 +401,10 @@ def run_ours(args, ws, rank):
         "e2e": {"value": ws * npts / e2e_s, "unit": "grid-pts/s", "h2d_bytes_per_step": npts * esize,
                 "d2h_bytes_per_step": npts * esize,
                 "path": "deo_apply_host_async + deo_plan_host_sync (C ABI, pinned host buffers, copies overlapped "
-                        "with the applies of neighbouring steps)"},
+                        "with the applies of neighbouring steps)",
+                # the host link with both copies in flight: each step moves npts * esize each way
+                "host_link_gbs_each_way": link, "link_bound": ws * link * 1e9 / esize,
+                "frac_of_link_bound": (npts / e2e_s) / (link * 1e9 / esize)},
         "gpu_launches": args.steps * len(kernels),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "kernel": kernels[0], "peak_source": f"{peak_kind} hbm_gbs (burst copy)",

@@ -7,7 +7,7 @@
 // which the GB300's FP64 rate (1.68 per clock per SM) caps far below the HBM
 // bound.  This kernel evaluates a point with integer instructions only:
 //
-//  * A CTA owns a 64 x 16 tile of (x, y) and streams z-planes of the tile plus
+//  * A CTA owns a 32 x 16 tile of (x, y) and streams z-planes of the tile plus
 //    its halo through a ring of P shared-memory slots with TMA.
 //  * When plane p lands, the CTA takes the largest biased exponent E_p over
 //    the plane tile (its own points and the x/y halo strips the stencil reads)
@@ -48,20 +48,21 @@ namespace deo {
 
 template <int H>
 struct BfxCfg {
-    static constexpr int TXT = 32, TYT = 8, NTHR = TXT * TYT;
+    static constexpr int TXT = 16, TYT = 8, NTHR = TXT * TYT;
     static constexpr int RX = 2, RY = 2;
-    static constexpr int TX = TXT * RX, TY = TYT * RY;          // 64 x 16 points per tile
+    static constexpr int TX = TXT * RX, TY = TYT * RY;          // 32 x 16 points per tile
     static constexpr int HR = H <= 2 ? 2 : 4;                    // x halo in doubles: >= H, a 16-byte multiple
     static constexpr int BX = TX + 2 * HR, BY = TY + 2 * H;
     static constexpr int PLANE = BX * BY;
     static constexpr int PLANE_BYTES = PLANE * 8;
     static constexpr int SLOT = ((PLANE_BYTES + 127) / 128) * 128;
-    static constexpr int LOOK = 2;                               // planes in flight beyond the next one
+    static constexpr int LOOK = 1;                               // planes in flight beyond the next one
+    // 128 threads, 7 slots of 5.6 KB and at most 96 registers: five CTAs per SM
     static constexpr int P = 2 * H + 2 + LOOK;                   // ring slots
     static constexpr int NHX = 2 * H * TY, NHY = 2 * H * TX;     // halo strips (no corners: a star stencil)
     static constexpr int NHALO = NHX + NHY;
     static constexpr int HPT = (NHALO + NTHR - 1) / NTHR;        // halo values per thread
-    static constexpr int QCAP = 256;                             // fallback queue entries per buffer
+    static constexpr int QCAP = 128;                             // fallback queue entries per buffer
     static constexpr int SMEM = P * SLOT;
     static constexpr int G0 = 7;
 };
@@ -188,7 +189,7 @@ __device__ __forceinline__ bool bfx_round(long long hi, unsigned long long lo, i
 }
 
 template <int H, bool CNEG>
-__global__ void __launch_bounds__(256, 2) k_lap_bfx(const __grid_constant__ CUtensorMap tmap,
+__global__ void __launch_bounds__(128, 5) k_lap_bfx(const __grid_constant__ CUtensorMap tmap,
                                                     const __grid_constant__ UniPlan U, const LapGrid g,
                                                     const double* __restrict__ u, double* __restrict__ du,
                                                     int overwrite) {

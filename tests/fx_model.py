@@ -123,9 +123,9 @@ def exact_point(u: np.ndarray, idx: tuple, w, H: int, nt: int):
 
 
 # ---------------------------------------------------------------------------
-# Block fixed point (k_lap_bfx): one exponent per (64 x 16 tile, z-plane)
+# Block fixed point (k_lap_bfx): one exponent per (32 x 16 tile, z-plane)
 # ---------------------------------------------------------------------------
-BFX_TX, BFX_TY, BFX_G0 = 64, 16, 7
+BFX_TX, BFX_TY, BFX_G0 = 32, 16, 7
 
 
 def bfx_weights(w, H: int):
