@@ -543,6 +543,13 @@ def run_nonuniform2d(args):
     res["fused_merged_ms"] = tm * 1e3
     res["fused_merged_terms"] = pm.evaluated_terms
     res["fused_merged_max_rel_diff"] = float((om - outs[1]).abs().max() / outs[1].abs().max())
+    # and DEO_PLAN_FACTOR_FIELD: the upwind term as a(x, y) * (sum of its taps), one multiply per point
+    pf = deo.plan_for(ops, (n, n), 0, merge_terms=True, factor_field=True)
+    of = deo.julia_array((n, n))
+    tf = _event_time(lambda: pf.apply(ud, of), args.steps, args.warmup)
+    torch.cuda.synchronize()
+    res["fused_merged_factored_ms"] = tf * 1e3
+    res["fused_merged_factored_max_rel_diff"] = float((of - outs[1]).abs().max() / outs[1].abs().max())
     return res
 
 

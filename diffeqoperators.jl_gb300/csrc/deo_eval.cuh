@@ -110,6 +110,18 @@ __device__ __forceinline__ T row_w(const RowTabDev& tb, const RowInfo& r, int k)
     return r.band ? band_w<T>(tb, k) : __ldg(reinterpret_cast<const T*>(tb.W) + (int64_t)k * tb.nexp + r.e);
 }
 
+// !(c >= 0) -- c negative (not -0) or NaN: the upwind operator's variant
+// choice (convolutions.jl:134), tested on the bits so that it issues no FP64
+// (Float32) comparison.
+__device__ __forceinline__ bool not_nonneg(double c) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(c);
+    return ((long long)b < 0 && (b << 1) != 0ULL) || (b << 1) > 0xFFE0000000000000ULL;
+}
+__device__ __forceinline__ bool not_nonneg(float c) {
+    const unsigned b = __float_as_uint(c);
+    return ((int)b < 0 && (b << 1) != 0u) || (b << 1) > 0xFF000000u;
+}
+
 // Coefficient and table variant of row i on the line starting at `base`.
 template <typename T>
 __device__ __forceinline__ const RowTabDev& row_variant(const TermDev& t, int64_t base, int i, T& c) {
@@ -117,7 +129,7 @@ __device__ __forceinline__ const RowTabDev& row_variant(const TermDev& t, int64_
     if (!t.has_field) return t.tab[0];
     const int ci = row_cidx(t.tab[0], i);
     c = __ldg(reinterpret_cast<const T*>(t.field) + base + (int64_t)(ci - 1) * t.stride);
-    if (t.nvar == 2 && !(c >= T(0))) return t.tab[1];
+    if (t.nvar == 2 && not_nonneg(c)) return t.tab[1];
     return t.tab[0];
 }
 
@@ -137,7 +149,10 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
         // band row away from the ghosts: straight tap loop (same order and rounding)
         const T* __restrict__ xp = line + (int64_t)(r.p0 - 2) * s;
         T acc = T(0);
-        if (t.has_field) {
+        if (t.has_field == 2) {  // DEO_PLAN_FACTOR_FIELD: c * (sum_k w_k x_k)
+            for (int k = 0; k < r.nk; ++k) acc = fma(band_w<T>(tb, k), __ldg(xp + (int64_t)k * s), acc);
+            acc = c * acc;
+        } else if (t.has_field) {
             for (int k = 0; k < r.nk; ++k) acc = fma(c * band_w<T>(tb, k), __ldg(xp + (int64_t)k * s), acc);
         } else {
             for (int k = 0; k < r.nk; ++k) acc = fma(band_w<T>(tb, k), __ldg(xp + (int64_t)k * s), acc);
@@ -152,7 +167,10 @@ __device__ __forceinline__ T eval_term(const TermDev& t, const T* __restrict__ u
         return (p == 1) ? gl : (p == L2 ? gr : __ldg(line + (int64_t)(p - 2) * s));
     };
     T acc = T(0);
-    if (t.has_field) {
+    if (t.has_field == 2) {
+        for (int k = 0; k < r.nk; ++k) acc = fma(row_w<T>(tb, r, k), tap(k), acc);
+        acc = c * acc;
+    } else if (t.has_field) {
         for (int k = 0; k < r.nk; ++k) acc = fma(c * row_w<T>(tb, r, k), tap(k), acc);
     } else {
         for (int k = 0; k < r.nk; ++k) acc = fma(row_w<T>(tb, r, k), tap(k), acc);

@@ -1220,7 +1220,7 @@ extern "C" deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_
             T.div_stride = make_fastdiv((uint32_t)stride);
             T.div_len = make_fastdiv((uint32_t)A.len);
         }
-        T.has_field = tm.coeff_field != nullptr;
+        T.has_field = tm.coeff_field != nullptr ? ((flags & DEO_PLAN_FACTOR_FIELD) ? 2 : 1) : 0;
         T.field = tm.coeff_field;
         T.nvar = (T.has_field && A.wind) ? 2 : 1;
         std::vector<int> rlo(A.len + 2, A.len + 1), rhi(A.len + 2, 0);

@@ -57,7 +57,7 @@ struct TermDev {
     FastDiv div_stride;  // valid when PlanDev::fastdiv
     FastDiv div_len;
     int nvar;            // 1, or 2 for an upwind operator with a coefficient field (c>=0 / c<0)
-    int has_field;
+    int has_field;       // 0: none; 1: row i = sum_k (c_i w_k) u_k; 2: c_i * sum_k w_k u_k (forward)
     const void* field;   // coefficient field (same shape/dtype as u) or null
     RowTabDev tab[2];
     // adjoint: rows touching padded column p (1..len+2) lie in [rlo[p-1], rhi[p-1]]

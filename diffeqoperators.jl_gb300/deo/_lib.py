@@ -26,6 +26,7 @@ DEO_OPT_SHELL_KERNEL = 9
 DEO_OPT_F32_TILE = 10
 DEO_PLAN_MERGE_TERMS = 1
 DEO_PLAN_STAR = 2
+DEO_PLAN_FACTOR_FIELD = 4
 DEO_MAX_BC = 16
 
 _dp = C.POINTER(C.c_double)

@@ -755,7 +755,8 @@ class Plan:
     """A compiled deo_plan for (terms, Julia size, dtype)."""
 
     def __init__(self, ghosts: Sequence[GhostDerivativeOperator], shape: Sequence[int], dtype_code: int,
-                 path: int = L.DEO_PATH_AUTO, merge_terms: bool = False, star: bool = False):
+                 path: int = L.DEO_PATH_AUTO, merge_terms: bool = False, star: bool = False,
+                 factor_field: bool = False):
         nd = len(shape)
         terms = (Term * len(ghosts))()
         self._keep = []
@@ -795,7 +796,8 @@ class Plan:
                 terms[i].coeff_field = None
         sizes = (C.c_int64 * nd)(*self.shape)
         h = C.c_void_p()
-        flags = (L.DEO_PLAN_MERGE_TERMS if merge_terms else 0) | (L.DEO_PLAN_STAR if star else 0)
+        flags = ((L.DEO_PLAN_MERGE_TERMS if merge_terms else 0) | (L.DEO_PLAN_STAR if star else 0) |
+                 (L.DEO_PLAN_FACTOR_FIELD if factor_field else 0))
         check(L.lib().deo_plan_create_opts(nd, sizes, dtype_code, len(ghosts), terms, flags, C.byref(h)))
         self._h = h
         self._ops = [g.L for g in ghosts]  # keep operators alive
@@ -955,13 +957,14 @@ class Plan:
 _plan_cache: dict = {}
 
 
-def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO, merge_terms: bool = False) -> Plan:
+def plan_for(ghosts, shape, dtype_code, path=L.DEO_PATH_AUTO, merge_terms: bool = False,
+             factor_field: bool = False) -> Plan:
     key = (tuple(id(g) for g in ghosts), tuple(shape), dtype_code, path,
-           tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts), merge_terms)
+           tuple(g.field.data_ptr() if g.field is not None else 0 for g in ghosts), merge_terms, factor_field)
     versions = tuple(g.L._version for g in ghosts)
     p = _plan_cache.get(key)
     if p is None or p._versions != versions:  # a plan of earlier coefficient values is replaced
-        p = Plan(ghosts, shape, dtype_code, path, merge_terms)
+        p = Plan(ghosts, shape, dtype_code, path, merge_terms, factor_field=factor_field)
         p._versions = versions
         # keep the ghosts alive with the plan so ids stay unique
         p._ghosts = list(ghosts)

@@ -200,6 +200,15 @@ deo_status deo_plan_create(int ndims, const int64_t* sizes, deo_dtype dtype, int
  *     the TMA path keep their interior kernels).  Rounding differs from the
  *     reference's term-by-term sums, within the same bar. */
 #define DEO_PLAN_STAR 2
+/*   DEO_PLAN_FACTOR_FIELD: a term with a coefficient field c(x) evaluates
+ *     row i as c_i * (sum_k w_k u_k) -- the taps summed first, one multiply
+ *     by the field value after -- instead of the reference's
+ *     sum_k (c_i w_k) u_k (convolutions.jl:47, :140): one FP64 (Float32)
+ *     multiply per point instead of one per tap.  Forward applies of the
+ *     generic, batched and Runge-Kutta stage kernels; the adjoint and the
+ *     concretisation keep c_i w_k.  Rounding differs from the reference's
+ *     order, within the same 4 ulp of sum |c_k u_k|. */
+#define DEO_PLAN_FACTOR_FIELD 4
 deo_status deo_plan_create_opts(int ndims, const int64_t* sizes, deo_dtype dtype, int nterms, const deo_term* terms,
                                 int flags, deo_plan** out);
 /* Frees the plan's device tables, streams and events (cudaFree waits for the device). */

@@ -72,6 +72,10 @@ def test_nonuniform_2048_fused_and_per_operator_against_oracle(cuda):
     assert pm.evaluated_terms == 3
     pm.apply(ud, out)
     worst["fused_merged"] = _ulps(to_host(out), ref, O.abs_scale(oterms, u))
+    # and the upwind term's field factored out of its tap sum (DEO_PLAN_FACTOR_FIELD)
+    pf = deo.plan_for(ops, (n, n), 0, merge_terms=True, factor_field=True)
+    pf.apply(ud, out)
+    worst["fused_merged_factored"] = _ulps(to_host(out), ref, O.abs_scale(oterms, u))
     assert deo.device_status() == 0
     _report("parity_nonuniform2d_2048", {"max_ulp_of_scale": worst})
     assert max(worst.values()) <= 4.0, worst
