@@ -295,6 +295,8 @@ def run_ours(args, ws, rank):
         plan.set_option(deo.DEO_OPT_EXACT_SUMS, args.exact_sums)
     if getattr(args, "serial_shell", False):
         plan.set_option(deo.DEO_OPT_CONCURRENT_SHELL, 0)
+    if getattr(args, "f32_scalar", False):
+        plan.set_option(deo.DEO_OPT_F32_VECTOR, 0)
     esize = 8 if dtype_name == "f64" else 4
     npts = n ** 3
     u_host = fourier_field(n, seed=SEED + rank, dtype=np.float64 if esize == 8 else np.float32)
@@ -310,7 +312,8 @@ def run_ours(args, ws, rank):
     # execution choices (tile shape, shell kernel, shell beside the interior or after it), all
     # bit-identical: timed on this workload by the library's autotuner before the warm-up
     tuned = None
-    if not getattr(args, "no_autotune", False) and not getattr(args, "serial_shell", False):
+    if not (getattr(args, "no_autotune", False) or getattr(args, "serial_shell", False) or
+            getattr(args, "f32_scalar", False)):
         tuned = plan.autotune(us[0], dus[0], os.path.join(REPORT_DIR, "plan_autotune.cache") if REPORT_DIR else None)
     for i in range(args.warmup):
         plan.apply(us[i % nbuf], dus[i % nbuf])
@@ -988,6 +991,8 @@ def main():
                     help="plan option DEO_OPT_EXACT_SUMS for the 3-D workload (default: the library's)")
     ap.add_argument("--serial-shell", action="store_true", help="the boundary shell after the interior kernel")
     ap.add_argument("--no-autotune", action="store_true", help="the plan's default execution choices")
+    ap.add_argument("--f32-scalar", action="store_true",
+                    help="Float32: the one-column-per-thread interior (DEO_OPT_F32_VECTOR=0), no autotuning")
     args = ap.parse_args()
     if args.workload in ("batch", "serve"):
         ws, rank, _ = dist_init()

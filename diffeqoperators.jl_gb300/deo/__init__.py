@@ -6,7 +6,7 @@ Neumann0BC, PeriodicBC, MultiDimBC, compose, `L*Q*u`, mul!) and run on the
 CUDA kernels of libdeo.so.  There is no CPU fallback.
 """
 from ._lib import (DEO_OPT_CONCURRENT_SHELL, DEO_OPT_EXACT_SUMS, DEO_OPT_FAST_PATH, DEO_OPT_FX_FP64_ROWS, DEO_OPT_LAUNCH_TIMING, DEO_OPT_TEST_WITHHOLD, DEO_OPT_F32_VECTOR, DEO_OPT_SHELL_KERNEL, DEO_OPT_F32_TILE, DEO_OPT_TMA, DeoArgError, DeoError,  # noqa: F401
-                   DeoShapeError, LIB_PATH, lib)
+                   DEO_PLAN_FACTOR_FIELD, DEO_PLAN_MERGE_TERMS, DEO_PLAN_STAR, DeoShapeError, LIB_PATH, lib)
 
 
 def device_status() -> int:

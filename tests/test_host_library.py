@@ -21,6 +21,17 @@ def header_functions():
     return sorted(set(re.findall(r"\b(deo_[a-z0-9_]+)\s*\(", src)))
 
 
+def test_header_constants_match_the_binding():
+    """Every DEO_PLAN_* and DEO_OPT_* value the header defines is the one the
+    Python binding passes."""
+    src = open(os.path.join(ROOT, "include", "deo.h")).read()
+    defs = dict(re.findall(r"#define\s+(DEO_(?:PLAN|OPT)_[A-Z0-9_]+)\s+(-?\d+)", src))
+    assert "DEO_PLAN_FACTOR_FIELD" in defs and "DEO_OPT_F32_VECTOR" in defs
+    for name, value in defs.items():
+        assert hasattr(_lib, name), name
+        assert getattr(_lib, name) == int(value), name
+
+
 def test_header_symbols_exported():
     lib = ctypes.CDLL(_lib.LIB_PATH)
     names = header_functions()
