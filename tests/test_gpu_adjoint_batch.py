@@ -491,8 +491,9 @@ def test_transposed_fast_path(cuda, case, dtype, sums):
     read only by band rows, k_shell_adj on the rest) against the generic
     transposed kernel: bit for bit in the reference's order (EXACT_SUMS=0;
     Float32), within the 4-ulp bar for the fixed-point interior; overwrite and
-    accumulate (the shell runs after the interior whatever
-    DEO_OPT_CONCURRENT_SHELL says)."""
+    accumulate; the same result whatever DEO_OPT_CONCURRENT_SHELL says (the
+    shell runs after the interior: beside it, one CTA per SM, the column
+    evaluator outlasted the interior)."""
     import torch
     A, oterms, u = build(case, dtype=dtype)
     shape = tuple(case["shape"])
@@ -507,6 +508,7 @@ def test_transposed_fast_path(cuda, case, dtype, sums):
     p.adjoint(v, ref_acc, overwrite=False)
     assert p.kernels == ("k_apply",)
     p.set_option(deo.DEO_OPT_FAST_PATH, 1)
+    outs = {}
     for conc in (1, 0):
         p.set_option(deo.DEO_OPT_CONCURRENT_SHELL, conc)
         o = deo.julia_array(shape, tdt, fill=np.nan)
@@ -514,6 +516,7 @@ def test_transposed_fast_path(cuda, case, dtype, sums):
         assert p.kernels[1] == "k_shell_adj" and p.kernels[0].startswith("k_lap_"), p.kernels
         a = base.clone()
         p.adjoint(v, a, overwrite=False)
+        outs[conc] = (o, a)
         if dtype == "f32" or sums == 0:
             assert torch.equal(o, ref), conc
             assert torch.equal(a, ref_acc), conc
@@ -523,4 +526,6 @@ def test_transposed_fast_path(cuda, case, dtype, sums):
             # the transposed sum's scale: sum_i |A[i, j] v_i|, from the forward operator's abs scale of |v|
             scale = O.abs_scale(oterms, np.abs(vh))
             assert (np.abs(g - r) <= 4 * np.spacing(np.maximum(scale, np.abs(r))) + 1e-300).all()
+    torch.cuda.synchronize()
+    assert torch.equal(outs[1][0], outs[0][0]) and torch.equal(outs[1][1], outs[0][1])
     assert deo.device_status() == 0
