@@ -1,6 +1,6 @@
 // deo_oracle.cpp -- CPU restatement of DiffEqOperators.jl's stencil-apply path.
 //
-// TEST INFRASTRUCTURE ONLY. This file is the checker: the parity tests, the
+// TEST INFRASTRUCTURE ONLY. This file is the oracle: the parity tests, the
 // smoke check and the bench's CPU-baseline leg call it; the product library
 // never links or calls it.
 //
@@ -8,7 +8,7 @@
 // DiffEqOperators.jl source tree) in the reference's own operation order.
 // Build flags disable FMA contraction (-ffp-contract=off) so each `a*b + c`
 // rounds twice, as plain Julia code does; the reference's @turbo loops may
-// contract to FMA and reorder, which is why parity is judged with a tolerance
+// contract to FMA and reorder, which is why parity is checked with a tolerance
 // of 4 ulp of sum|c_k*u_k| per point rather than bit-exactly.
 //
 // Known-unreproducible details (documented, absorbed by the tolerance):
