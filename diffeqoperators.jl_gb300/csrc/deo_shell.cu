@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <utility>
 
 #include "deo_ptx.cuh"
 #include "deo_rows.cuh"
